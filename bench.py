@@ -1,0 +1,388 @@
+"""Benchmark: RK3 cell-updates/s of Enlightning's per-patch time advance on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload pulse512]
+
+Prints one JSON line (rank 0).  A "step" is one SSP-RK3 time step of the whole
+workload (three stages, each: ghost fill, RHS, RK update, update_state,
+absorbing envelope).  value = cell-updates/s = advanced interior cells x K /
+max-over-ranks device time of the K timed steps.  Inputs are synthetic (see
+enlightning_gb300/workloads.py).
+
+--impl reference times the reference's CPU path on this machine's host cores:
+the oracle's line-by-line restatement of the Fortran (no Fortran compiler
+exists on the GPU machine), all host threads, on a bounded sample of the same
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK3 cell-updates/s on 1 GB300: batched+learned vs plain at <=1e-3 rel L2"
+UNIT = "cell-updates/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+# Algorithmic bytes of the RHS kernel per cell and stage: read w_n (5 fields),
+# pressure, temperature, source (8 B each) and write KK (5 fields).
+RHS_BYTES_PER_CELL = (5 + 3 + 5) * 8
+# Algorithmic bytes per RK3 cell-update with ideal fusion (5 FP64 fields):
+# stage 1 reads u^n and writes w1 (80 B), stages 2 and 3 read w, u^n and write
+# (120 B each).
+STEP_BYTES_PER_CELL = 320
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+
+class Pulse512Plain:
+    """Config 1: one 512x512 patch, Gaussian overpressure 0.1 p0, sigma 8 cells,
+    dx = 0.1 m, reflective walls, CFL 0.5, hybrid WENO5/DRP with LLF splitting,
+    advanced through the drop-in F77 entry points (plain FP64 path)."""
+
+    name = "pulse512: 1 patch 512x512, hybrid_high_llf, reflect, CFL 0.5"
+
+    def __init__(self, n=512):
+        import torch
+
+        from enlightning_gb300 import workloads
+        from enlightning_gb300.constants import default_params
+        from enlightning_gb300.strategy import Enlightning, Patch
+
+        self.torch = torch
+        self.prm = default_params()
+        self.n = n
+        self.dx = (0.1, 0.1)
+        self.dt = workloads.pulse_dt(self.prm, self.dx)
+        self.box = (0, n - 1, 0, n - 1)
+        self.w0 = workloads.pulse_patch_state(n, n, self.prm, amp_frac=0.1, sigma_cells=8.0)
+        self.patch = Patch(self.box, (0.0, 0.0), self.dx).allocate()
+        self.strat = Enlightning(self.prm, domain_xhi=(n * self.dx[0], n * self.dx[1]))
+        self.reset()
+        self.cells = n * n
+        self.rhs_events = []
+
+    def reset(self):
+        P = self.patch
+        P.w_scr.copy_(self.torch.from_numpy(self.w0))
+        P.w_cur.copy_(P.interior(P.w_scr))
+        # p, T of the initial state (update_state over the interior; the
+        # ghosts are filled by the boundary fill of every stage)
+        P.pres.fill_(self.prm["p0"])
+        P.temp.fill_(self.prm["T0"])
+        self._eos()
+
+    def _eos(self):
+        from enlightning_gb300 import _lib
+        P, p, L = self.patch, self.prm, self.strat.L
+        I, D = _lib.iref, _lib.dref
+        b = self.box
+        L.update_state_(_lib.darr(P.dx), _lib.darr(P.xlo), I(b[0]), I(b[1]), I(b[2]), I(b[3]), I(3), I(3),
+                        self.strat_ptr(P.w_scr), self.strat_ptr(P.pres), self.strat_ptr(P.temp), D(p["rho0"]),
+                        D(p["c"]), D(p["gamma1"]), D(p["c_p"]), D(p["p0"]), D(p["T0"]), D(p["c_lr"]),
+                        D(p["c_v"]), D(p["R_tilde"]), D(p["M"]), D(p["R"]), I(5))
+
+    @staticmethod
+    def strat_ptr(t):
+        import ctypes as C
+        return C.c_void_p(t.data_ptr())
+
+    def launches_per_step(self):
+        # per stage: 4 edge + 4 node BC fills, rhs, runge_kutta, update_state
+        return 3 * (8 + 3)
+
+    def step(self, timed_rhs=False):
+        P, s = self.patch, self.strat
+        a1s, a2s, bs = s.rk
+        P.interior(P.w_scr).copy_(P.w_cur)
+        for st in range(3):
+            s.set_physical_boundary_conditions(P)
+            self._single_step(P, a1s[st], a2s[st], bs[st], timed_rhs)
+        P.w_cur.copy_(P.interior(P.w_scr))
+
+    def _single_step(self, P, a1, a2, beta, timed_rhs):
+        torch = self.torch
+        s = self.strat
+        if not timed_rhs:
+            s.single_step(P, self.dt, a1, a2, beta)
+            return
+        # identical call sequence; the rhs_ launch is bracketed by events
+        from enlightning_gb300 import _lib
+        L, p, b, g = s.L, s.p, P.box, P.g
+        I, D = _lib.iref, _lib.dref
+        ptr = self.strat_ptr
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        L.rhs_(I(b[0]), I(b[1]), I(b[2]), I(b[3]), I(g), I(g), _lib.darr(P.xlo), _lib.darr(P.dx),
+               ptr(P.w_scr), ptr(P.src), ptr(P.K), ptr(P.pres), ptr(P.temp), D(p["weno_alpha"]), D(p["kappa"]),
+               D(p["mu"]), D(p["muB"]), D(p["R"]), D(p["T_star_n"]), D(p["T_star_o"]), D(p["tau_n"]),
+               D(p["tau_o"]), _lib.darr(p["tol"]), I(P.level), D(p["c"]), D(p["c_lr"]), I(5))
+        e1.record()
+        self.rhs_events.append((e0, e1))
+        L.runge_kutta_(I(b[0]), I(b[1]), I(b[2]), I(b[3]), I(g), I(g), D(self.dt), D(a1), D(a2), D(beta),
+                       ptr(P.w_scr), ptr(P.w_cur), ptr(P.K), I(5))
+        L.update_state_(_lib.darr(P.dx), _lib.darr(P.xlo), I(b[0]), I(b[1]), I(b[2]), I(b[3]), I(g), I(g),
+                        ptr(P.w_scr), ptr(P.pres), ptr(P.temp), D(p["rho0"]), D(p["c"]), D(p["gamma1"]),
+                        D(p["c_p"]), D(p["p0"]), D(p["T0"]), D(p["c_lr"]), D(p["c_v"]), D(p["R_tilde"]),
+                        D(p["M"]), D(p["R"]), I(5))
+        s.set_absorbing_boundary_conditions(P)
+
+    # host-buffer path: state in pinned host memory, copied in and out each step
+    def e2e_setup(self):
+        torch = self.torch
+        P = self.patch
+        self.h_w = torch.empty_like(P.w_cur, device="cpu").pin_memory()
+        self.h_p = torch.empty_like(P.pres, device="cpu").pin_memory()
+        self.h_t = torch.empty_like(P.temp, device="cpu").pin_memory()
+        self.h_w.copy_(P.w_cur)
+        self.h_p.copy_(P.pres)
+        self.h_t.copy_(P.temp)
+        torch.cuda.synchronize()
+        return (self.h_w.numel() + self.h_p.numel() + self.h_t.numel()) * 8
+
+    def e2e_step(self):
+        P = self.patch
+        P.w_cur.copy_(self.h_w, non_blocking=True)
+        P.pres.copy_(self.h_p, non_blocking=True)
+        P.temp.copy_(self.h_t, non_blocking=True)
+        self.step()
+        self.h_w.copy_(P.w_cur, non_blocking=True)
+        self.h_p.copy_(P.pres, non_blocking=True)
+        self.h_t.copy_(P.temp, non_blocking=True)
+
+    def cpu_baseline(self, budget_s=12.0, threads=None):
+        """The oracle (restated Fortran) on this host, all threads, whole patch."""
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as ora
+        threads = threads or os.cpu_count() or 1
+        ora.set_threads(threads)
+        n, dx, prm = self.n, self.dx, self.prm
+        op = ora.Patch(self.box, (0.0, 0.0), dx)
+        op.w_scr[...] = self.w0
+        op.w_cur[...] = op.interior(self.w0)
+        ora.update_state(dx, (0, 0), self.box, (3, 3), op.w_scr, op.pres, op.temp, prm)
+        dom = ((0.0, 0.0), (n * dx[0], n * dx[1]))
+        ora.advance(op, prm, "hybrid_high_llf", self.dt, 1, domain=dom)  # warm-up
+        steps, t0 = 0, time.perf_counter()
+        while True:
+            ora.advance(op, prm, "hybrid_high_llf", self.dt, 1, domain=dom)
+            steps += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s or steps >= 400:
+                break
+        return {"value": self.cells * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"{steps} RK3 steps of the full 512x512 patch ({el:.1f} s)"}
+
+
+WORKLOADS = {"pulse512": Pulse512Plain}
+
+
+# ---------------------------------------------------------------------------
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]
+    # the reference arm needs no GPU: build the workload description only
+    obj = wl.__new__(wl)
+    from enlightning_gb300 import workloads
+    from enlightning_gb300.constants import default_params
+    obj.prm = default_params()
+    obj.n = 512
+    obj.dx = (0.1, 0.1)
+    obj.dt = workloads.pulse_dt(obj.prm, obj.dx)
+    obj.box = (0, 511, 0, 511)
+    obj.w0 = workloads.pulse_patch_state(512, 512, obj.prm, amp_frac=0.1, sigma_cells=8.0)
+    obj.cells = 512 * 512
+    vals = []
+    for _ in range(args.warmup):
+        obj.cpu_baseline(budget_s=2.0)
+    for _ in range(args.steps):
+        vals.append(obj.cpu_baseline(budget_s=6.0))
+    v = float(np.median([x["value"] for x in vals]))
+    cb = dict(vals[-1])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": {"workload": obj.name}, "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    wl = WORKLOADS[args.workload]()
+    hbm_peak, peak_kind = peaks()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(3, args.warmup)):
+        wl.step()
+    barrier()
+    # timed region: per-step CUDA events, L2 flushed between steps (outside the events)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    wl.rhs_events = []
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record()
+            wl.step(timed_rhs=True)
+            ev[k][1].record()
+        barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = wl.cells * args.steps * ws / (ms * 1e-3)
+    rhs_ms = float(np.mean([a.elapsed_time(b) for a, b in wl.rhs_events]))
+    achieved = wl.cells * RHS_BYTES_PER_CELL / (rhs_ms * 1e-3) / 1e9
+
+    # e2e: host buffers in pinned memory, copies inside the timed region
+    nbytes = wl.e2e_setup()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record()
+    for _ in range(args.steps):
+        wl.e2e_step()
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e = {"value": wl.cells * args.steps * ws / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes}
+    if rank != 0:
+        return
+    cb = wl.cpu_baseline() if not args.no_cpu_baseline else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "rhs_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(args.workload)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl.name, "path": "plain FP64, drop-in F77 ABI", "cells": wl.cells,
+                   "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "rhs_plain_kernel",
+                     "peak_kind": peak_kind, "bytes_per_cell": RHS_BYTES_PER_CELL, "kernel_ms": rhs_ms},
+        "step_roofline": {"bytes_per_cell_update": STEP_BYTES_PER_CELL,
+                          "frac": value * STEP_BYTES_PER_CELL / (hbm_peak * 1e9)},
+        "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
+        "gpu_launches": wl.launches_per_step() * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pulse512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

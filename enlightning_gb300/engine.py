@@ -1,0 +1,272 @@
+"""Host side of the batched multi-level engine (include/enlightning_gpu.h, part 3).
+
+``Engine`` owns one enl_engine handle: level canvases in device memory, the
+patch boxes of every level, and the step entry points (fused batched path,
+plain per-patch path, CUDA-graph capture/replay).  ``Hierarchy`` adds the AMR
+host logic that SAMRAI provides to the reference (main.C:253-312,489-502):
+tagging with tag_cells on the device, buffering of tags, clustering of tagged
+cells into patches, proper nesting, and initialisation of new fine cells.
+
+Canvas convention: field k of level cell (i, j) is at
+``base[k*fstride + (j+3)*pitch + (i+3)]``; fields are rho, rho*u, rho*v,
+rho*s, rho*T_n, p, T.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import REFLECT, RK3_ALPHA1, RK3_ALPHA2, RK3_BETA, VARIANTS
+from .cluster import cluster_tags
+
+MAX_LEVELS = 4
+PREC_FP64, PREC_FP32 = 0, 1
+
+
+from ._lib import ENGINE_SIGNATURES, EngineConfig  # noqa: E402
+
+
+def _boxes_arg(boxes):
+    flat = np.ascontiguousarray(np.asarray(boxes, dtype=np.int32).reshape(-1))
+    return flat, flat.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Engine:
+    """One multi-level canvas engine on the current CUDA device."""
+
+    def __init__(self, params: dict, nx0: int, ny0: int, dx0, nlevels=1, ratio=2, xlo=(0.0, 0.0),
+                 bc=(REFLECT,) * 4, variant="hybrid_high_llf", precision=PREC_FP64, learned=False):
+        self.L = _lib.lib()
+        p = params
+        cfg = EngineConfig()
+        cfg.nlevels, cfg.ratio, cfg.nx0, cfg.ny0 = nlevels, ratio, nx0, ny0
+        cfg.xlo[:] = list(xlo)
+        cfg.dx0[:] = list(dx0)
+        cfg.bc[:] = list(bc)
+        cfg.variant = VARIANTS.index(variant) if isinstance(variant, str) else int(variant)
+        cfg.precision, cfg.learned = int(precision), int(bool(learned))
+        for k in ("weno_alpha", "kappa", "mu", "muB", "R", "T_star_n", "tau_n", "c", "c_lr", "rho0", "gamma1",
+                  "c_p", "p0", "T0", "c_v"):
+            setattr(cfg, k, float(p[k]))
+        cfg.tol[:] = list(p["tol"])
+        cfg.absorb_width = float(p["bc_absorb_width"])
+        cfg.rk_alpha1[:] = list(RK3_ALPHA1)
+        cfg.rk_alpha2[:] = list(RK3_ALPHA2)
+        cfg.rk_beta[:] = list(RK3_BETA)
+        self.cfg = cfg
+        self.params = dict(p)
+        self.nlevels, self.ratio = nlevels, ratio
+        self.dx0 = tuple(dx0)
+        self.xlo = tuple(xlo)
+        _lib.check(self.L.enl_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream)), "enl_set_stream")
+        h = C.c_void_p()
+        _lib.check(self.L.enl_engine_create(C.byref(cfg), C.byref(h)), "enl_engine_create")
+        self.h = h
+        self.patches = [[] for _ in range(nlevels)]
+
+    def close(self):
+        if self.h:
+            self.L.enl_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- geometry -----------------------------------------------------------
+    def level_shape(self, level):
+        nx, ny = C.c_int(), C.c_int()
+        _lib.check(self.L.enl_engine_buffer(self.h, level, 0, None, None, None, C.byref(nx), C.byref(ny)))
+        return nx.value, ny.value
+
+    def dx(self, level):
+        r = self.ratio ** level
+        return (self.dx0[0] / r, self.dx0[1] / r)
+
+    def buffer(self, level, which=0):
+        """torch view (nfields, ny+6, nx+6) of a level canvas (no copy)."""
+        base, pitch, fstride = C.c_void_p(), C.c_long(), C.c_long()
+        nx, ny = C.c_int(), C.c_int()
+        _lib.check(self.L.enl_engine_buffer(self.h, level, which, C.byref(base), C.byref(pitch), C.byref(fstride),
+                                            C.byref(nx), C.byref(ny)), "enl_engine_buffer")
+        nf = 1 if which == 3 else 7
+        n = fstride.value * nf
+        storage = _DeviceMemory(base.value, n)
+        t = torch.as_tensor(storage, device="cuda")
+        t = t.as_strided((nf, ny.value + 6, nx.value + 6), (fstride.value, pitch.value, 1))
+        return t
+
+    # -- patches ------------------------------------------------------------
+    def set_patches(self, level, boxes):
+        boxes = [tuple(int(v) for v in b) for b in boxes]
+        flat, ptr = _boxes_arg(boxes if boxes else np.zeros((0, 4)))
+        _lib.check(self.L.enl_engine_set_patches(self.h, level, len(boxes), ptr), "enl_engine_set_patches")
+        self.patches[level] = boxes
+
+    def refine_init(self, level, boxes):
+        if not boxes:
+            return
+        flat, ptr = _boxes_arg(boxes)
+        _lib.check(self.L.enl_engine_refine_init(self.h, level, len(boxes), ptr), "enl_engine_refine_init")
+
+    def cells(self):
+        return sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1) for lv in self.patches for b in lv)
+
+    # -- stepping -----------------------------------------------------------
+    def fill(self, which=0):
+        _lib.check(self.L.enl_engine_fill(self.h, which), "enl_engine_fill")
+
+    def step(self, dt, plain=False):
+        fn = self.L.enl_engine_step_plain if plain else self.L.enl_engine_step
+        _lib.check(fn(self.h, float(dt)), "enl_engine_step")
+
+    def capture(self, dt):
+        _lib.check(self.L.enl_engine_graph_capture(self.h, float(dt)), "enl_engine_graph_capture")
+
+    def replay(self, nsteps):
+        _lib.check(self.L.enl_engine_graph_replay(self.h, int(nsteps)), "enl_engine_graph_replay")
+
+    def launches_per_step(self, plain=False):
+        return int(self.L.enl_engine_launches_per_step(self.h, int(plain)))
+
+    def stats(self):
+        arr = (C.c_longlong * (2 * MAX_LEVELS))()
+        _lib.check(self.L.enl_engine_stats(self.h, arr), "enl_engine_stats")
+        a = np.array(arr[:], dtype=np.int64).reshape(MAX_LEVELS, 2)
+        return a[: self.nlevels]
+
+    def health(self):
+        return int(self.L.enl_engine_health(self.h))
+
+    def tag(self, level):
+        nx, ny = self.level_shape(level)
+        tags = torch.zeros((ny, nx), dtype=torch.int32, device="cuda")
+        _lib.check(self.L.enl_engine_tag(self.h, level, C.c_void_p(tags.data_ptr())), "enl_engine_tag")
+        return tags
+
+    # -- state I/O ----------------------------------------------------------
+    def set_level_state(self, level, w, pres, temp, which=0):
+        """Write interior (5, ny, nx) state and p, T (ny, nx) of a level."""
+        buf = self.buffer(level, which)
+        ny, nx = pres.shape
+        buf[0:5, 3:3 + ny, 3:3 + nx].copy_(torch.as_tensor(w, device="cuda"))
+        buf[5, 3:3 + ny, 3:3 + nx].copy_(torch.as_tensor(pres, device="cuda"))
+        buf[6, 3:3 + ny, 3:3 + nx].copy_(torch.as_tensor(temp, device="cuda"))
+
+    def level_state(self, level, which=0):
+        buf = self.buffer(level, which)
+        nx, ny = self.level_shape(level)
+        return buf[:, 3:3 + ny, 3:3 + nx]
+
+
+class _DeviceMemory:
+    """__cuda_array_interface__ wrapper of library-owned device memory."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3,
+                                         "strides": None}
+
+
+# ---------------------------------------------------------------------------
+# AMR hierarchy (host metadata, as SAMRAI keeps it)
+# ---------------------------------------------------------------------------
+
+class Hierarchy:
+    """Patch hierarchy over an Engine: tagging, clustering, nesting, regrid.
+
+    Follows the reference's gridding loop (main.C:489-502 with
+    StandardTagAndInitialize + BergerRigoutsos, input.txt:103-127): tag cells
+    of level l with tag_cells (fortran/tag_cells.m4), grow the tags by
+    tag_buffer cells, cluster them into boxes of efficiency >= 0.7 with sides
+    between min_size and max_size, refine the boxes by the ratio, and keep
+    them properly nested inside level l.
+    """
+
+    def __init__(self, engine: Engine, min_size=16, max_size=256, tag_buffer=2, efficiency=0.7, nest=2):
+        self.E = engine
+        self.min_size, self.max_size = min_size, max_size
+        self.tag_buffer, self.efficiency, self.nest = tag_buffer, efficiency, nest
+
+    def base_patches(self, size=256):
+        nx, ny = self.E.level_shape(0)
+        boxes = []
+        for j in range(0, ny, size):
+            for i in range(0, nx, size):
+                boxes.append((i, min(nx, i + size) - 1, j, min(ny, j + size) - 1))
+        self.E.set_patches(0, boxes)
+        return boxes
+
+    def _nesting_mask(self, level):
+        """Cells of `level` index space that may carry level+1 patches."""
+        nx, ny = self.E.level_shape(level)
+        m = np.zeros((ny, nx), bool)
+        for b in self.E.patches[level]:
+            m[b[2]:b[3] + 1, b[0]:b[1] + 1] = True
+        if self.nest > 0:
+            from scipy.ndimage import binary_erosion
+            m = binary_erosion(m, iterations=self.nest, border_value=1)
+        return m
+
+    def regrid_level(self, level, tags=None):
+        """Rebuild level+1 from the tags of `level`; returns the new boxes."""
+        E = self.E
+        if level + 1 >= E.nlevels:
+            return []
+        if tags is None:
+            tags = E.tag(level).cpu().numpy().astype(bool)
+        if self.tag_buffer > 0 and tags.any():
+            from scipy.ndimage import binary_dilation
+            tags = binary_dilation(tags, iterations=self.tag_buffer)
+        tags &= self._nesting_mask(level)
+        r = E.ratio
+        cboxes = cluster_tags(tags, efficiency=self.efficiency, min_size=max(1, self.min_size // r),
+                              max_size=max(2, self.max_size // r))
+        fine = [(b[0] * r, (b[1] + 1) * r - 1, b[2] * r, (b[3] + 1) * r - 1) for b in cboxes]
+        old = list(E.patches[level + 1])
+        new_regions = box_difference(fine, old)
+        E.set_patches(level + 1, fine)
+        E.refine_init(level + 1, new_regions)
+        return fine
+
+    def regrid(self):
+        """Regrid every finer level, coarse to fine (regridAllFinerLevels)."""
+        out = []
+        for l in range(self.E.nlevels - 1):
+            out.append(self.regrid_level(l))
+        return out
+
+
+def box_difference(boxes, remove):
+    """Rectangles covering the union of `boxes` minus the union of `remove`."""
+    out = []
+    for b in boxes:
+        pieces = [b]
+        for r in remove:
+            nxt = []
+            for p in pieces:
+                nxt.extend(_subtract(p, r))
+            pieces = nxt
+        out.extend(pieces)
+    return out
+
+
+def _subtract(a, r):
+    ilo, ihi, jlo, jhi = a
+    if r[1] < ilo or r[0] > ihi or r[3] < jlo or r[2] > jhi:
+        return [a]
+    res = []
+    if jlo < r[2]:
+        res.append((ilo, ihi, jlo, r[2] - 1))
+    if jhi > r[3]:
+        res.append((ilo, ihi, r[3] + 1, jhi))
+    j0, j1 = max(jlo, r[2]), min(jhi, r[3])
+    if ilo < r[0]:
+        res.append((ilo, r[0] - 1, j0, j1))
+    if ihi > r[1]:
+        res.append((r[1] + 1, ihi, j0, j1))
+    return res

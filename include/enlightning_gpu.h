@@ -1,0 +1,270 @@
+/*
+ * enlightning_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of
+ * Enlightning's per-patch time advance.
+ *
+ * Part 1 is the drop-in boundary: the four Fortran entry points that
+ * enlightning.C calls through enlightningfort.h, with the same symbol names
+ * (gfortran mangling of SAMRAI_F77_FUNC: lower case + trailing underscore),
+ * the same argument order and the same meaning.  As in the reference every
+ * scalar is passed by reference (a C++ reference, or a pointer from C, which
+ * is the same ABI).  The difference is where the data lives:
+ *   - patch arrays (w_n, source, rhs, pressure, temperature, tags, ww) are
+ *     DEVICE pointers in SAMRAI CellData layout (depth-major, i fastest);
+ *   - the small geometry arrays (xlo, dx, tag_tolerance) are HOST pointers,
+ *     as SAMRAI's CartesianPatchGeometry hands them out.
+ * Calls are asynchronous on the library stream (enl_set_stream); the caller
+ * synchronises before reading results on the host.  The Fortran routines have
+ * no error channel, so these return void; failures are recorded in a sticky
+ * error word read with enl_get_last_error().
+ *
+ * Part 2 adds status-returning entry points (0 = success, nonzero = an
+ * ENL_ERR_* code) that the reference has no counterpart for: explicit scheme
+ * selection, switch-flag export, the physical-boundary fill and absorbing
+ * envelope of enlightning.C as device kernels, the fused stage, the batched
+ * multi-level engine and the learned sensor.
+ */
+#ifndef ENLIGHTNING_GPU_H
+#define ENLIGHTNING_GPU_H
+
+#ifdef __cplusplus
+#define ENL_REF(T) const T&
+extern "C" {
+#else
+#define ENL_REF(T) const T*
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* Status codes                                                            */
+/* ---------------------------------------------------------------------- */
+#define ENL_OK 0
+#define ENL_ERR_ARG 1        /* invalid argument (sizes, variant, null)    */
+#define ENL_ERR_CUDA 2       /* a CUDA runtime call or launch failed       */
+#define ENL_ERR_NONFINITE 3  /* the health check found rho <= 0 or NaN      */
+#define ENL_ERR_TIMEOUT 4    /* a bounded device-side wait gave up          */
+#define ENL_ERR_STATE 5      /* call order violated (e.g. no engine levels) */
+
+/* RHS scheme ids (the reference picks one at build time, makefile:6). */
+#define ENL_HYBRID_HIGH_LLF 0 /* fortran/rhs_hybrid_high_llf.m4 (default) */
+#define ENL_HYBRID_HIGH 1     /* fortran/rhs_hybrid_high.m4               */
+#define ENL_HYBRID_LOW_LLF 2  /* fortran/rhs_hybrid_low_llf.m4            */
+#define ENL_HYBRID_LOW 3      /* fortran/rhs_hybrid_low.m4                */
+#define ENL_WENO_HIGH_LLF 4   /* fortran/rhs_weno_high_llf.m4             */
+#define ENL_WENO_HIGH 5       /* fortran/rhs_weno_high.m4                 */
+#define ENL_WENO_LOW_LLF 6    /* fortran/rhs_weno_low_llf.m4              */
+#define ENL_WENO_LOW 7        /* fortran/rhs_weno_low.m4                  */
+#define ENL_DRP 8             /* fortran/rhs_drp.m4                       */
+
+/* ====================================================================== */
+/* Part 1: drop-in F77 entry points (enlightningfort.h:22-102)             */
+/* ====================================================================== */
+
+/* Replaces SAMRAI_F77_FUNC(rhs, RHS), enlightningfort.h:23-49
+ * (fortran/rhs_*.m4).  Scheme = the one chosen with enl_set_rhs_variant
+ * (default ENL_HYBRID_HIGH_LLF, the reference makefile's default).
+ * w_n, pressure, temperature: ghosted (gcw0, gcw1); source, rhs: interior. */
+void rhs_(ENL_REF(int) ifirst0, ENL_REF(int) ilast0, ENL_REF(int) ifirst1,
+          ENL_REF(int) ilast1, ENL_REF(int) gcw0, ENL_REF(int) gcw1,
+          const double* xlo, const double* dx, const double* w_n,
+          const double* source, double* rhs, const double* pressure,
+          const double* temperature, ENL_REF(double) weno_alpha,
+          ENL_REF(double) kappa, ENL_REF(double) mu, ENL_REF(double) muB,
+          ENL_REF(double) R, ENL_REF(double) T_star_n,
+          ENL_REF(double) T_star_o, ENL_REF(double) tau_n,
+          ENL_REF(double) tau_o, const double* tag_tolerance,
+          ENL_REF(int) level, ENL_REF(double) c, ENL_REF(double) c_lr,
+          ENL_REF(int) nequ);
+
+/* Replaces SAMRAI_F77_FUNC(runge_kutta, RUNGE_KUTTA), enlightningfort.h:51-64
+ * (fortran/runge_kutta.m4:57-66): w_n = alpha_1*w + alpha_2*w_n + beta*dt*rhs
+ * over the interior.  w_n ghosted; w and rhs interior-only. */
+void runge_kutta_(ENL_REF(int) ifirst0, ENL_REF(int) ilast0,
+                  ENL_REF(int) ifirst1, ENL_REF(int) ilast1, ENL_REF(int) gcw0,
+                  ENL_REF(int) gcw1, ENL_REF(double) dt, ENL_REF(double) alpha_1,
+                  ENL_REF(double) alpha_2, ENL_REF(double) beta, double* w_n,
+                  const double* w, const double* rhs, ENL_REF(int) nequ);
+
+/* Replaces SAMRAI_F77_FUNC(update_state, UPDATE_STATE), enlightningfort.h:66-88
+ * (fortran/update_state.m4:87-107).  Note dx comes before xlo here. */
+void update_state_(const double* dx, const double* xlo, ENL_REF(int) ifirst0,
+                   ENL_REF(int) ilast0, ENL_REF(int) ifirst1,
+                   ENL_REF(int) ilast1, ENL_REF(int) gcw0, ENL_REF(int) gcw1,
+                   const double* w_n, double* pressure, double* temperature,
+                   ENL_REF(double) rho0, ENL_REF(double) c,
+                   ENL_REF(double) gamma1, ENL_REF(double) c_p,
+                   ENL_REF(double) p0, ENL_REF(double) T0,
+                   ENL_REF(double) c_lr, ENL_REF(double) c_v,
+                   ENL_REF(double) R_tilde, ENL_REF(double) M,
+                   ENL_REF(double) R, ENL_REF(int) nequ);
+
+/* Replaces SAMRAI_F77_FUNC(tag_cells, TAG_CELLS), enlightningfort.h:90-101
+ * (fortran/tag_cells.m4:58-108).  tags interior-only (int); w_n and source
+ * ghosted.  Bit-exact with the reference. */
+void tag_cells_(ENL_REF(int) ifirst0, ENL_REF(int) ilast0,
+                ENL_REF(int) ifirst1, ENL_REF(int) ilast1, ENL_REF(int) gcw0,
+                ENL_REF(int) gcw1, int* tags, const double* w_n,
+                const double* source, ENL_REF(int) refine_tag_val,
+                const double* tag_tolerance, ENL_REF(int) nequ);
+
+/* ====================================================================== */
+/* Part 2: library control and extended entry points                      */
+/* ====================================================================== */
+
+/* Stream all calls enqueue on (a cudaStream_t; NULL = legacy default). */
+int enl_set_stream(void* stream);
+/* Sticky error word: first ENL_ERR_* recorded since the last call. */
+int enl_get_last_error(void);
+const char* enl_error_string(int code);
+/* Scheme used by rhs_ (ENL_* id).  The reference fixes it at build time. */
+int enl_set_rhs_variant(int variant);
+int enl_get_rhs_variant(void);
+
+/* rhs_ with an explicit scheme, an optional per-cell switch output
+ * (flags: device int[nx*ny], 1 = WENO, 0 = DRP; may be NULL) and explicit
+ * row pitches so patches stored inside a larger array can be addressed.
+ * w_pitch/w_fstride: elements between rows / fields of w_n (pressure and
+ * temperature share w_pitch and hold one field each); out_pitch/out_fstride
+ * likewise for rhs, source uses out_pitch.  Everything else as rhs_.
+ * Follows fortran/rhs_<variant>.m4. */
+int enl_rhs(int variant, int ifirst0, int ilast0, int ifirst1, int ilast1,
+            int gcw0, int gcw1, const double* xlo, const double* dx,
+            const double* w_n, long w_pitch, long w_fstride,
+            const double* source, double* rhs, long out_pitch,
+            long out_fstride, const double* pressure,
+            const double* temperature, double weno_alpha, double kappa,
+            double mu, double muB, double R, double T_star_n, double tau_n,
+            const double* tag_tolerance, int level, double c, double c_lr,
+            int* flags);
+
+/* Physical-boundary ghost fill of one patch, enlightning.C:790-1013.
+ * touches[4] (host): patch side lies on the domain boundary (L, R, B, T).
+ * bc[4] (host): 10 = REFLECT, 20 = ABSORB.  fill0/fill1: ghost width to fill.
+ * Arrays ghosted (SAMRAI layout): w_n (5 fields), pressure, temperature,
+ * source. */
+int enl_phys_bc(int ifirst0, int ilast0, int ifirst1, int ilast1, int gcw0,
+                int gcw1, const int* touches, const int* bc, int fill0,
+                int fill1, double* w_n, double* pressure, double* temperature,
+                double* source);
+
+/* Absorbing envelope of one patch, enlightning.C:634-786 (including its loop
+ * exit rules).  patch_xlo, dx, grid_xlo, grid_xhi, bc: host arrays. */
+int enl_absorb(int ifirst0, int ilast0, int ifirst1, int ilast1, int gcw0,
+               int gcw1, const double* patch_xlo, const double* dx,
+               const double* grid_xlo, const double* grid_xhi, const int* bc,
+               double absorb_width, double p0, double T0, double rho0,
+               double* w_n, double* pressure, double* temperature);
+
+/* ====================================================================== */
+/* Part 3: batched multi-level engine                                      */
+/* ====================================================================== */
+/* All patches of all AMR levels advance together.  Each level is stored as
+ * one ghosted canvas covering the whole level index space (3 ghost cells on
+ * every side, 7 FP64 fields: rho, rho*u, rho*v, rho*s, rho*T_n, p, T), with
+ * three such buffers (current, stage A, stage B) plus the source H0.
+ * Patches are index boxes into the canvas: same-level ghost exchange is a
+ * read of the neighbour's cells, coarse-fine ghosts are filled by bilinear
+ * interpolation from the coarser canvas (the reference registers
+ * LINEAR_REFINE, enlightning.C:259-288), physical ghosts by the rule of
+ * enlightning.C:790-1013, and fine data is averaged onto the coarse level
+ * after every step (CONSERVATIVE_COARSEN).  One RK3 step = per stage: ghost
+ * fill of every level, then one persistent kernel over a device tile list
+ * that fuses rhs + runge_kutta + update_state; the absorbing envelope and the
+ * coarsening follow.  The whole step can be captured once as a CUDA graph and
+ * replayed until the next regrid (the tile and halo tables are device data,
+ * so a regrid rewrites them without a new capture unless they outgrow their
+ * capacity). */
+
+#define ENL_MAX_LEVELS 4
+#define ENL_PREC_FP64 0   /* RHS in FP64: same results as the plain path   */
+#define ENL_PREC_FP32 1   /* RHS in FP32 perturbation form, FP64 state     */
+
+typedef struct {
+  int nlevels;            /* 1..ENL_MAX_LEVELS                              */
+  int ratio;              /* refinement ratio between levels (2)            */
+  int nx0, ny0;           /* level-0 cells                                   */
+  double xlo[2];          /* domain lower corner (m)                         */
+  double dx0[2];          /* level-0 cell size (m)                           */
+  int bc[4];              /* L, R, B, T: 10 = REFLECT, 20 = ABSORB           */
+  int variant;            /* ENL_* scheme id                                 */
+  int precision;          /* ENL_PREC_FP64 or ENL_PREC_FP32                  */
+  int learned;            /* 1: learned switch on level 0 (FP32 only)        */
+  double weno_alpha, kappa, mu, muB, R, T_star_n, tau_n, c, c_lr;
+  double tol[3];
+  double rho0, gamma1, c_p, p0, T0, c_v;
+  double absorb_width;
+  double rk_alpha1[3], rk_alpha2[3], rk_beta[3];
+} enl_engine_config;
+
+/* Create / destroy.  Allocates the canvases of every level (device memory). */
+int enl_engine_create(const enl_engine_config* cfg, void** engine);
+int enl_engine_destroy(void* engine);
+/* Device canvas of one level: which = 0 current, 1 stage A, 2 stage B,
+ * 3 source H0.  Cell (i, j) of the level (i, j >= -3) is element
+ * base[k*fstride + (j+3)*pitch + (i+3)] of field k. */
+int enl_engine_buffer(void* engine, int level, int which, double** base,
+                      long* pitch, long* fstride, int* nx, int* ny);
+/* Patch boxes of one level, (ilo, ihi, jlo, jhi) per patch in that level's
+ * index space, host array of 4*npatch ints.  Level l > 0 boxes must be
+ * properly nested in level l-1 (after coarsening) and start at even x. */
+int enl_engine_set_patches(void* engine, int level, int npatch, const int* boxes);
+/* Fill the cells of the given boxes of `level` (current buffer) by bilinear
+ * interpolation from level-1 (new fine data after a regrid). */
+int enl_engine_refine_init(void* engine, int level, int nbox, const int* boxes);
+/* Ghost fill of buffer `which` on every level (physical + coarse-fine). */
+int enl_engine_fill(void* engine, int which);
+/* One RK3 step of the batched fused path (kernel launches on the stream). */
+int enl_engine_step(void* engine, double dt);
+/* One RK3 step of the plain path: per patch, unfused FP64 rhs, runge_kutta
+ * and update_state launches (what enlightning.C issues through the F77
+ * entry points), same storage and ghost fill. */
+int enl_engine_step_plain(void* engine, double dt);
+/* Capture one fused step as a CUDA graph, then replay it nsteps times. */
+int enl_engine_graph_capture(void* engine, double dt);
+int enl_engine_graph_replay(void* engine, int nsteps);
+/* tag_cells over the patches of `level` (fortran/tag_cells.m4), into a
+ * device int array of nx*ny (level index space, row pitch nx); cells outside
+ * the patches are 0.  Fills ghosts of the current buffer and H0 first. */
+int enl_engine_tag(void* engine, int level, int* tags);
+/* Counters of the last steps: per level, cells advanced with WENO and in
+ * total (host array of 2*ENL_MAX_LEVELS long long), then reset. */
+int enl_engine_stats(void* engine, long long* counts);
+/* Health word: 0, or ENL_ERR_NONFINITE / ENL_ERR_TIMEOUT raised by a kernel
+ * since the last call (rho <= 0 or non-finite; a bounded wait gave up). */
+int enl_engine_health(void* engine);
+/* Number of kernel launches one enl_engine_step issues (for accounting). */
+int enl_engine_launches_per_step(void* engine, int plain);
+
+/* Adaptive time step computed on the device at the start of every step:
+ * dt = cfl * (finest dx) / max over all patch cells of max(|u|,|v|) + c, a
+ * warp-shuffle max reduction; stage kernels read dt from device memory, so a
+ * captured graph stays valid.  The dt passed to enl_engine_step is then an
+ * upper bound.  Off by default (the reference uses cfl*dx/c,
+ * enlightning.C:433-456). */
+int enl_engine_set_adaptive_dt(void* engine, int on, double cfl);
+/* Last device dt and accumulated simulated time (adaptive mode). */
+int enl_engine_time(void* engine, double* dt_last, double* sim_time);
+
+/* Source painting on the H0 canvas of one level over its patches, as
+ * enlightning::addSource does (enlightning.C:2140-2307): type 10 = POINT,
+ * 20 = SINE, 30 = LIGHTNING; mode 10 = PULSE, 20 = DRIVEN (POINT only; the
+ * painted value is multiplied by `drive` = sin(omega*(n+1-n0)*dt)).  amp and
+ * spread as src_amp / src_spread (Gaussian exp(-ln2 r^2/spread^2)); pos (host,
+ * 2 doubles) for POINT and SINE; segs (host, 4*nseg doubles x0,y0,x1,y1) for
+ * LIGHTNING, accumulated in order with the capsule-union rule. */
+int enl_engine_paint_source(void* engine, int level, int type, int mode,
+                            double amp, double spread, const double* pos,
+                            double sine_amp, double sine_freq, int nseg,
+                            const double* segs, double drive);
+/* Read H0 of a level as an overpressure and write the corresponding ambient-
+ * entropy state (inverse of update_state.m4:90-94) into the current buffer on
+ * the level's patches; H0 is zeroed.  Builds synthetic initial conditions. */
+int enl_engine_state_from_overpressure(void* engine, int level);
+/* Regrid helper: tag_cells on `level`, then a block map (host array of
+ * nbx*nby bytes, block x block cells per entry) marking blocks with a tagged
+ * cell within `buffer` cells.  With map_host == NULL only nbx, nby are set. */
+int enl_engine_tag_blocks(void* engine, int level, int block, int buffer,
+                          unsigned char* map_host, int* nbx, int* nby);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ENLIGHTNING_GPU_H */

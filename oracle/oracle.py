@@ -161,3 +161,46 @@ def phys_bc(box, g, touches, bc, w_n, pres, temp, source, fill=None):
     lib().ora_phys_bc(if0, il0, if1, il1, g[0], g[1], _ip(np.asarray(touches, np.int32)),
                       _ip(np.asarray(bc, np.int32)), fw[0], fw[1], _dp(w_n), _dp(pres), _dp(temp),
                       _dp(source))
+
+
+class Patch:
+    """Single-patch state for the oracle's stage driver (numpy, SAMRAI layout)."""
+
+    def __init__(self, box, xlo, dx, level=0, touches=(1, 1, 1, 1), g=3):
+        self.box, self.xlo, self.dx, self.level, self.touches, self.g = box, xlo, dx, level, touches, g
+        nx, ny = box[1] - box[0] + 1, box[3] - box[2] + 1
+        self.nx, self.ny = nx, ny
+        NX, NY = nx + 2 * g, ny + 2 * g
+        self.w_scr = np.zeros((5, NY, NX))
+        self.w_cur = np.zeros((5, ny, nx))
+        self.pres = np.zeros((NY, NX))
+        self.temp = np.zeros((NY, NX))
+        self.src = np.zeros((ny, nx))
+        self.src_g = np.zeros((NY, NX))
+
+    def interior(self, a):
+        g = self.g
+        return a[..., g:g + self.ny, g:g + self.nx]
+
+
+def advance(P: Patch, prm, variant, dt, nsteps, bc=(REFLECT,) * 4, domain=((0, 0), (1, 1)),
+            rk=((1.0, 0.75, 0.3333333333), (0.0, 0.25, 0.6666666667), (1.0, 0.25, 0.6666666667)),
+            flags_out=None):
+    """SAMRAI MOL loop for one patch with the reference's stage order
+    (enlightning.C:459-583), the oracle's restatement of every call."""
+    a1s, a2s, bs = rk
+    g = P.g
+    for _ in range(nsteps):
+        P.interior(P.w_scr)[...] = P.w_cur
+        for s in range(len(a1s)):
+            phys_bc(P.box, (g, g), P.touches, bc, P.w_scr, P.pres, P.temp, P.src_g)
+            res = rhs(variant, P.box, (g, g), P.xlo, P.dx, P.w_scr, P.src, P.pres, P.temp, prm, P.level,
+                      flags=flags_out is not None)
+            KK = res[0] if flags_out is not None else res
+            if flags_out is not None:
+                flags_out.append(res[1])
+            runge_kutta(P.box, (g, g), dt, a1s[s], a2s[s], bs[s], P.w_scr, P.w_cur, KK)
+            update_state(P.dx, P.xlo, P.box, (g, g), P.w_scr, P.pres, P.temp, prm)
+            absorb(P.box, (g, g), P.xlo, P.dx, domain[0], domain[1], bc, prm["bc_absorb_width"], prm,
+                   P.w_scr, P.pres, P.temp)
+        P.w_cur[...] = P.interior(P.w_scr)

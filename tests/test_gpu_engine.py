@@ -1,0 +1,173 @@
+"""Batched multi-level engine (GPU) against the oracle's written specification.
+
+* FP64 fused path and plain per-patch path: relative L2 <= 1e-12 per field
+  after several RK3 steps, on a single patch (the reference's own
+  single-patch semantics) and on a two-level hierarchy (oracle/amr.py);
+* graph replay is bit-identical to direct launches;
+* the FP32 perturbation-form path stays within 1e-3 relative L2 of FP64,
+  also on the perturbation fields;
+* tag_cells over the level canvas is bit-exact.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from enlightning_gb300 import workloads  # noqa: E402
+from enlightning_gb300.constants import ABSORB, REFLECT, default_params  # noqa: E402
+from enlightning_gb300.engine import PREC_FP32, PREC_FP64, Engine  # noqa: E402
+
+G = 3
+
+
+def relL2(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    d = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (d if d > 0 else 1.0)
+
+
+def pulse_level(nx, ny, prm, amp=0.1, sigma=4.0, cx=None, cy=None):
+    dp = workloads.gaussian_dp(nx, ny, amp * prm["p0"], sigma, cx, cy)
+    w = workloads.state_from_dp(dp, prm)
+    import oracle as ora
+    pres, temp = np.zeros((ny + 2 * G, nx + 2 * G)), np.zeros((ny + 2 * G, nx + 2 * G))
+    wg = np.zeros((5, ny + 2 * G, nx + 2 * G))
+    wg[:, G:-G, G:-G] = w
+    wg[0][wg[0] == 0] = prm["rho0"]
+    ora.update_state((1.0, 1.0), (0.0, 0.0), (0, nx - 1, 0, ny - 1), (G, G), wg, pres, temp, prm)
+    return w, pres[G:-G, G:-G].copy(), temp[G:-G, G:-G].copy()
+
+
+def make_pair(prm, nx, ny, dx, nlevels, patches, bc, variant, precision=PREC_FP64):
+    from amr import OracleAMR
+    E = Engine(prm, nx, ny, dx, nlevels=nlevels, bc=bc, variant=variant, precision=precision)
+    O = OracleAMR(prm, nx, ny, dx, nlevels=nlevels, bc=bc, variant=variant)
+    w, p, t = pulse_level(nx, ny, prm, amp=0.2, sigma=3.0, cx=nx * 0.45, cy=ny * 0.5)
+    E.set_level_state(0, w, p, t)
+    O.cur[0][0:5, G:-G, G:-G] = w
+    O.cur[0][5, G:-G, G:-G] = p
+    O.cur[0][6, G:-G, G:-G] = t
+    for l, boxes in enumerate(patches):
+        E.set_patches(l, boxes)
+        O.patches[l] = list(boxes)
+        if l > 0:
+            O.refine_init(l, boxes)
+            E.refine_init(l, boxes)
+    return E, O
+
+
+def compare(E, O, l, tol):
+    got = E.level_state(l).cpu().numpy()
+    ref = O.interior(O.cur[l], l)
+    prm = O.prm
+    mask = np.zeros(ref.shape[1:], bool)
+    for b in O.patches[l]:
+        mask[b[2]:b[3] + 1, b[0]:b[1] + 1] = True
+    errs = []
+    for k in range(7):
+        errs.append(relL2(got[k][mask], ref[k][mask]))
+    errs.append(relL2(got[0][mask] - prm["rho0"], ref[0][mask] - prm["rho0"]))
+    errs.append(relL2(got[5][mask] - prm["p0"], ref[5][mask] - prm["p0"]))
+    assert max(errs) <= tol, errs
+    return max(errs)
+
+
+@pytest.mark.parametrize("plain", [False, True])
+@pytest.mark.parametrize("variant", ["hybrid_high_llf", "weno_high", "drp"])
+def test_single_level_fp64_matches_oracle(ora, variant, plain):
+    prm = default_params()
+    nx, ny = 64, 48
+    E, O = make_pair(prm, nx, ny, (0.1, 0.1), 1, [[(0, 31, 0, 47), (32, 63, 0, 23), (32, 63, 24, 47)]],
+                     (REFLECT,) * 4, variant)
+    dt = workloads.pulse_dt(prm, (0.1, 0.1))
+    for _ in range(8):
+        E.step(dt, plain=plain)
+        O.step(dt)
+    torch.cuda.synchronize()
+    assert E.health() == 0
+    compare(E, O, 0, 1e-12)
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_two_level_fp64_matches_oracle(ora, plain):
+    prm = default_params(bc_absorb_width=0.5)
+    nx, ny = 48, 40
+    fine = [(24, 55, 20, 51), (56, 71, 28, 43)]
+    E, O = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 23, 0, 39), (24, 47, 0, 39)], fine],
+                     (ABSORB, REFLECT, REFLECT, ABSORB), "hybrid_high_llf")
+    dt = workloads.pulse_dt(prm, (0.05, 0.05))
+    for _ in range(5):
+        E.step(dt, plain=plain)
+        O.step(dt)
+    torch.cuda.synchronize()
+    assert E.health() == 0
+    compare(E, O, 0, 1e-12)
+    compare(E, O, 1, 1e-12)
+
+
+def test_graph_replay_bit_identical(ora):
+    prm = default_params()
+    nx, ny = 64, 64
+    res = []
+    for use_graph in (False, True):
+        E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 63, 0, 63)], [(40, 87, 40, 87)]], (REFLECT,) * 4,
+                         "hybrid_high_llf")
+        dt = workloads.pulse_dt(prm, (0.05, 0.05))
+        torch.cuda.synchronize()
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            E.L.enl_set_stream(__import__("ctypes").c_void_p(s.cuda_stream))
+            if use_graph:
+                E.capture(dt)
+                E.replay(6)
+            else:
+                for _ in range(6):
+                    E.step(dt)
+        torch.cuda.synchronize()
+        res.append([E.level_state(l).cpu().numpy().copy() for l in range(2)])
+        E.L.enl_set_stream(__import__("ctypes").c_void_p(torch.cuda.current_stream().cuda_stream))
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b)
+
+
+def test_fp32_fast_path_within_budget(ora):
+    prm = default_params()
+    nx, ny = 96, 64
+    boxes = [[(0, 47, 0, 63), (48, 95, 0, 63)], [(48, 143, 32, 95)]]
+    out = {}
+    for prec in (PREC_FP64, PREC_FP32):
+        E, O = make_pair(prm, nx, ny, (0.1, 0.1), 2, boxes, (REFLECT,) * 4, "hybrid_high_llf", precision=prec)
+        dt = workloads.pulse_dt(prm, (0.05, 0.05))
+        for _ in range(20):
+            E.step(dt)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        out[prec] = [E.level_state(l).cpu().numpy().copy() for l in range(2)]
+    for l in range(2):
+        a, b = out[PREC_FP32][l], out[PREC_FP64][l]
+        m = np.zeros(a.shape[1:], bool)
+        for bx in boxes[l]:
+            m[bx[2]:bx[3] + 1, bx[0]:bx[1] + 1] = True
+        for k in (0, 1, 2, 4):
+            assert relL2(a[k][m], b[k][m]) <= 1e-3
+        assert relL2(a[0][m] - prm["rho0"], b[0][m] - prm["rho0"]) <= 1e-3
+        assert relL2(a[5][m] - prm["p0"], b[5][m] - prm["p0"]) <= 1e-3
+
+
+def test_engine_tag_bit_exact(ora):
+    prm = default_params()
+    nx, ny = 64, 48
+    E, O = make_pair(prm, nx, ny, (0.1, 0.1), 1, [[(0, 63, 0, 47)]], (REFLECT,) * 4, "hybrid_high_llf")
+    dt = workloads.pulse_dt(prm, (0.1, 0.1))
+    for _ in range(3):
+        E.step(dt)
+    tags = E.tag(0).cpu().numpy()
+    st = E.level_state(0).cpu().numpy()
+    buf = E.buffer(0, 0).cpu().numpy()
+    h0 = E.buffer(0, 3).cpu().numpy()[0]
+    w = np.ascontiguousarray(buf[0:5])
+    ref = ora.tag_cells((0, nx - 1, 0, ny - 1), (G, G), w, np.ascontiguousarray(h0), prm["tol"])
+    assert np.array_equal(tags, ref)
+    assert tags.sum() > 0
+    assert st.shape == (7, ny, nx)
