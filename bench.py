@@ -246,7 +246,117 @@ class Pulse512Plain:
                 "sample": f"{steps} RK3 steps of the full 512x512 patch ({el:.1f} s)"}
 
 
-WORKLOADS = {"pulse512": Pulse512Plain}
+class LineSource:
+    """Config 3: thunder-like line source on a 3-level hierarchy.
+
+    4096x2048 base cells, dx = 0.5 m, refinement ratio 2 (finest dx 0.125 m),
+    200-segment seeded random-walk channel depositing 10 p0 with sigma 2 base
+    cells, ABSORB left/right/top and REFLECT ground, patches of 16..256 cells,
+    regrid every 10 steps.  The headline arm is the batched engine (all
+    patches of all levels in one persistent FP32-perturbation stage kernel,
+    CUDA graph); the plain arm advances the same hierarchy with per-patch
+    FP64 rhs / runge_kutta / update_state launches (the drop-in path)."""
+
+    name = ("linesource3L: 4096x2048 base, dx 0.5 m, 3 levels ratio 2, 200-segment channel 10 p0 "
+            "sigma 2 cells, hybrid_high_llf, regrid every 10 steps")
+    REGRID = 10
+
+    def __init__(self, seed=100, learned=False):
+        import torch
+
+        from enlightning_gb300 import workloads
+        from enlightning_gb300.constants import default_params
+        from enlightning_gb300.engine import PREC_FP32, PREC_FP64
+
+        self.torch = torch
+        self.prm = default_params()
+        self.learned = learned
+        self.fast, self.fast_h, self.segs = workloads.line_source(self.prm, seed=seed, precision=PREC_FP32,
+                                                                  learned=learned)
+        self.plain, self.plain_h, _ = workloads.line_source(self.prm, seed=seed, precision=PREC_FP64)
+        self.steps_done = {"fast": 0, "plain": 0}
+        self.graph_ok = False
+        self.dt_cap = 1.0
+
+    def cells(self, E):
+        return E.cells()
+
+    def advance(self, which, nsteps, use_graph=False):
+        """nsteps RK3 steps with regrids every REGRID steps; returns cell-updates."""
+        E = self.fast if which == "fast" else self.plain
+        H = self.fast_h if which == "fast" else self.plain_h
+        done = 0
+        for _ in range(nsteps):
+            if self.steps_done[which] > 0 and self.steps_done[which] % self.REGRID == 0:
+                H.regrid()
+                self.graph_ok = False if which == "fast" else self.graph_ok
+            done += E.cells()
+            if which == "fast" and use_graph:
+                if not self.graph_ok:
+                    E.capture(self.dt_cap)
+                    self.graph_ok = True
+                E.replay(1)
+            else:
+                E.step(self.dt_cap, plain=(which == "plain"))
+            self.steps_done[which] += 1
+        return done
+
+    def compare(self):
+        """rel-L2 of the fast arm against the plain FP64 arm on level 0 (composite)."""
+        a = self.fast.level_state(0).cpu().numpy()
+        b = self.plain.level_state(0).cpu().numpy()
+        p = self.prm
+        out = {}
+        names = ["rho", "rho_u", "rho_v", "rho_s", "rho_Tn", "p", "T"]
+        for k, n in enumerate(names):
+            out[n] = float(np.linalg.norm(a[k] - b[k]) / max(np.linalg.norm(b[k]), 1e-300))
+        out["rho-rho0"] = float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0] - p["rho0"]))
+        out["p-p0"] = float(np.linalg.norm(a[5] - b[5]) / np.linalg.norm(b[5] - p["p0"]))
+        return out
+
+    def cpu_baseline(self, budget_s=12.0, threads=None):
+        """The oracle's restated Fortran on a sample of this hierarchy's patches
+        (one RK3 step each, all host threads); patches drawn across levels in
+        proportion to the levels' cell counts."""
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as ora
+        threads = threads or os.cpu_count() or 1
+        ora.set_threads(threads)
+        E = self.fast
+        rng = np.random.default_rng(0)
+        cells_l = [sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1) for b in E.patches[l]) for l in range(E.nlevels)]
+        tot = float(sum(cells_l))
+        sample = []
+        for l in range(E.nlevels):
+            k = max(1, int(round(12 * cells_l[l] / tot))) if E.patches[l] else 0
+            idx = rng.choice(len(E.patches[l]), size=min(k, len(E.patches[l])), replace=False) if k else []
+            buf = E.buffer(l, 0).cpu().numpy()
+            for q in idx:
+                b = E.patches[l][q]
+                v = np.ascontiguousarray(buf[:, b[2]:b[3] + 7, b[0]:b[1] + 7])
+                sample.append((l, b, v))
+        ncell, steps, t0 = 0, 0, time.perf_counter()
+        while True:
+            for l, b, v in sample:
+                dx = E.dx(l)
+                P = ora.Patch(b, (E.xlo[0] + dx[0] * b[0], E.xlo[1] + dx[1] * b[2]), dx, level=l,
+                              touches=(0, 0, 0, 0))
+                P.w_scr[...] = v[0:5]
+                P.w_cur[...] = P.interior(v[0:5])
+                P.pres[...] = v[5]
+                P.temp[...] = v[6]
+                ora.advance(P, self.prm, "hybrid_high_llf", 1e-5, 1, bc=(20, 20, 10, 20))
+                ncell += P.nx * P.ny
+            steps += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s or steps >= 50:
+                break
+        return {"value": ncell / el, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"{len(sample)} patches ({ncell // steps} cells) across the 3 levels x {steps} RK3 "
+                          f"steps ({el:.1f} s)"}
+
+
+WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource}
 
 
 # ---------------------------------------------------------------------------
@@ -259,9 +369,90 @@ def dist_env():
     return ws, rank, local
 
 
+def linesource_cpu_sample(seed=100, patch=128):
+    """Patches of the line-source initial state built on the CPU (oracle
+    painter, enlightning.C:2214-2281): per level (dx 0.5, 0.25, 0.125 m)
+    patches centred on the channel, plus ambient level-0 patches, in the mix
+    of cells the GPU hierarchy holds (level 0 : 1 : 2 ~ 2 : 1 : 1)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as ora
+    from enlightning_gb300 import workloads
+    from enlightning_gb300.constants import default_params
+    prm = default_params()
+    rng = np.random.default_rng(seed)
+    nx0, ny0, dx0 = 4096, 2048, 0.5
+    segs = workloads.random_walk_channel(rng, nseg=200, start=(0.5 * nx0 * dx0, 0.85 * ny0 * dx0),
+                                         heading_deg=-90.0)
+    amp, spread = 10.0 * prm["p0"], workloads.gaussian_spread(2.0 * dx0)
+    out = []
+    plan = [(0, 3, True), (0, 3, False), (1, 3, True), (2, 3, True)]
+    for level, count, on_channel in plan:
+        dx = dx0 / 2 ** level
+        for q in range(count):
+            if on_channel:
+                sgm = segs[(q + 1) * len(segs) // (count + 1)]
+                cx, cy = 0.5 * (sgm[0] + sgm[2]), 0.5 * (sgm[1] + sgm[3])
+            else:
+                cx, cy = 200.0 + 300.0 * q, 200.0
+            i0 = int(cx / dx) - patch // 2
+            j0 = int(cy / dx) - patch // 2
+            n = patch + 6
+            xlo = (dx * (i0 - 3), dx * (j0 - 3))
+            H = np.zeros((n, n))
+            ora.paint_source(n, n, xlo, (dx, dx), H, 30, amp=amp, spread=spread, segs=segs)
+            w = workloads.state_from_dp(H, prm)
+            out.append((level, (i0, i0 + patch - 1, j0, j0 + patch - 1), (dx, dx), np.ascontiguousarray(w)))
+    return prm, out
+
+
+def run_reference_linesource(args):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as ora
+    threads = os.cpu_count() or 1
+    ora.set_threads(threads)
+    prm, sample = linesource_cpu_sample()
+    patches = []
+    for level, box, dx, w in sample:
+        P = ora.Patch(box, (box[0] * dx[0], box[2] * dx[1]), dx, level=level, touches=(0, 0, 0, 0))
+        P.w_scr[...] = w
+        P.w_cur[...] = P.interior(w)
+        ora.update_state(dx, (0, 0), (box[0] - 3, box[1] + 3, box[2] - 3, box[3] + 3), (0, 0), P.w_scr, P.pres,
+                         P.temp, prm)
+        patches.append(P)
+    dt = 0.5 * 0.125 / 733.0
+
+    def one_pass():
+        t0 = time.perf_counter()
+        nc = 0
+        for P in patches:
+            ora.advance(P, prm, "hybrid_high_llf", dt, 1, bc=(20, 20, 10, 20))
+            nc += P.nx * P.ny
+        return nc, time.perf_counter() - t0
+
+    for _ in range(max(1, args.warmup)):
+        one_pass()
+    vals = []
+    for _ in range(args.steps):
+        nc, el = one_pass()
+        vals.append(nc / el)
+    v = float(np.median(vals))
+    cells = sum(P.nx * P.ny for P in patches)
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"{len(patches)} patches of 128x128 ({cells} cells) of the line-source state across the 3 "
+                    f"levels' resolutions, one RK3 step per timed step"}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist_env()[0],
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": LineSource.name},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
+        return
+    if args.workload == "linesource":
+        run_reference_linesource(args)
         return
     wl = WORKLOADS[args.workload]
     # the reference arm needs no GPU: build the workload description only
@@ -369,17 +560,139 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def run_linesource(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    # one non-default stream for torch and the library (graph capture needs it)
+    torch.cuda.set_stream(torch.cuda.Stream())
+    hbm_peak, peak_kind = peaks()
+    t_build = time.perf_counter()
+    wl = LineSource(learned=args.learned)
+    t_build = time.perf_counter() - t_build
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # accuracy: both arms from the same initial state, same regrid cadence
+    ncmp = args.compare_steps
+    wl.advance("fast", ncmp, use_graph=True)
+    wl.advance("plain", ncmp)
+    barrier()
+    err = wl.compare()
+    weno = wl.fast.stats()
+    # warm-up, then the timed region (graph replay, regrids included)
+    wl.advance("fast", max(3, args.warmup), use_graph=True)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    wl.fast.stats()
+    with ClockSampler(local) as clk:
+        e0.record()
+        cu = wl.advance("fast", args.steps, use_graph=True)
+        e1.record()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cu * ws / (ms * 1e-3)
+    st = wl.fast.stats()
+    weno_frac = {f"L{l}": float(st[l, 0] / max(1, st[l, 1])) for l in range(st.shape[0])}
+    weno_frac["all"] = float(st[:, 0].sum() / max(1, st[:, 1].sum()))
+    launches = wl.fast.launches_per_step() * args.steps
+    # plain arm (per-patch FP64 launches, same hierarchy logic)
+    kp = max(1, min(args.steps, args.plain_steps))
+    barrier()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record()
+    cup = wl.advance("plain", kp)
+    p1.record()
+    barrier()
+    plain_value = cup / (p0.elapsed_time(p1) * 1e-3)
+    # dominant kernel: stage kernel timed with events around each launch
+    wl.fast.profile(True)
+    wl.advance("fast", 3, use_graph=False)
+    barrier()
+    kms, kl, kcells = wl.fast.profile(False)
+    per_launch_ms = kms / max(1, kl)
+    cells_per_launch = kcells / max(1, kl)
+    achieved = cells_per_launch * (STEP_BYTES_PER_CELL / 3.0) / (per_launch_ms * 1e-3) / 1e9
+    # e2e: hierarchy state through the public API from pinned host memory
+    n = wl.fast.packed_size()
+    host = torch.empty(n, dtype=torch.float64).pin_memory()
+    wl.fast.download(host)
+    barrier()
+    ke = max(1, min(args.steps, 10))
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    q0.record()
+    cue = 0
+    for _ in range(ke):
+        wl.fast.upload(host)
+        cue += wl.advance("fast", 1, use_graph=True)
+        wl.fast.download(host)
+    q1.record()
+    barrier()
+    e2e_value = cue * ws / (q0.elapsed_time(q1) * 1e-3)
+    nbytes = int(n * 8)
+    if rank != 0:
+        return
+    health = wl.fast.health()
+    cb = wl.cpu_baseline() if not args.no_cpu_baseline else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("linesource")
+        except Exception:
+            traffic = None
+    dt_last, sim_t = wl.fast.time()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 rhs / f64 state", "data": "synthetic",
+        "config": {"workload": wl.name, "path": "batched: persistent fused stage kernel over all levels, "
+                   "FP32 perturbation RHS, CUDA graph" + (", learned sensor" if wl.learned else ", plain sensor"),
+                   "cells_per_step": cu / args.steps, "patches": [len(p) for p in wl.fast.patches],
+                   "l2": "inputs larger than L2 (hierarchy state ~1.5 GB)", "regrid_every": wl.REGRID,
+                   "dt": "device CFL reduction, cfl 0.5 on max(|u|+c)", "dt_last": dt_last, "sim_time": sim_t,
+                   "plain_value": plain_value, "plain_steps": kp, "speedup_vs_plain": value / plain_value,
+                   "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
+                   "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "stage_kernel (FP32)",
+                     "peak_kind": peak_kind, "bytes_per_cell_launch": STEP_BYTES_PER_CELL / 3.0,
+                     "kernel_ms": per_launch_ms, "cells_per_launch": cells_per_launch},
+        "cpu_baseline": cb,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "clocks": clk.summary(), "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pulse512", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="linesource", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--plain-steps", type=int, default=10)
+    ap.add_argument("--compare-steps", type=int, default=20)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "linesource":
+        run_linesource(args)
     else:
         run_ours(args)
 

@@ -73,6 +73,19 @@ ENGINE_SIGNATURES = {
                                           C.POINTER(C.c_double), C.c_double]),
     "enl_engine_state_from_overpressure": (C.c_int, [C.c_void_p, C.c_int]),
     "enl_engine_set_adaptive_dt": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "enl_engine_packed_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "enl_mlp_nparams": (C.c_int, []),
+    "enl_mlp_forward": (C.c_int, [C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]),
+    "enl_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "enl_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                               C.c_float, C.c_float, C.c_int]),
+    "enl_engine_set_mlp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float]),
+    "enl_engine_harvest": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.c_double, C.c_uint,
+                                     C.c_void_p, C.c_void_p, C.c_long, C.c_void_p]),
+    "enl_engine_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_longlong)]),
+    "enl_engine_download": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "enl_engine_upload": (C.c_int, [C.c_void_p, C.c_void_p]),
     "enl_engine_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "enl_engine_tag_blocks": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int),
                                         C.POINTER(C.c_int)]),

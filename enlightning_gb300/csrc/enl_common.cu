@@ -1,5 +1,6 @@
 // Library-wide state: stream, sticky error word, scheme selection.
 #include <cstdio>
+#include <cstdlib>
 
 #include "enl_common.cuh"
 
@@ -15,7 +16,20 @@ void set_error(int code) {
   if (g_last_error == ENL_OK) g_last_error = code;
 }
 
+static int sync_check() {
+  static int v = -1;
+  if (v < 0) {
+    const char* s = getenv("ENL_SYNC_CHECK");
+    v = (s && s[0] == '1') ? 1 : 0;
+  }
+  return v;
+}
+
 int check_launch(const char* where) {
+  if (sync_check()) {
+    cudaError_t se = cudaDeviceSynchronize();
+    if (se != cudaSuccess) fprintf(stderr, "enlightning_gpu: %s (sync): %s\n", where, cudaGetErrorString(se));
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     fprintf(stderr, "enlightning_gpu: %s: %s\n", where, cudaGetErrorString(e));

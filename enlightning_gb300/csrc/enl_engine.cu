@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "enl_fast.cuh"
+#include "enl_mlp.cuh"
 #include "enl_rhs_cell.cuh"
 #include "enl_tma.cuh"
 
@@ -54,7 +55,10 @@ struct StageArgs {
   const int* ntiles;
   int* counter;
   int* health;
-  unsigned long long* stats;  // [level][2]: weno cells, cells
+  unsigned long long* stats;  // [level][3]: weno cells, cells, cells decided by the plain-sensor fallback
+  const float* mlp;           // learned-sensor parameters (FP32 vector) or null
+  float margin;               // |p - 0.5| <= margin -> plain sensor decides
+  float feat_eps, feat_eps_p, feat_inv_sqrt_eps;
 };
 
 // Shared-memory accessors centred on one cell of the staged halo tile.
@@ -96,41 +100,62 @@ __device__ __forceinline__ void raise_health(int* h, int code) { atomicCAS(h, 0,
 // ---------------------------------------------------------------------------
 template <int SCHEME, int ORDER, bool LLF, bool FAST>
 __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ StageArgs A) {
+  // dynamic shared memory: two FP64 staging buffers (TMA destinations, the
+  // next tile's copy overlaps the current tile's compute) + one FP32 tile
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  double* tile = reinterpret_cast<double*>(smem_raw);
-  float* tile32 = reinterpret_cast<float*>(smem_raw + kTileBytes64);
-  __shared__ __align__(8) uint64_t mbar;
-  __shared__ int s_tile;
+  double* stage_buf[2] = {reinterpret_cast<double*>(smem_raw),
+                          reinterpret_cast<double*>(smem_raw + kTileBytes64)};
+  float* tile32 = reinterpret_cast<float*>(smem_raw + 2 * kTileBytes64);
+  // learned sensor (FAST + hybrid only): network image and feature tile
+  MlpSmem* mlp_s = reinterpret_cast<MlpSmem*>(smem_raw + 2 * kTileBytes64 + kTileElems * 4);
+  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + 2 * kTileBytes64 + kTileElems * 4 +
+                                                          ((sizeof(MlpSmem) + 127) / 128) * 128);
+  __shared__ unsigned char s_flag[256];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ int s_t[2];
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ntiles = *A.ntiles;
+  auto issue = [&](int t, int b) {
+    const int4 td = A.tiles[t];
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&mbar[b], kTileBytes64);
+    // canvas column of cell i0-3 is i0 (ghost offset 3); i0 is even
+    tma_load_3d(stage_buf[b], &A.tmap[td.z & 0xff], td.x, td.y, 0, &mbar[b]);
+  };
+  const bool learned = FAST && SCHEME == kHybrid && A.mlp != nullptr;
+  if (learned) mlp_stage_params(*mlp_s, A.mlp, tid, 256);
   if (tid == 0) {
-    mbar_init(&mbar, 1);
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
     fence_mbar_init();
+    int t = atomicAdd(A.counter, 1);
+    s_t[0] = t;
+    if (t < ntiles) issue(t, 0);
   }
   __syncthreads();
-  uint32_t phase = 0;
-  for (;;) {
-    if (tid == 0) s_tile = atomicAdd(A.counter, 1);
-    __syncthreads();
-    const int t = s_tile;
-    if (t >= *A.ntiles) break;
+  uint32_t phase[2] = {0u, 0u};
+  int b = 0;
+  int t = s_t[0];
+  while (t < ntiles) {
+    if (tid == 0) {
+      int nt = atomicAdd(A.counter, 1);
+      s_t[b ^ 1] = nt;
+      if (nt < ntiles) issue(nt, b ^ 1);
+    }
+    double* tile = stage_buf[b];
     const int4 td = A.tiles[t];
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     const int i0 = td.x, j0 = td.y;
-    if (tid == 0) {
-      fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&mbar, kTileBytes64);
-      // canvas column of cell i0-3 is i0 (ghost offset 3); i0 is even
-      tma_load_3d(tile, &A.tmap[lvl], i0, j0, 0, &mbar);
-    }
-    if (!mbar_wait_bounded(&mbar, phase, kWaitIters)) {
+    if (!mbar_wait_bounded(&mbar[b], phase[b], kWaitIters)) {
       if (tid == 0) raise_health(A.health, ENL_ERR_TIMEOUT);
-      // let the copy land (bounded) before the block leaves
-      mbar_wait_bounded(&mbar, phase, kWaitIters);
+      // let copies in flight land (bounded) before the block leaves
+      mbar_wait_bounded(&mbar[b], phase[b], kWaitIters);
+      mbar_wait_bounded(&mbar[b ^ 1], phase[b ^ 1], kWaitIters);
       break;
     }
-    phase ^= 1u;
+    phase[b] ^= 1u;
     const double bdt = A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt;
     if (FAST) {
       const float rho0 = (float)A.rho0;
@@ -147,7 +172,45 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
     const bool valid = tx < w && ty < h;
     const int cc = (ty + 3) * kBW + (tx + 3);
     int flag = 0;
-    if (valid) {
+    int fallback = 0;
+    if (learned && lvl == 0) {
+      // learned switch: features -> BF16 MLP on the tensor cores (one warp per
+      // tile row, two m16 tiles) -> p; cells with |p - 0.5| <= margin fall
+      // back to the plain sensor
+      float fv[kFeat];
+      if (valid) {
+        SAcc32R acc{SAcc32{tile32, cc}};
+        cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
+      } else {
+#pragma unroll
+        for (int q = 0; q < kFeat; ++q) fv[q] = 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < kFeat; q += 2)
+        *reinterpret_cast<uint32_t*>(feat + tid * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
+      __syncwarp();
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        MlpFwd16 F;
+        mlp_forward16(*mlp_s, feat + (warp * 32 + half * 16) * kFeat, kFeat, lane, F);
+        if ((lane & 3) == 0) {
+          int c0 = warp * 32 + half * 16 + (lane >> 2);
+          s_flag[c0] = (unsigned char)(F.logit[0] > 0.f ? 2 : 1) | (fabsf(F.logit[0]) <= A.margin ? 4 : 0);
+          s_flag[c0 + 8] = (unsigned char)(F.logit[1] > 0.f ? 2 : 1) | (fabsf(F.logit[1]) <= A.margin ? 4 : 0);
+        }
+      }
+      __syncwarp();
+      if (valid) {
+        unsigned char d = s_flag[tid];
+        if (d & 4) {
+          SAcc32R acc{SAcc32{tile32, cc}};
+          flag = sensor_fast(acc, A.F[lvl]);
+          fallback = 1;
+        } else {
+          flag = (d & 2) ? 1 : 0;
+        }
+      }
+    } else if (valid) {
       if (FAST) {
         SAcc32R acc{SAcc32{tile32, cc}};
         flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
@@ -156,6 +219,7 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
         flag = rhs_switch<SCHEME, ORDER, LLF>(acc, A.P[lvl]);
       }
     }
+    const int nfb = learned ? __syncthreads_count(fallback) : 0;
     // compaction: DRP cells first, then WENO cells, each in tile order
     unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
     unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
@@ -180,8 +244,9 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
       s_list[pos] = (ty << 5) | tx | (flag << 16);
     }
     if (tid == 0 && A.stats) {
-      atomicAdd(&A.stats[2 * lvl + 0], (unsigned long long)nw);
-      atomicAdd(&A.stats[2 * lvl + 1], (unsigned long long)(nd + nw));
+      atomicAdd(&A.stats[3 * lvl + 0], (unsigned long long)nw);
+      atomicAdd(&A.stats[3 * lvl + 1], (unsigned long long)(nd + nw));
+      if (nfb) atomicAdd(&A.stats[3 * lvl + 2], (unsigned long long)nfb);
     }
     __syncthreads();
     if (tid < nd + nw) {
@@ -241,7 +306,9 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
       for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
       if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
     }
-    __syncthreads();  // tile buffers are reused by the next TMA copy
+    __syncthreads();  // this staging buffer is refilled two tiles later
+    t = s_t[b ^ 1];
+    b ^= 1;
   }
 }
 
@@ -528,15 +595,18 @@ struct PaintArgs {
   int nseg;
 };
 
+// Per-segment constants (host-computed once, like the reference computes them
+// once per segment): x0, y0, x1, y1, theta, tan(pi/2 - theta), sin, cos,
+// orientation, and a culling box outside which all three Gaussian terms
+// underflow to exactly 0 (so skipping the segment there changes nothing).
+constexpr int kSegStride = 13;
+
 __device__ double capsule_union(double H, double xc0, double xc1, const PaintArgs& A) {
-  const double PI_ = 3.14159265358979323846264338;
   for (int k = 0; k < A.nseg; ++k) {
-    const double* s = A.segs + 4 * k;
-    double theta = -atan((s[3] - s[1]) / (s[2] - s[0]));
-    int orientation = 0;
-    if (((s[0] > s[2]) && (s[1] > s[3])) || ((s[0] <= s[2]) && (s[1] >= s[3]))) orientation = 1;
-    else if (((s[0] >= s[2]) && (s[1] <= s[3])) || ((s[0] < s[2]) && (s[1] < s[3]))) orientation = 2;
-    double tn = tan(PI_ / 2.0 - theta);
+    const double* s = A.segs + kSegStride * k;
+    if (xc0 < s[9] || xc0 > s[10] || xc1 < s[11] || xc1 > s[12]) continue;
+    const int orientation = (int)s[8];
+    const double theta = s[4], tn = s[5];
     double line0 = tn * (xc0 - s[0]) + s[1];
     double line1 = tn * (xc0 - s[2]) + s[3];
     if (((orientation == 1) && (xc1 >= line0)) || ((orientation == 2) && (xc1 <= line0))) {
@@ -551,10 +621,11 @@ __device__ double capsule_union(double H, double xc0, double xc1, const PaintArg
     }
     if (((orientation == 1) && (xc1 < line0) && (xc1 > line1)) ||
         ((orientation == 2) && (xc1 > line0) && (xc1 < line1))) {
-      double d = sin(theta) * (xc0 - s[0]) + cos(theta) * (xc1 - s[1]);
+      double d = s[6] * (xc0 - s[0]) + s[7] * (xc1 - s[1]);
       double t = A.amp * exp(-A.inv_s2ln2 * (d * d));
       H = H + t - (H / A.amp) * t;
     }
+    (void)theta;
   }
   return H;
 }
@@ -683,6 +754,113 @@ __global__ void dt_kernel(unsigned long long* smax_bits, double* dt, double* tim
   *smax_bits = 0ull;
 }
 
+// Pack / unpack the patch interiors of every level (7 fields) into a dense
+// buffer: field k of the cell (tx, ty) of tile t sits at
+// k*total + off[t] + ty*w + tx.  Used to exchange the hierarchy state with
+// host memory.
+struct PackArgs {
+  CanvasView lev[kL];
+  const int4* tiles;
+  const long long* off;
+  int ntiles;
+  long long total;
+  double* packed;
+  int unpack;
+};
+
+__global__ void pack_kernel(PackArgs A) {
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    int4 td = A.tiles[t];
+    int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
+    int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    if (tx >= w || ty >= h) continue;
+    long long o = A.off[t] + ty * w + tx;
+    const CanvasView& V = A.lev[lvl];
+    for (int k = 0; k < kNF; ++k) {
+      double& c = V.at(k, td.x + tx, td.y + ty);
+      double& p = A.packed[k * A.total + o];
+      if (A.unpack) c = p;
+      else p = c;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Training-data harvest for the learned sensor (hybrid_high_llf, level 0):
+// per cell the 40 features, the exact plain switch, and the local difference
+// between the DRP and WENO right-hand sides,
+//   err = max_k dt |KK_drp,k - KK_weno,k| / scale_k,
+// computed in FP64 from the current buffer (ghosts filled by the caller).
+// Every WENO-flagged cell is kept; DRP cells are kept with probability
+// keep0 (hash of the cell and `seed`).
+// ---------------------------------------------------------------------------
+struct HarvestArgs {
+  CanvasView V;
+  CanvasView H;
+  RhsConst P;
+  float eps, eps_p, inv_sqrt_eps, rho0, p0, T0;
+  const int4* tiles;
+  int off, cnt;
+  double dt;
+  double inv_scale[5];
+  unsigned keep0, seed;
+  __nv_bfloat16* X;
+  float* lab;  // (flag, err) per row
+  unsigned long long* count;
+  long cap;
+};
+
+struct CanvasAcc64 {
+  const CanvasView* V;
+  int i, j;
+  __device__ double w(int k, int di, int dj) const { return V->at(k, i + di, j + dj); }
+  __device__ double p(int di, int dj) const { return V->at(5, i + di, j + dj); }
+  __device__ double t(int di, int dj) const { return V->at(6, i + di, j + dj); }
+};
+struct CanvasAcc32 {
+  const CanvasView* V;
+  int i, j;
+  double rho0, p0;
+  __device__ float w(int k, int di, int dj) const { return (float)(V->at(k, i + di, j + dj) - (k == 0 ? rho0 : 0.0)); }
+  __device__ float p(int di, int dj) const { return (float)(V->at(5, i + di, j + dj) - p0); }
+};
+
+__global__ void harvest_kernel(HarvestArgs A) {
+  for (int t = blockIdx.x; t < A.cnt; t += gridDim.x) {
+    int4 td = A.tiles[A.off + t];
+    int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
+    int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    if (tx >= w || ty >= h) continue;
+    int i = td.x + tx, j = td.y + ty;
+    CanvasAcc64 a64{&A.V, i, j};
+    int flag = rhs_switch<kHybrid, 5, true>(a64, A.P);
+    if (!flag) {
+      unsigned hsh = (unsigned)i * 73856093u ^ (unsigned)j * 19349663u ^ A.seed * 83492791u;
+      hsh ^= hsh >> 13;
+      hsh *= 0x5bd1e995u;
+      hsh ^= hsh >> 15;
+      if (hsh > A.keep0) continue;
+    }
+    double H[5], Kd[5], Kw[5];
+    H[0] = A.H.at(0, i, j);
+    rhs_sources(a64, A.P, H);
+    double H2[5] = {H[0], H[1], H[2], H[3], H[4]};
+    rhs_fluxes<kHybrid, 5, true>(a64, A.P, j, 0, H, Kd);
+    rhs_fluxes<kHybrid, 5, true>(a64, A.P, j, 1, H2, Kw);
+    double err = 0.0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) err = fmax(err, A.dt * fabs(Kd[k] - Kw[k]) * A.inv_scale[k]);
+    unsigned long long idx = atomicAdd(A.count, 1ull);
+    if ((long)idx >= A.cap) continue;
+    CanvasAcc32 a32{&A.V, i, j, (double)A.rho0, (double)A.p0};
+    float fv[kFeat];
+    cell_features(a32, A.eps, A.eps_p, A.inv_sqrt_eps, fv);
+    for (int q = 0; q < kFeat; ++q) A.X[(long)idx * kFeat + q] = __float2bfloat16_rn(fv[q]);
+    A.lab[2 * idx] = (float)flag;
+    A.lab[2 * idx + 1] = (float)err;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -754,9 +932,19 @@ struct Engine {
   size_t bmap_cap = 0;
   double* d_segs = nullptr;
   size_t segs_cap = 0;
+  float* d_mlp = nullptr;    // learned-sensor parameters
+  float margin = 0.f;
   int adaptive = 0;          // device-computed dt
   double cfl = 0.5;
   double* d_dt = nullptr;    // [0] = dt of the current step, [1] = simulated time
+  int profile = 0;            // time each stage-kernel launch with events
+  cudaEvent_t pev[6] = {};
+  double prof_ms = 0.0;
+  long long prof_launches = 0, prof_cells = 0;
+  DevArray<long long> d_tileoff;
+  std::vector<long long> h_tileoff;
+  double* d_packed = nullptr;
+  size_t packed_cap = 0;
   unsigned long long* d_smax = nullptr;
   int nsm = 148;
   int stage_blocks = 0;
@@ -868,6 +1056,17 @@ static int rebuild_tables(Engine* E) {
     E->h_meta[M_CT_CNT + l] = (int)E->h_ctiles.size() - E->h_meta[M_CT_OFF + l];
   }
   E->h_meta[M_NTILES] = (int)E->h_tiles.size();
+  E->h_tileoff.resize(E->h_tiles.size());
+  long long acc = 0;
+  for (size_t q = 0; q < E->h_tiles.size(); ++q) {
+    E->h_tileoff[q] = acc;
+    int4 td = E->h_tiles[q];
+    acc += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
+  }
+  E->d_tileoff.ensure(std::max<size_t>(E->h_tileoff.size(), 1));
+  if (!E->h_tileoff.empty())
+    cudaMemcpyAsync(E->d_tileoff.p, E->h_tileoff.data(), E->h_tileoff.size() * sizeof(long long),
+                    cudaMemcpyHostToDevice, stream());
   bool grew = false;
   grew |= E->d_tiles.ensure(std::max<size_t>(E->h_tiles.size(), 1));
   grew |= E->d_halo.ensure(std::max<size_t>(E->h_halo.size(), 1));
@@ -956,6 +1155,11 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.counter = E->d_counters + stage;
   A.health = E->d_health;
   A.stats = E->d_stats;
+  A.mlp = (E->cfg.learned && E->cfg.precision == ENL_PREC_FP32) ? E->d_mlp : nullptr;
+  A.margin = E->margin;
+  A.feat_eps = (float)A.P[0].sensor_eps;
+  A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
+  A.feat_inv_sqrt_eps = (float)(1.0 / sqrt(A.P[0].sensor_eps));
   return A;
 }
 
@@ -1055,10 +1259,24 @@ static int step_fused(Engine* E, double dt) {
     fill_all(E, in);
     StageArgs A = stage_args(E, st, dt);
     void* args[] = {&A};
+    if (E->profile) cudaEventRecord(E->pev[2 * st], s);
     cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
+    if (E->profile) cudaEventRecord(E->pev[2 * st + 1], s);
     absorb_all(E, out);
   }
   coarsen_all(E);
+  if (E->profile) {
+    cudaEventSynchronize(E->pev[5]);
+    long long cells = 0;
+    for (auto& td : E->h_tiles) cells += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
+    for (int st = 0; st < 3; ++st) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, E->pev[2 * st], E->pev[2 * st + 1]);
+      E->prof_ms += ms;
+      E->prof_launches += 1;
+      E->prof_cells += cells;
+    }
+  }
   return check_launch("engine step");
 }
 
@@ -1165,13 +1383,15 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMalloc(&E->d_counters, 4 * sizeof(int));
   cudaMalloc(&E->d_health, sizeof(int));
   cudaMemset(E->d_health, 0, sizeof(int));
-  cudaMalloc(&E->d_stats, 2 * kL * sizeof(unsigned long long));
-  cudaMemset(E->d_stats, 0, 2 * kL * sizeof(unsigned long long));
+  cudaMalloc(&E->d_stats, 3 * kL * sizeof(unsigned long long));
+  cudaMemset(E->d_stats, 0, 3 * kL * sizeof(unsigned long long));
   cudaMalloc(&E->d_dt, 2 * sizeof(double));
   cudaMemset(E->d_dt, 0, 2 * sizeof(double));
   cudaMalloc(&E->d_smax, sizeof(unsigned long long));
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
-  E->smem_bytes = kTileBytes64 + (cfg->precision == ENL_PREC_FP32 ? kTileElems * 4 : 0);
+  E->smem_bytes = 2 * kTileBytes64 + (cfg->precision == ENL_PREC_FP32 ? kTileElems * 4 : 0);
+  if (cfg->precision == ENL_PREC_FP32 && cfg->learned)
+    E->smem_bytes += ((sizeof(MlpSmem) + 127) / 128) * 128 + 256 * kFeat * sizeof(__nv_bfloat16);
   StageFn fn = cfg->precision == ENL_PREC_FP32 ? pick_stage<true>(cfg->variant) : pick_stage<false>(cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
   int per_sm = 0;
@@ -1206,6 +1426,10 @@ int enl_engine_destroy(void* e) {
     if (E->d_tags[l]) cudaFree(E->d_tags[l]);
   if (E->d_bmap) cudaFree(E->d_bmap);
   if (E->d_dt) cudaFree(E->d_dt);
+  if (E->d_mlp) cudaFree(E->d_mlp);
+  if (E->d_packed) cudaFree(E->d_packed);
+  for (int q = 0; q < 6; ++q)
+    if (E->pev[q]) cudaEventDestroy(E->pev[q]);
   if (E->d_smax) cudaFree(E->d_smax);
   if (E->d_segs) cudaFree(E->d_segs);
   if (E->graph) cudaGraphExecDestroy(E->graph);
@@ -1381,10 +1605,10 @@ int enl_engine_tag(void* e, int level, int* tags) {
 int enl_engine_stats(void* e, long long* counts) {
   Engine* E = (Engine*)e;
   if (!E || !counts) return ENL_ERR_ARG;
-  unsigned long long h[2 * kL];
+  unsigned long long h[3 * kL];
   cudaMemcpyAsync(h, E->d_stats, sizeof(h), cudaMemcpyDeviceToHost, stream());
   cudaStreamSynchronize(stream());
-  for (int q = 0; q < 2 * kL; ++q) counts[q] = (long long)h[q];
+  for (int q = 0; q < 3 * kL; ++q) counts[q] = (long long)h[q];
   cudaMemsetAsync(E->d_stats, 0, sizeof(h), stream());
   return check_launch("engine stats");
 }
@@ -1447,7 +1671,32 @@ int enl_engine_paint_source(void* e, int level, int type, int mode, double amp, 
   A.dx0 = L.dx[0];
   A.dx1 = L.dx[1];
   if (type == 30 && nseg > 0) {
-    size_t need = (size_t)nseg * 4;
+    size_t need = (size_t)nseg * kSegStride;
+    std::vector<double> pre(need);
+    const double PI_ = 3.14159265358979323846264338;
+    // exp(-ln2 d^2/spread^2) underflows to 0 beyond d = 32.8 spread
+    const double cull = 40.0 * spread;
+    for (int k = 0; k < nseg; ++k) {
+      const double* c = segs + 4 * k;
+      double* o = pre.data() + (size_t)kSegStride * k;
+      double theta = -atan((c[3] - c[1]) / (c[2] - c[0]));
+      int orientation = 0;
+      if (((c[0] > c[2]) && (c[1] > c[3])) || ((c[0] <= c[2]) && (c[1] >= c[3]))) orientation = 1;
+      else if (((c[0] >= c[2]) && (c[1] <= c[3])) || ((c[0] < c[2]) && (c[1] < c[3]))) orientation = 2;
+      o[0] = c[0];
+      o[1] = c[1];
+      o[2] = c[2];
+      o[3] = c[3];
+      o[4] = theta;
+      o[5] = tan(PI_ / 2.0 - theta);
+      o[6] = sin(theta);
+      o[7] = cos(theta);
+      o[8] = orientation;
+      o[9] = std::min(c[0], c[2]) - cull;
+      o[10] = std::max(c[0], c[2]) + cull;
+      o[11] = std::min(c[1], c[3]) - cull;
+      o[12] = std::max(c[1], c[3]) + cull;
+    }
     if (need > E->segs_cap) {
       if (E->d_segs) cudaFree(E->d_segs);
       if (cudaMalloc(&E->d_segs, need * sizeof(double)) != cudaSuccess) {
@@ -1458,7 +1707,7 @@ int enl_engine_paint_source(void* e, int level, int type, int mode, double amp, 
       }
       E->segs_cap = need;
     }
-    cudaMemcpyAsync(E->d_segs, segs, need * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(E->d_segs, pre.data(), need * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
     A.segs = E->d_segs;
     A.nseg = nseg;
@@ -1507,8 +1756,6 @@ int enl_engine_tag_blocks(void* e, int level, int block, int buffer, unsigned ch
   size_t nb = (size_t)nbx * nby;
   if (nb > E->bmap_cap) {
     if (E->d_bmap) cudaFree(E->d_bmap);
-  if (E->d_dt) cudaFree(E->d_dt);
-  if (E->d_smax) cudaFree(E->d_smax);
     if (cudaMalloc(&E->d_bmap, nb) != cudaSuccess) {
       E->d_bmap = nullptr;
       E->bmap_cap = 0;
@@ -1546,6 +1793,135 @@ int enl_engine_time(void* e, double* dt_last, double* sim_time) {
   if (dt_last) *dt_last = h[0];
   if (sim_time) *sim_time = h[1];
   return check_launch("engine time");
+}
+
+static long long packed_cells(Engine* E) {
+  if (E->h_tiles.empty()) return 0;
+  int4 td = E->h_tiles.back();
+  return E->h_tileoff.back() + (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
+}
+
+int enl_engine_packed_size(void* e, long long* ndoubles) {
+  Engine* E = (Engine*)e;
+  if (!E || !ndoubles) return ENL_ERR_ARG;
+  *ndoubles = packed_cells(E) * kNF;
+  return ENL_OK;
+}
+
+static int pack_common(Engine* E, double* host, int unpack) {
+  long long cells = packed_cells(E);
+  if (cells == 0) return ENL_OK;
+  size_t need = (size_t)cells * kNF;
+  if (need > E->packed_cap) {
+    if (E->d_packed) cudaFree(E->d_packed);
+    if (cudaMalloc(&E->d_packed, need * sizeof(double)) != cudaSuccess) {
+      E->d_packed = nullptr;
+      E->packed_cap = 0;
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+    E->packed_cap = need;
+  }
+  cudaStream_t s = stream();
+  PackArgs A;
+  memset(&A, 0, sizeof(A));
+  for (int l = 0; l < E->cfg.nlevels; ++l) A.lev[l] = E->lev[l].view(0);
+  A.tiles = E->d_tiles.p;
+  A.off = E->d_tileoff.p;
+  A.ntiles = (int)E->h_tiles.size();
+  A.total = cells;
+  A.packed = E->d_packed;
+  A.unpack = unpack;
+  if (unpack) cudaMemcpyAsync(E->d_packed, host, need * sizeof(double), cudaMemcpyHostToDevice, s);
+  pack_kernel<<<std::min(A.ntiles, E->nsm * 8), 256, 0, s>>>(A);
+  if (!unpack) cudaMemcpyAsync(host, E->d_packed, need * sizeof(double), cudaMemcpyDeviceToHost, s);
+  return check_launch(unpack ? "engine upload" : "engine download");
+}
+
+int enl_engine_download(void* e, double* host) {
+  Engine* E = (Engine*)e;
+  if (!E || !host) return ENL_ERR_ARG;
+  return pack_common(E, host, 0);
+}
+
+int enl_engine_upload(void* e, const double* host) {
+  Engine* E = (Engine*)e;
+  if (!E || !host) return ENL_ERR_ARG;
+  return pack_common(E, const_cast<double*>(host), 1);
+}
+
+int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, long long* cells) {
+  Engine* E = (Engine*)e;
+  if (!E) return ENL_ERR_ARG;
+  if (ms_total) *ms_total = E->prof_ms;
+  if (launches) *launches = E->prof_launches;
+  if (cells) *cells = E->prof_cells;
+  E->prof_ms = 0.0;
+  E->prof_launches = 0;
+  E->prof_cells = 0;
+  if (on && !E->pev[0])
+    for (int q = 0; q < 6; ++q) cudaEventCreate(&E->pev[q]);
+  E->profile = on ? 1 : 0;
+  return check_launch("engine profile");
+}
+
+int enl_engine_set_mlp(void* e, const float* params_host, float margin) {
+  Engine* E = (Engine*)e;
+  if (!E || !params_host || margin < 0.f) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  if (!(E->cfg.precision == ENL_PREC_FP32 && E->cfg.learned)) {
+    set_error(ENL_ERR_STATE);
+    return ENL_ERR_STATE;
+  }
+  if (!E->d_mlp && cudaMalloc(&E->d_mlp, kNParams * sizeof(float)) != cudaSuccess) {
+    E->d_mlp = nullptr;
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  cudaMemcpyAsync(E->d_mlp, params_host, kNParams * sizeof(float), cudaMemcpyHostToDevice, stream());
+  cudaStreamSynchronize(stream());
+  E->margin = margin;
+  return check_launch("set_mlp");
+}
+
+int enl_engine_harvest(void* e, int level, double dt, const double* scale, double keep0, unsigned seed, void* X,
+                       float* labels, long capacity, unsigned long long* count_dev) {
+  Engine* E = (Engine*)e;
+  if (!E || level < 0 || level >= E->cfg.nlevels || !scale || !X || !labels || !count_dev || capacity < 0) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  const auto& c = E->cfg;
+  Level& L = E->lev[level];
+  fill_all(E, 0);
+  HarvestArgs A;
+  memset(&A, 0, sizeof(A));
+  A.V = L.view(0);
+  A.H = L.view(3);
+  double xlo[2] = {c.xlo[0], c.xlo[1]};
+  A.P = make_rhs_const(xlo, L.dx, c.weno_alpha, c.kappa, c.mu, c.muB, c.R, c.T_star_n, c.tau_n, c.tol, 0, c.c,
+                       c.c_lr);
+  A.eps = (float)A.P.sensor_eps;
+  A.eps_p = (float)(A.P.sensor_eps * (c.c * c.c) * (c.c * c.c));
+  A.inv_sqrt_eps = (float)(1.0 / sqrt(A.P.sensor_eps));
+  A.rho0 = (float)c.rho0;
+  A.p0 = (float)c.p0;
+  A.T0 = (float)c.T0;
+  A.tiles = E->d_tiles.p;
+  A.off = E->tile_off[level];
+  A.cnt = E->tile_cnt[level];
+  A.dt = dt;
+  for (int k = 0; k < 5; ++k) A.inv_scale[k] = 1.0 / scale[k];
+  A.keep0 = (unsigned)(std::min(1.0, std::max(0.0, keep0)) * 4294967295.0);
+  A.seed = seed;
+  A.X = (__nv_bfloat16*)X;
+  A.lab = labels;
+  A.count = count_dev;
+  A.cap = capacity;
+  if (A.cnt) harvest_kernel<<<std::min(A.cnt, E->nsm * 16), 256, 0, stream()>>>(A);
+  return check_launch("harvest");
 }
 
 }  // extern "C"

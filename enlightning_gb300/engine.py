@@ -135,9 +135,10 @@ class Engine:
         return int(self.L.enl_engine_launches_per_step(self.h, int(plain)))
 
     def stats(self):
-        arr = (C.c_longlong * (2 * MAX_LEVELS))()
+        """Per level: [WENO cells, cells, cells decided by the plain fallback] since the last call."""
+        arr = (C.c_longlong * (3 * MAX_LEVELS))()
         _lib.check(self.L.enl_engine_stats(self.h, arr), "enl_engine_stats")
-        a = np.array(arr[:], dtype=np.int64).reshape(MAX_LEVELS, 2)
+        a = np.array(arr[:], dtype=np.int64).reshape(MAX_LEVELS, 3)
         return a[: self.nlevels]
 
     def health(self):
@@ -148,6 +149,59 @@ class Engine:
         tags = torch.zeros((ny, nx), dtype=torch.int32, device="cuda")
         _lib.check(self.L.enl_engine_tag(self.h, level, C.c_void_p(tags.data_ptr())), "enl_engine_tag")
         return tags
+
+    def set_mlp(self, params, margin):
+        """Install the learned switch (FP32 parameter vector) in a learned FP32 engine."""
+        P = np.ascontiguousarray(np.asarray(params, np.float32))
+        _lib.check(self.L.enl_engine_set_mlp(self.h, P.ctypes.data_as(C.c_void_p), float(margin)),
+                   "enl_engine_set_mlp")
+
+    def profile(self, on=True):
+        """Switch stage-kernel event timing; returns (ms, launches, cells) since the last call."""
+        ms, n, c = C.c_double(), C.c_longlong(), C.c_longlong()
+        _lib.check(self.L.enl_engine_profile(self.h, int(on), C.byref(ms), C.byref(n), C.byref(c)),
+                   "enl_engine_profile")
+        return ms.value, n.value, c.value
+
+    def packed_size(self):
+        n = C.c_longlong()
+        _lib.check(self.L.enl_engine_packed_size(self.h, C.byref(n)), "enl_engine_packed_size")
+        return n.value
+
+    def download(self, host: torch.Tensor):
+        _lib.check(self.L.enl_engine_download(self.h, C.c_void_p(host.data_ptr())), "enl_engine_download")
+
+    def upload(self, host: torch.Tensor):
+        _lib.check(self.L.enl_engine_upload(self.h, C.c_void_p(host.data_ptr())), "enl_engine_upload")
+
+    def set_adaptive_dt(self, on=True, cfl=0.5):
+        _lib.check(self.L.enl_engine_set_adaptive_dt(self.h, int(on), float(cfl)), "enl_engine_set_adaptive_dt")
+
+    def time(self):
+        dt, t = C.c_double(), C.c_double()
+        _lib.check(self.L.enl_engine_time(self.h, C.byref(dt), C.byref(t)), "enl_engine_time")
+        return dt.value, t.value
+
+    def paint_source(self, level, src_type, mode=10, amp=1.0, spread=1.0, pos=(0.0, 0.0), sine_amp=0.0,
+                     sine_freq=0.0, segs=None, drive=1.0):
+        """enlightning::addSource on one level (types 10 POINT, 20 SINE, 30 LIGHTNING)."""
+        segarr = np.ascontiguousarray(np.asarray(segs if segs is not None else np.zeros((0, 4)), np.float64))
+        nseg = segarr.shape[0]
+        _lib.check(self.L.enl_engine_paint_source(
+            self.h, level, int(src_type), int(mode), float(amp), float(spread), _lib.darr(pos), float(sine_amp),
+            float(sine_freq), nseg, segarr.ctypes.data_as(C.POINTER(C.c_double)), float(drive)),
+            "enl_engine_paint_source")
+
+    def state_from_overpressure(self, level):
+        _lib.check(self.L.enl_engine_state_from_overpressure(self.h, level), "enl_engine_state_from_overpressure")
+
+    def tag_blocks(self, level, block, buffer):
+        nbx, nby = C.c_int(), C.c_int()
+        _lib.check(self.L.enl_engine_tag_blocks(self.h, level, block, buffer, None, C.byref(nbx), C.byref(nby)))
+        m = np.zeros((nby.value, nbx.value), np.uint8)
+        _lib.check(self.L.enl_engine_tag_blocks(self.h, level, block, buffer, m.ctypes.data_as(C.c_void_p),
+                                                C.byref(nbx), C.byref(nby)), "enl_engine_tag_blocks")
+        return m.astype(bool)
 
     # -- state I/O ----------------------------------------------------------
     def set_level_state(self, level, w, pres, temp, which=0):
@@ -181,16 +235,21 @@ class Hierarchy:
 
     Follows the reference's gridding loop (main.C:489-502 with
     StandardTagAndInitialize + BergerRigoutsos, input.txt:103-127): tag cells
-    of level l with tag_cells (fortran/tag_cells.m4), grow the tags by
-    tag_buffer cells, cluster them into boxes of efficiency >= 0.7 with sides
-    between min_size and max_size, refine the boxes by the ratio, and keep
-    them properly nested inside level l.
+    of level l with tag_cells (fortran/tag_cells.m4, on the device), grow the
+    tags by tag_buffer cells, cluster them into boxes of efficiency >= 0.7 with
+    sides between min_size and max_size (level l+1 cells), refine the boxes by
+    the ratio and keep them properly nested inside level l.  Tags reach the
+    host as a map of block x block cells (the device folds the tag buffer into
+    that reduction), so clustering works on 1/block^2 of the cells and patch
+    corners fall on block boundaries.
     """
 
-    def __init__(self, engine: Engine, min_size=16, max_size=256, tag_buffer=2, efficiency=0.7, nest=2):
+    def __init__(self, engine: Engine, min_size=16, max_size=256, tag_buffer=2, efficiency=0.7, block=4,
+                 nest_blocks=1):
         self.E = engine
         self.min_size, self.max_size = min_size, max_size
-        self.tag_buffer, self.efficiency, self.nest = tag_buffer, efficiency, nest
+        self.tag_buffer, self.efficiency = tag_buffer, efficiency
+        self.block, self.nest_blocks = block, nest_blocks
 
     def base_patches(self, size=256):
         nx, ny = self.E.level_shape(0)
@@ -201,32 +260,41 @@ class Hierarchy:
         self.E.set_patches(0, boxes)
         return boxes
 
-    def _nesting_mask(self, level):
-        """Cells of `level` index space that may carry level+1 patches."""
-        nx, ny = self.E.level_shape(level)
-        m = np.zeros((ny, nx), bool)
+    def _nesting_blocks(self, level, nbx, nby):
+        B = self.block
+        m = np.zeros((nby, nbx), bool)
         for b in self.E.patches[level]:
-            m[b[2]:b[3] + 1, b[0]:b[1] + 1] = True
-        if self.nest > 0:
+            bx0, bx1 = -(-b[0] // B), (b[1] + 1) // B - 1
+            by0, by1 = -(-b[2] // B), (b[3] + 1) // B - 1
+            if bx1 >= bx0 and by1 >= by0:
+                m[by0:by1 + 1, bx0:bx1 + 1] = True
+        if self.nest_blocks > 0 and level > 0:
             from scipy.ndimage import binary_erosion
-            m = binary_erosion(m, iterations=self.nest, border_value=1)
+            m = binary_erosion(m, structure=np.ones((3, 3), bool), iterations=self.nest_blocks, border_value=1)
         return m
 
-    def regrid_level(self, level, tags=None):
+    def propose(self, level):
+        """Fine boxes (level+1 index space) from the current tags of `level`."""
+        E, B, r = self.E, self.block, self.E.ratio
+        bmap = E.tag_blocks(level, B, self.tag_buffer)
+        bmap &= self._nesting_blocks(level, bmap.shape[1], bmap.shape[0])
+        cell = B * r  # level+1 cells per block side
+        cboxes = cluster_tags(bmap, efficiency=self.efficiency, min_size=max(1, self.min_size // cell),
+                              max_size=max(1, self.max_size // cell))
+        nxf, nyf = E.level_shape(level + 1)
+        fine = []
+        for b in cboxes:
+            fb = (b[0] * cell, min(nxf, (b[1] + 1) * cell) - 1, b[2] * cell, min(nyf, (b[3] + 1) * cell) - 1)
+            if fb[1] >= fb[0] and fb[3] >= fb[2]:
+                fine.append(fb)
+        return fine
+
+    def regrid_level(self, level):
         """Rebuild level+1 from the tags of `level`; returns the new boxes."""
         E = self.E
         if level + 1 >= E.nlevels:
             return []
-        if tags is None:
-            tags = E.tag(level).cpu().numpy().astype(bool)
-        if self.tag_buffer > 0 and tags.any():
-            from scipy.ndimage import binary_dilation
-            tags = binary_dilation(tags, iterations=self.tag_buffer)
-        tags &= self._nesting_mask(level)
-        r = E.ratio
-        cboxes = cluster_tags(tags, efficiency=self.efficiency, min_size=max(1, self.min_size // r),
-                              max_size=max(2, self.max_size // r))
-        fine = [(b[0] * r, (b[1] + 1) * r - 1, b[2] * r, (b[3] + 1) * r - 1) for b in cboxes]
+        fine = self.propose(level)
         old = list(E.patches[level + 1])
         new_regions = box_difference(fine, old)
         E.set_patches(level + 1, fine)
@@ -235,10 +303,7 @@ class Hierarchy:
 
     def regrid(self):
         """Regrid every finer level, coarse to fine (regridAllFinerLevels)."""
-        out = []
-        for l in range(self.E.nlevels - 1):
-            out.append(self.regrid_level(l))
-        return out
+        return [self.regrid_level(l) for l in range(self.E.nlevels - 1)]
 
 
 def box_difference(boxes, remove):

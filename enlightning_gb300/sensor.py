@@ -1,0 +1,277 @@
+"""Learned hybrid sensor: harvest, training and evaluation (GPU).
+
+The reference's hybrid switch (fortran/rhs_hybrid_high_llf.m4:239-256) sends
+a level-0 cell to WENO when any of six density-ratio tests falls below
+0.9999; with the test's small epsilon it does so for almost every cell that a
+wave of any amplitude has reached.  The learned switch predicts, from 40
+stencil features, whether WENO actually changes the right-hand side there:
+
+  label y = 1  iff  the plain switch says WENO  and
+                    err = max_k dt |KK_drp,k - KK_weno,k| / scale_k > tau
+
+where KK_drp and KK_weno are the two right-hand sides of the same cell in
+FP64 (harvested by enl_engine_harvest from trajectories of the batched
+engine).  Training runs entirely on the GPU with the library's BF16
+tensor-core forward/backward kernels (enl_mlp_grad) and Adam (enl_mlp_adam).
+At run time the plain switch still decides every cell whose logit lies within
++-margin of 0, and it remains the reference the learned run is measured
+against.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import math
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import default_params
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WEIGHTS = os.path.join(HERE, "learned_sensor.npz")
+NF = 40
+
+
+def nparams():
+    return int(_lib.lib().enl_mlp_nparams())
+
+
+def load_weights(path=WEIGHTS):
+    d = np.load(path)
+    return d["params"].astype(np.float32), float(d["margin"])
+
+
+def init_params(seed=0):
+    rng = np.random.default_rng(seed)
+    n = nparams()
+    P = np.zeros(n, np.float32)
+    P[0:40 * 64] = rng.normal(0, math.sqrt(2.0 / 40), 40 * 64)
+    o = 40 * 64 + 64
+    P[o:o + 64 * 64] = rng.normal(0, math.sqrt(2.0 / 64), 64 * 64)
+    o += 64 * 64 + 64
+    P[o:o + 64] = rng.normal(0, math.sqrt(1.0 / 64), 64)
+    return P
+
+
+def state_scales(prm):
+    """Per-field scales of the harvest error: rho0, rho0 c, rho0 c, rho0 c_v, rho0 T0."""
+    r = prm["rho0"]
+    return np.array([r, r * prm["c"], r * prm["c"], r * prm["c_v"], r * prm["T0"]], np.float64)
+
+
+class Harvest:
+    """Device buffers receiving harvested rows."""
+
+    def __init__(self, capacity):
+        self.cap = int(capacity)
+        self.X = torch.zeros((self.cap, NF), dtype=torch.bfloat16, device="cuda")
+        self.lab = torch.zeros((self.cap, 2), dtype=torch.float32, device="cuda")
+        self.count = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+    def take(self, engine, level, dt, prm, keep0, seed):
+        sc = (C.c_double * 5)(*state_scales(prm))
+        _lib.check(engine.L.enl_engine_harvest(engine.h, level, float(dt), sc, float(keep0), int(seed) & 0xffffffff,
+                                               C.c_void_p(self.X.data_ptr()), C.c_void_p(self.lab.data_ptr()),
+                                               self.cap, C.c_void_p(self.count.data_ptr())), "enl_engine_harvest")
+
+    def rows(self):
+        n = min(int(self.count.item()), self.cap)
+        return self.X[:n], self.lab[:n]
+
+
+def labels(lab, tau):
+    flag = lab[:, 0] > 0.5
+    err = lab[:, 1]
+    return (flag & (err > tau)).float()
+
+
+def class_weights(y, pos_boost=4.0):
+    n = y.numel()
+    npos = float(y.sum().item())
+    nneg = n - npos
+    wp = pos_boost * n / max(1.0, 2.0 * npos)
+    wn = n / max(1.0, 2.0 * nneg)
+    return torch.where(y > 0.5, torch.full_like(y, wp), torch.full_like(y, wn))
+
+
+def train(X, y, w, params=None, epochs=20, batch=65536, lr=3e-3, seed=0, log=None):
+    """Adam on the device with the library's tensor-core gradient kernel."""
+    L = _lib.lib()
+    n = X.shape[0]
+    P = torch.tensor(params if params is not None else init_params(seed), device="cuda")
+    m = torch.zeros_like(P)
+    v = torch.zeros_like(P)
+    g = torch.zeros_like(P)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    step = 0
+    hist = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, device="cuda", generator=gen)
+        loss.zero_()
+        for b0 in range(0, n, batch):
+            idx = perm[b0:b0 + batch]
+            xb = X[idx].contiguous()
+            yb = y[idx].contiguous()
+            wb = w[idx].contiguous()
+            g.zero_()
+            _lib.check(L.enl_mlp_grad(C.c_void_p(xb.data_ptr()), C.c_void_p(yb.data_ptr()),
+                                      C.c_void_p(wb.data_ptr()), xb.shape[0], C.c_void_p(P.data_ptr()),
+                                      C.c_void_p(g.data_ptr()), C.c_void_p(loss.data_ptr())), "enl_mlp_grad")
+            step += 1
+            inv = 1.0 / max(1e-30, float(wb.sum().item()))
+            lr_t = lr * 0.5 * (1 + math.cos(math.pi * min(1.0, ep / max(1, epochs))))
+            _lib.check(L.enl_mlp_adam(C.c_void_p(P.data_ptr()), C.c_void_p(g.data_ptr()), C.c_void_p(m.data_ptr()),
+                                      C.c_void_p(v.data_ptr()), lr_t, 0.9, 0.999, 1e-8, inv, step), "enl_mlp_adam")
+        hist.append(float(loss.item()) / max(1e-30, float(w.sum().item())))
+        if log:
+            log(f"epoch {ep}: loss {hist[-1]:.5f}")
+    return P.cpu().numpy(), hist
+
+
+def logits(X, params):
+    L = _lib.lib()
+    P = torch.as_tensor(params, device="cuda")
+    out = torch.zeros(X.shape[0], dtype=torch.float32, device="cuda")
+    _lib.check(L.enl_mlp_forward(C.c_void_p(X.data_ptr()), X.shape[0], C.c_void_p(P.data_ptr()),
+                                 C.c_void_p(out.data_ptr())), "enl_mlp_forward")
+    return out
+
+
+def harvest_line_source(H, seeds, steps=30, every=10, keep0=0.05, prm=None, log=None, **kw):
+    from . import workloads
+    from .engine import PREC_FP32
+    prm = prm or default_params()
+    for sd in seeds:
+        E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32, **kw)
+        for s in range(steps):
+            if s and s % 10 == 0:
+                Hy.regrid()
+            E.step(1.0)
+            if (s + 1) % every == 0:
+                dt, _ = E.time()
+                H.take(E, 0, dt, prm, keep0, sd * 1000 + s)
+        if log:
+            log(f"line source seed {sd}: {int(H.count.item())} rows")
+        E.close()
+
+
+def harvest_shock(H, seeds, steps=40, every=10, keep0=0.05, prm=None, log=None, **kw):
+    from . import workloads
+    prm = prm or default_params()
+    for sd in seeds:
+        E, Hy = workloads.mach_shock(prm, seed=sd, **kw)
+        for s in range(steps):
+            if s and s % 10 == 0:
+                Hy.regrid()
+            E.step(1.0)
+            if (s + 1) % every == 0:
+                dt, _ = E.time()
+                H.take(E, 0, dt, prm, keep0, 77 + sd * 1000 + s)
+        if log:
+            log(f"shock seed {sd}: {int(H.count.item())} rows")
+        E.close()
+
+
+def evaluate(params, margin, seeds=(100, 101, 102, 103, 104), steps=40, prm=None, log=None, **kw):
+    """Learned vs plain-switch runs of the FP32 engine on held-out seeds:
+    WENO fractions (level 0 and all levels), fallback fraction, and the
+    relative L2 difference of the final level-0 states."""
+    from . import workloads
+    from .engine import PREC_FP32
+    prm = prm or default_params()
+    rows = []
+    for sd in seeds:
+        res = {}
+        for learned in (False, True):
+            E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32, learned=learned, **kw)
+            if learned:
+                E.set_mlp(params, margin)
+            E.stats()
+            t0 = time.perf_counter()
+            for s in range(steps):
+                if s and s % 10 == 0:
+                    Hy.regrid()
+                E.step(1.0)
+            torch.cuda.synchronize()
+            st = E.stats()
+            res[learned] = dict(state=E.level_state(0).cpu().numpy().copy(),
+                                weno0=float(st[0, 0] / max(1, st[0, 1])),
+                                weno=float(st[:, 0].sum() / max(1, st[:, 1].sum())),
+                                fallback0=float(st[0, 2] / max(1, st[0, 1])), secs=time.perf_counter() - t0,
+                                health=E.health())
+            E.close()
+        a, b = res[True]["state"], res[False]["state"]
+        err = {}
+        for k, nm in enumerate(["rho", "rho_u", "rho_v", "rho_s", "rho_Tn", "p", "T"]):
+            err[nm] = float(np.linalg.norm(a[k] - b[k]) / max(1e-300, np.linalg.norm(b[k])))
+        err["rho-rho0"] = float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0] - prm["rho0"]))
+        err["p-p0"] = float(np.linalg.norm(a[5] - b[5]) / np.linalg.norm(b[5] - prm["p0"]))
+        row = dict(seed=sd, err=err, weno0_plain=res[False]["weno0"], weno0_learned=res[True]["weno0"],
+                   weno_plain=res[False]["weno"], weno_learned=res[True]["weno"],
+                   fallback0=res[True]["fallback0"], health=(res[False]["health"], res[True]["health"]))
+        rows.append(row)
+        if log:
+            log(json.dumps(row))
+    return rows
+
+
+def main(out_dir="gpurun_out", quick=False):
+    torch.cuda.set_device(0)
+    torch.cuda.set_stream(torch.cuda.Stream())
+    prm = default_params()
+    logf = open(os.path.join(out_dir, "sensor_train.log"), "w")
+
+    def log(msg):
+        print(msg, flush=True)
+        logf.write(msg + "\n")
+        logf.flush()
+
+    H = Harvest(6_000_000 if not quick else 400_000)
+    seeds = range(10) if not quick else range(2)
+    t0 = time.perf_counter()
+    harvest_line_source(H, seeds, log=log)
+    harvest_shock(H, seeds, log=log)
+    X, lab = H.rows()
+    log(f"harvested {X.shape[0]} rows in {time.perf_counter() - t0:.1f} s")
+    err = lab[:, 1]
+    flag = lab[:, 0] > 0.5
+    q = torch.quantile(err[flag][: 1_000_000].double(), torch.tensor([0.1, 0.5, 0.9, 0.99], dtype=torch.float64,
+                                                                      device="cuda"))
+    log(f"WENO-flagged rows {int(flag.sum())}; err quantiles 10/50/90/99%: {q.tolist()}")
+    tau = 1e-6
+    y = labels(lab, tau)
+    w = class_weights(y)
+    log(f"tau {tau}: positives {int(y.sum())} of {y.numel()}")
+    # held-out 5 % for validation
+    n = X.shape[0]
+    perm = torch.randperm(n, device="cuda")
+    nv = n // 20
+    va, tr = perm[:nv], perm[nv:]
+    P, hist = train(X[tr], y[tr], w[tr], epochs=12 if not quick else 3, log=log)
+    z = logits(X[va].contiguous(), P)
+    yv = y[va]
+    for margin in (0.0, 0.5, 1.0, 2.0):
+        sure = z.abs() > margin
+        pred = z > 0
+        fn = int(((~pred) & sure & (yv > 0.5)).sum())
+        fp = int((pred & sure & (yv < 0.5)).sum())
+        log(f"margin {margin}: decided {float(sure.float().mean()):.3f}, false-DRP {fn}, false-WENO {fp}, "
+            f"positives {int(yv.sum())}")
+    margin = 1.0
+    np.savez(os.path.join(out_dir, "learned_sensor.npz"), params=P, margin=np.float32(margin), tau=np.float64(tau),
+             loss=np.array(hist))
+    rows = evaluate(P, margin, steps=40 if not quick else 10, log=log)
+    json.dump(dict(tau=tau, margin=margin, loss=hist, eval=rows, rows=int(n)),
+              open(os.path.join(out_dir, "sensor_report.json"), "w"), indent=1)
+    log("done")
+
+
+if __name__ == "__main__":
+    import sys
+    main(quick="--quick" in sys.argv)

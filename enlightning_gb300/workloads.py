@@ -84,3 +84,100 @@ def random_walk_channel(rng, nseg=200, start=(0.0, 0.0), heading_deg=-90.0, seg_
         segs[n] = (x, y, x1, y1)
         x, y = x1, y1
     return segs
+
+
+# ---------------------------------------------------------------------------
+# multi-level workloads
+# ---------------------------------------------------------------------------
+
+SRC_POINT, SRC_SINE, SRC_LIGHTNING = 10, 20, 30
+
+
+def gaussian_spread(sigma):
+    """Reference spread for exp(-ln2 r^2/spread^2) equal to exp(-r^2/(2 sigma^2))."""
+    return sigma * math.sqrt(2.0 * math.log(2.0))
+
+
+def line_source(prm, nx0=4096, ny0=2048, dx0=0.5, nlevels=3, seed=100, nseg=200, precision=1,
+                variant="hybrid_high_llf", learned=False, base_patch=256, cfl=0.5, amp_frac=10.0,
+                sigma_cells=2.0, min_size=16, max_size=256):
+    """Thunder-like line source on a multi-level hierarchy (synthetic).
+
+    A seeded random-walk channel of `nseg` segments (lengths U(1, 3) m, turns
+    U(-16, 16) deg) starting high in the domain and heading down deposits a
+    Gaussian overpressure amp_frac*p0 of sigma = sigma_cells base cells per
+    segment with the reference's capsule-union painting (enlightning.C:
+    2214-2281), evaluated on the device at every level's own resolution and
+    converted to the state.  Boundaries as the reference's input.txt:14-18
+    (ABSORB left/right/top, REFLECT ground).  The time step is the device CFL
+    reduction (cfl * dx_min / max(|u|+c)): the reference's c-only dt
+    (enlightning.C:433-456) is unstable for a 10 p0 source.
+    """
+    from .constants import ABSORB, REFLECT
+    from .engine import Engine, Hierarchy
+
+    rng = np.random.default_rng(seed)
+    L = nx0 * dx0
+    Hh = ny0 * dx0
+    segs = random_walk_channel(rng, nseg=nseg, start=(0.5 * L, 0.85 * Hh), heading_deg=-90.0)
+    E = Engine(prm, nx0, ny0, (dx0, dx0), nlevels=nlevels, ratio=2, bc=(ABSORB, ABSORB, REFLECT, ABSORB),
+               variant=variant, precision=precision, learned=learned)
+    E.set_adaptive_dt(True, cfl)
+    Hy = Hierarchy(E, min_size=min_size, max_size=max_size, tag_buffer=2)
+    Hy.base_patches(base_patch)
+    amp = amp_frac * prm["p0"]
+    spread = gaussian_spread(sigma_cells * dx0)
+
+    def paint(level):
+        E.paint_source(level, SRC_LIGHTNING, amp=amp, spread=spread, segs=segs)
+        E.state_from_overpressure(level)
+
+    paint(0)
+    for l in range(nlevels - 1):
+        Hy.regrid_level(l)
+        paint(l + 1)
+    return E, Hy, segs
+
+
+def eos_state(rho, u, v, p, prm):
+    """State (5, ...) and T for given rho, velocity and pressure at c_lr = 0,
+    inverting update_state.m4:90-94 for rho*s and using T_n = T."""
+    k = (prm["gamma1"] - 1.0) / (2.0 * prm["rho0"])
+    drho = rho - prm["rho0"]
+    rs = prm["c_p"] * ((p - prm["p0"]) / prm["c"] ** 2 - drho - k * drho ** 2)
+    T = prm["T0"] * np.exp((rs / rho - prm["R"] * np.log(prm["rho0"] / rho)) / prm["c_v"])
+    return np.stack([rho, rho * u, rho * v, rs, rho * T]), T
+
+
+def mach_shock(prm, seed=0, nx0=1024, ny0=512, dx0=0.1, nlevels=2, mach=1.5, precision=1, learned=False,
+               variant="hybrid_high_llf", base_patch=128, cfl=0.5, min_size=32, max_size=128):
+    """Planar shock moving +x into ambient air with 1 % i.i.d. density noise.
+
+    Post-shock state from the ideal-gas Rankine-Hugoniot relations at
+    gamma = 1.4, mapped onto the reference's state through its equation of
+    state (eos_state).  Shock at x = 0.1 L; ABSORB left/right (zero-width
+    envelope: zero-gradient ghosts), REFLECT top/bottom; device CFL time step.
+    """
+    from .constants import ABSORB, REFLECT
+    from .engine import Engine, Hierarchy
+
+    rng = np.random.default_rng(seed)
+    r, pr, u2f = rankine_hugoniot(mach, 1.4)
+    p = dict(prm)
+    p["bc_absorb_width"] = 1e-9
+    E = Engine(p, nx0, ny0, (dx0, dx0), nlevels=nlevels, ratio=2, bc=(ABSORB, ABSORB, REFLECT, REFLECT),
+               variant=variant, precision=precision, learned=learned)
+    E.set_adaptive_dt(True, cfl)
+    Hy = Hierarchy(E, min_size=min_size, max_size=max_size, tag_buffer=2)
+    Hy.base_patches(base_patch)
+    X = np.arange(nx0)[None, :].repeat(ny0, 0)
+    post = X < int(0.1 * nx0)
+    rho = np.where(post, prm["rho0"] * r, prm["rho0"] * (1.0 + rng.uniform(-0.01, 0.01, (ny0, nx0))))
+    pres = np.where(post, prm["p0"] * pr, prm["p0"] + prm["c"] ** 2 * (rho - prm["rho0"]) +
+                    prm["c"] ** 2 * (prm["gamma1"] - 1) / (2 * prm["rho0"]) * (rho - prm["rho0"]) ** 2)
+    u = np.where(post, u2f * prm["c"], 0.0)
+    w, T = eos_state(rho, u, np.zeros_like(u), pres, prm)
+    E.set_level_state(0, w, pres, T)
+    for l in range(nlevels - 1):
+        Hy.regrid_level(l)
+    return E, Hy

@@ -224,8 +224,9 @@ int enl_engine_graph_replay(void* engine, int nsteps);
  * device int array of nx*ny (level index space, row pitch nx); cells outside
  * the patches are 0.  Fills ghosts of the current buffer and H0 first. */
 int enl_engine_tag(void* engine, int level, int* tags);
-/* Counters of the last steps: per level, cells advanced with WENO and in
- * total (host array of 2*ENL_MAX_LEVELS long long), then reset. */
+/* Counters of the last steps: per level, cells advanced with WENO, cells in
+ * total, and cells the learned switch left to the plain switch (host array of
+ * 3*ENL_MAX_LEVELS long long), then reset. */
 int enl_engine_stats(void* engine, long long* counts);
 /* Health word: 0, or ENL_ERR_NONFINITE / ENL_ERR_TIMEOUT raised by a kernel
  * since the last call (rho <= 0 or non-finite; a bounded wait gave up). */
@@ -242,6 +243,53 @@ int enl_engine_launches_per_step(void* engine, int plain);
 int enl_engine_set_adaptive_dt(void* engine, int on, double cfl);
 /* Last device dt and accumulated simulated time (adaptive mode). */
 int enl_engine_time(void* engine, double* dt_last, double* sim_time);
+
+/* State exchange with host memory: the current buffer's patch interiors of
+ * every level, packed (7 fields, tile order: level by level, patch by patch,
+ * 32x8 tiles row-major).  Asynchronous on the stream; host memory should be
+ * pinned.  enl_engine_packed_size gives the number of doubles. */
+int enl_engine_packed_size(void* engine, long long* ndoubles);
+int enl_engine_download(void* engine, double* host);
+int enl_engine_upload(void* engine, const double* host);
+
+/* Stage-kernel timing: with on = 1 every direct (not graph) enl_engine_step
+ * brackets its three stage-kernel launches with CUDA events on the stream.
+ * Returns (and resets) the accumulated kernel milliseconds, launches and
+ * cells advanced by them since the previous call. */
+int enl_engine_profile(void* engine, int on, double* ms_total,
+                       long long* launches, long long* cells);
+
+/* ---------------------------------------------------------------------- */
+/* Learned hybrid sensor                                                   */
+/* ---------------------------------------------------------------------- */
+/* A 40 -> 64 -> 64 -> 1 MLP (GELU) replacing the hybrid switch of
+ * fortran/rhs_hybrid_high_llf.m4:239-256 on level 0 of the FP32 engine.
+ * Parameters are one FP32 vector of enl_mlp_nparams() floats: W1[40][64],
+ * b1[64], W2[64][64], b2[64], w3[64], b3.  Kernels compute with BF16 weights
+ * and activations on the tensor cores, FP32 accumulation.  Cells whose logit
+ * is within +-margin of 0 are decided by the plain switch. */
+int enl_mlp_nparams(void);
+/* Logits of n feature rows (device BF16 [n][40]) into device float[n]. */
+int enl_mlp_forward(const void* X, long n, const float* params, float* logits);
+/* Sums over the n rows of the weighted BCE-with-logits loss gradient
+ * (device arrays; grad is accumulated into, loss_sum too, may be NULL). */
+int enl_mlp_grad(const void* X, const float* y, const float* weight, long n,
+                 const float* params, float* grad, double* loss_sum);
+/* One Adam step on the device parameters (grad scaled by inv_n). */
+int enl_mlp_adam(float* params, const float* grad, float* m, float* v,
+                 float lr, float beta1, float beta2, float eps, float inv_n,
+                 int step);
+/* Install the network (host FP32 vector) in an engine created with
+ * precision ENL_PREC_FP32 and learned = 1. */
+int enl_engine_set_mlp(void* engine, const float* params_host, float margin);
+/* Harvest training rows from a level of the engine (plain FP64 arithmetic):
+ * features (device BF16 [capacity][40]), labels (device float [capacity][2]
+ * = plain switch, max_k dt|KK_drp - KK_weno|/scale_k), count_dev (device
+ * counter, incremented).  WENO-flagged cells are all kept, DRP cells with
+ * probability keep0. */
+int enl_engine_harvest(void* engine, int level, double dt, const double* scale,
+                       double keep0, unsigned seed, void* X, float* labels,
+                       long capacity, unsigned long long* count_dev);
 
 /* Source painting on the H0 canvas of one level over its patches, as
  * enlightning::addSource does (enlightning.C:2140-2307): type 10 = POINT,

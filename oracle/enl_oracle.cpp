@@ -692,3 +692,55 @@ int ora_get_threads() {
 #endif
 }
 }
+
+// Source painting, enlightning.C:2140-2307 (addSource) for one patch of nx*ny
+// cells with lower corner xlo and spacing dx; H is interior-only (nx*ny).
+// type 10 POINT, 20 SINE, 30 LIGHTNING; mode 10 PULSE, 20 DRIVEN (POINT, the
+// value times `drive`).  LIGHTNING accumulates onto H with the capsule-union
+// rule of enlightning.C:2214-2281.
+extern "C" void ora_paint_source(int nx, int ny, const double* xlo, const double* dx, double* H, int type,
+                                 int mode, double amp, double spread, const double* pos, double sine_amp,
+                                 double sine_freq, int nseg, const double* segs, double drive) {
+  const double PI = 3.14159265358979323846264338;
+  auto SQ = [](double x) { return x * x; };
+  for (int j = 0; j < ny; ++j) {
+    double xc1 = xlo[1] + dx[1] * ((double)j + 0.5);
+    for (int i = 0; i < nx; ++i) {
+      double xc0 = xlo[0] + dx[0] * ((double)i + 0.5);
+      double& out = H[(long)j * nx + i];
+      if (type == 10) {
+        double x0 = xc0 - pos[0], x1 = xc1 - pos[1];
+        double v = amp * std::exp(-std::log(2.0) / SQ(spread) * (x0 * x0 + x1 * x1));
+        out = mode == 20 ? v * drive : v;
+      } else if (type == 20) {
+        double x0 = xc0 - pos[0], x1 = xc1 - pos[1];
+        out = amp * std::exp(-std::log(2.0) / SQ(spread) * SQ((x0)-sine_amp * std::sin(sine_freq * (x1))));
+      } else {
+        for (int k = 0; k < nseg; ++k) {
+          const double* c = segs + 4 * k;
+          int orientation = 0;
+          double theta = -std::atan((c[3] - c[1]) / (c[2] - c[0]));
+          if (((c[0] > c[2]) && (c[1] > c[3])) || ((c[0] <= c[2]) && (c[1] >= c[3]))) orientation = 1;
+          else if (((c[0] >= c[2]) && (c[1] <= c[3])) || ((c[0] < c[2]) && (c[1] < c[3]))) orientation = 2;
+          double line0 = std::tan(PI / 2.0 - theta) * (xc0 - c[0]) + c[1];
+          double line1 = std::tan(PI / 2.0 - theta) * (xc0 - c[2]) + c[3];
+          if (((orientation == 1) && (xc1 >= line0)) || ((orientation == 2) && (xc1 <= line0))) {
+            double t = amp * std::exp(-std::log(2.0) / SQ(spread) * (SQ(xc0 - c[0]) + SQ(xc1 - c[1])));
+            out = out + t - (out / amp) * t;
+          }
+          if (((orientation == 1) && (xc1 <= line1)) || ((orientation == 2) && (xc1 >= line1))) {
+            double t = amp * std::exp(-std::log(2.0) / SQ(spread) * (SQ(xc0 - c[2]) + SQ(xc1 - c[3])));
+            out = out + t - (out / amp) * t;
+          }
+          if (((orientation == 1) && (xc1 < line0) && (xc1 > line1)) ||
+              ((orientation == 2) && (xc1 > line0) && (xc1 < line1))) {
+            double t = amp * std::exp(-std::log(2.0) / SQ(spread) *
+                                      (SQ(std::sin(theta) * (xc0 - c[0]) + std::cos(theta) * (xc1 - c[1]))));
+            out = out + t - (out / amp) * t;
+          }
+        }
+      }
+    }
+  }
+}
+

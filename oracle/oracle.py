@@ -66,6 +66,7 @@ def lib():
         L.ora_set_f32_literals.argtypes = [i]
         L.ora_set_threads.argtypes = [i]
         L.ora_get_threads.restype = i
+        L.ora_paint_source.argtypes = [i, i, dp, dp, dp, i, i, d, d, dp, d, d, i, dp, d]
         _lib = L
     return _lib
 
@@ -161,6 +162,16 @@ def phys_bc(box, g, touches, bc, w_n, pres, temp, source, fill=None):
     lib().ora_phys_bc(if0, il0, if1, il1, g[0], g[1], _ip(np.asarray(touches, np.int32)),
                       _ip(np.asarray(bc, np.int32)), fw[0], fw[1], _dp(w_n), _dp(pres), _dp(temp),
                       _dp(source))
+
+
+def paint_source(nx, ny, xlo, dx, H, src_type, mode=10, amp=1.0, spread=1.0, pos=(0.0, 0.0),
+                 sine_amp=0.0, sine_freq=0.0, segs=None, drive=1.0):
+    """enlightning.C:2140-2307 on one patch (H interior (ny, nx), modified in place)."""
+    sg = np.ascontiguousarray(np.asarray(segs if segs is not None else np.zeros((0, 4)), np.float64))
+    lib().ora_paint_source(nx, ny, _dp(np.asarray(xlo, np.float64)), _dp(np.asarray(dx, np.float64)), _dp(H),
+                           int(src_type), int(mode), float(amp), float(spread),
+                           _dp(np.asarray(pos, np.float64)), float(sine_amp), float(sine_freq), sg.shape[0],
+                           _dp(sg), float(drive))
 
 
 class Patch:

@@ -171,3 +171,87 @@ def test_engine_tag_bit_exact(ora):
     assert np.array_equal(tags, ref)
     assert tags.sum() > 0
     assert st.shape == (7, ny, nx)
+
+
+def test_paint_source_matches_oracle(ora):
+    """Device source painting (POINT, SINE, LIGHTNING, DRIVEN) vs the oracle
+    restatement of enlightning.C:2140-2307."""
+    prm = default_params()
+    nx, ny, dx = 96, 64, (0.25, 0.25)
+    E = Engine(prm, nx, ny, dx, nlevels=1)
+    E.set_patches(0, [(0, 47, 0, 63), (48, 95, 0, 63)])
+    rng = np.random.default_rng(3)
+    segs = workloads.random_walk_channel(rng, nseg=30, start=(12.0, 14.0), heading_deg=-90.0)
+    cases = [dict(src_type=10, amp=5e5, spread=0.6, pos=(7.0, 9.0)),
+             dict(src_type=10, mode=20, amp=5e5, spread=0.6, pos=(7.0, 9.0), drive=0.37),
+             dict(src_type=20, amp=2e5, spread=0.4, pos=(12.0, 8.0), sine_amp=1.5, sine_freq=0.8),
+             dict(src_type=30, amp=10 * prm["p0"], spread=workloads.gaussian_spread(0.5), segs=segs)]
+    for kw in cases:
+        E.buffer(0, 3).zero_()
+        E.paint_source(0, **kw)
+        torch.cuda.synchronize()
+        got = E.buffer(0, 3).cpu().numpy()[0, 3:3 + ny, 3:3 + nx]
+        ref = np.zeros((ny, nx))
+        ora.paint_source(nx, ny, (0.0, 0.0), dx, ref, **kw)
+        assert relL2(got, ref) <= 1e-12, kw["src_type"]
+        assert np.abs(ref).max() > 0
+
+
+def test_pack_roundtrip_and_adaptive_dt(ora):
+    prm = default_params()
+    nx, ny = 64, 48
+    E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 63, 0, 47)], [(32, 95, 24, 71)]], (REFLECT,) * 4,
+                     "hybrid_high_llf")
+    n = E.packed_size()
+    host = torch.empty(n, dtype=torch.float64).pin_memory()
+    E.download(host)
+    torch.cuda.synchronize()
+    before = [E.level_state(l).cpu().numpy().copy() for l in range(2)]
+    E.buffer(0, 0).zero_()
+    E.buffer(1, 0).zero_()
+    E.upload(host)
+    torch.cuda.synchronize()
+    for l in range(2):
+        after = E.level_state(l).cpu().numpy()
+        for b in E.patches[l]:
+            sl = (slice(None), slice(b[2], b[3] + 1), slice(b[0], b[1] + 1))
+            assert np.array_equal(after[sl], before[l][sl])
+    # device CFL reduction: dt = cfl * finest dx / max(|u|,|v|) + c
+    E.buffer(0, 0)[1, 3:3 + ny, 3:3 + nx] += 3.0  # give the flow a speed
+    torch.cuda.synchronize()
+    st = [E.level_state(l).cpu().numpy() for l in range(2)]
+    smax = 0.0
+    for l in range(2):
+        for b in E.patches[l]:
+            r = st[l][0, b[2]:b[3] + 1, b[0]:b[1] + 1]
+            u = np.abs(st[l][1, b[2]:b[3] + 1, b[0]:b[1] + 1] / r)
+            v = np.abs(st[l][2, b[2]:b[3] + 1, b[0]:b[1] + 1] / r)
+            smax = max(smax, max(u.max(), v.max()) + prm["c"])
+    E.set_adaptive_dt(True, 0.5)
+    E.step(1.0)
+    dt, t = E.time()
+    assert dt == pytest.approx(0.5 * 0.05 / smax, rel=1e-14)
+    assert t == pytest.approx(dt, rel=1e-14)
+    assert E.health() == 0
+
+
+def test_line_source_hierarchy_small():
+    """A reduced line-source run: painting, tagging, clustering into three
+    levels, regrids, FP32 batched vs FP64 plain within 1e-3."""
+    prm = default_params()
+    out = {}
+    for prec, plain in ((PREC_FP32, False), (PREC_FP64, True)):
+        E, H, segs = workloads.line_source(prm, nx0=256, ny0=128, dx0=0.5, nlevels=3, nseg=20, precision=prec,
+                                           base_patch=64)
+        assert len(E.patches[1]) > 0 and len(E.patches[2]) > 0
+        for s in range(12):
+            if s and s % 5 == 0:
+                H.regrid()
+            E.step(1.0, plain=plain)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        out[prec] = E.level_state(0).cpu().numpy().copy()
+    a, b = out[PREC_FP32], out[PREC_FP64]
+    for k in (0, 1, 2, 4, 5):
+        assert relL2(a[k], b[k]) <= 1e-3
+    assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) <= 1e-3

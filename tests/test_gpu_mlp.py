@@ -1,0 +1,122 @@
+"""Learned sensor kernels (GPU) against the CPU oracle of the network.
+
+* forward logits and the loss gradient of the BF16 tensor-core kernels match
+  oracle/mlp.py (same BF16 rounding points, FP32 vs FP64 accumulation);
+* a few Adam steps on the device lower the loss;
+* inside the fused stage kernel, a learned engine whose margin covers every
+  logit defers every level-0 cell to the plain switch and reproduces the
+  plain-switch run bit for bit;
+* with the trained network committed in enlightning_gb300/learned_sensor.npz,
+  the learned run sends fewer level-0 cells to WENO and stays within 1e-3
+  relative L2 of the plain-switch run.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from enlightning_gb300 import _lib, sensor, workloads  # noqa: E402
+from enlightning_gb300.constants import default_params  # noqa: E402
+from enlightning_gb300.engine import PREC_FP32  # noqa: E402
+
+
+def relL2(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(1e-300, np.linalg.norm(b)))
+
+
+def synthetic_rows(n, seed=0):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(0.5, 0.4, (n, 40)).astype(np.float32)
+    y = (rng.uniform(size=n) < 0.3).astype(np.float32)
+    w = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    return X, y, w
+
+
+def to_dev_bf16(X):
+    return torch.from_numpy(X).to(torch.bfloat16).cuda().contiguous()
+
+
+def test_forward_matches_oracle():
+    import mlp as omlp
+    X, _, _ = synthetic_rows(1000)
+    P = omlp.init_params(1)
+    P[omlp.OFF_B1:omlp.OFF_W2] = 0.1
+    z = sensor.logits(to_dev_bf16(X), P).cpu().numpy()
+    ref, _ = omlp.forward(P, X)
+    assert relL2(z, ref) < 1e-2
+    assert np.corrcoef(z, ref)[0, 1] > 0.9999
+
+
+def test_gradient_matches_oracle():
+    import mlp as omlp
+    n = 4096
+    X, y, w = synthetic_rows(n, 2)
+    P = omlp.init_params(3)
+    L = _lib.lib()
+    Xd, yd, wd = to_dev_bf16(X), torch.from_numpy(y).cuda(), torch.from_numpy(w).cuda()
+    Pd = torch.from_numpy(P).cuda()
+    g = torch.zeros_like(Pd)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    _lib.check(L.enl_mlp_grad(C.c_void_p(Xd.data_ptr()), C.c_void_p(yd.data_ptr()), C.c_void_p(wd.data_ptr()), n,
+                              C.c_void_p(Pd.data_ptr()), C.c_void_p(g.data_ptr()), C.c_void_p(loss.data_ptr())))
+    torch.cuda.synchronize()
+    gg = g.cpu().numpy().astype(np.float64)
+    lref, gref = omlp.loss_and_grad(P, X, y, w)
+    assert abs(loss.item() - lref) / lref < 1e-4
+    blocks = {"W1": (omlp.OFF_W1, omlp.OFF_B1), "b1": (omlp.OFF_B1, omlp.OFF_W2), "W2": (omlp.OFF_W2, omlp.OFF_B2),
+              "b2": (omlp.OFF_B2, omlp.OFF_W3), "w3": (omlp.OFF_W3, omlp.OFF_B3), "b3": (omlp.OFF_B3, omlp.NPARAMS)}
+    for name, (a, b) in blocks.items():
+        assert relL2(gg[a:b], gref[a:b]) < 2e-2, name
+
+
+def test_adam_lowers_loss():
+    X, y, w = synthetic_rows(20000, 4)
+    y = (X[:, 0] + X[:, 5] > 1.0).astype(np.float32)  # learnable rule
+    Xd = to_dev_bf16(X)
+    P, hist = sensor.train(Xd, torch.from_numpy(y).cuda(), torch.from_numpy(w).cuda(), epochs=6, batch=4096)
+    assert hist[-1] < 0.7 * hist[0]
+
+
+def _run(prm, learned, params=None, margin=0.0, steps=8, seed=5):
+    E, H, _ = workloads.line_source(prm, nx0=256, ny0=128, dx0=0.5, nlevels=2, nseg=20, seed=seed,
+                                    precision=PREC_FP32, learned=learned, base_patch=64)
+    if learned:
+        E.set_mlp(params, margin)
+    E.stats()
+    for s in range(steps):
+        if s and s % 5 == 0:
+            H.regrid()
+        E.step(1.0)
+    torch.cuda.synchronize()
+    st = E.stats()
+    assert E.health() == 0
+    return [E.level_state(l).cpu().numpy().copy() for l in range(2)], st
+
+
+def test_learned_with_full_margin_equals_plain():
+    prm = default_params()
+    P = sensor.init_params(0)
+    a, sa = _run(prm, False)
+    b, sb = _run(prm, True, P, margin=1e30)
+    for l in range(2):
+        assert np.array_equal(a[l], b[l])
+    assert sb[0, 2] == sb[0, 1]  # every level-0 cell deferred to the plain switch
+    assert np.array_equal(sa[:, :2], sb[:, :2])
+
+
+@pytest.mark.skipif(not os.path.exists(sensor.WEIGHTS), reason="no trained network committed")
+def test_trained_network_gains_over_plain_switch():
+    prm = default_params()
+    P, margin = sensor.load_weights()
+    a, sa = _run(prm, False, steps=20, seed=101)
+    b, sb = _run(prm, True, P, margin=margin, steps=20, seed=101)
+    weno_plain = sa[0, 0] / max(1, sa[0, 1])
+    weno_learned = sb[0, 0] / max(1, sb[0, 1])
+    assert weno_learned < weno_plain
+    for k in (0, 1, 2, 4, 5):
+        assert relL2(b[0][k], a[0][k]) <= 1e-3
+    assert relL2(b[0][0] - prm["rho0"], a[0][0] - prm["rho0"]) <= 1e-3

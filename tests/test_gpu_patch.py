@@ -262,4 +262,6 @@ def test_pulse_multistep_parity(L, ora, variant):
     assert relL2(wg[0] - prm["rho0"], op.w_cur[0] - prm["rho0"]) <= tol
     assert relL2(wg[4] - prm["rho0"] * prm["T0"], op.w_cur[4] - prm["rho0"] * prm["T0"]) <= tol
     if variant in ("hybrid_high_llf", "drp"):
-        assert tol == TOL  # well-conditioned schemes: the plain 1e-12 bar
+        # well-conditioned schemes: the plain 1e-12 bar, whatever the sensitivity
+        for k in range(5):
+            assert relL2(wg[k], op.w_cur[k]) <= TOL, (k, relL2(wg[k], op.w_cur[k]))
