@@ -261,7 +261,7 @@ class LineSource:
             "sigma 2 cells, hybrid_high_llf, regrid every 10 steps")
     REGRID = 10
 
-    def __init__(self, seed=100, learned=False):
+    def __init__(self, seed=100, learned=False, scale=1):
         import torch
 
         from enlightning_gb300 import workloads
@@ -271,9 +271,17 @@ class LineSource:
         self.torch = torch
         self.prm = default_params()
         self.learned = learned
+        # scale > 1 shrinks the base grid (same dx, smaller domain) for profiling captures
+        kw = dict(nx0=4096 // scale, ny0=2048 // scale, nseg=max(20, 200 // scale)) if scale > 1 else {}
+        if scale > 1:
+            self.name = self.name.replace("4096x2048", f"{4096 // scale}x{2048 // scale}")
         self.fast, self.fast_h, self.segs = workloads.line_source(self.prm, seed=seed, precision=PREC_FP32,
-                                                                  learned=learned)
-        self.plain, self.plain_h, _ = workloads.line_source(self.prm, seed=seed, precision=PREC_FP64)
+                                                                  learned=learned, **kw)
+        if learned:
+            from enlightning_gb300 import sensor
+            P, margin = sensor.load_weights()
+            self.fast.set_mlp(P, margin)
+        self.plain, self.plain_h, _ = workloads.line_source(self.prm, seed=seed, precision=PREC_FP64, **kw)
         self.steps_done = {"fast": 0, "plain": 0}
         self.graph_ok = False
         self.dt_cap = 1.0
@@ -573,7 +581,7 @@ def run_linesource(args):
     torch.cuda.set_stream(torch.cuda.Stream())
     hbm_peak, peak_kind = peaks()
     t_build = time.perf_counter()
-    wl = LineSource(learned=args.learned)
+    wl = LineSource(learned=args.learned, scale=args.scale)
     t_build = time.perf_counter() - t_build
 
     def barrier():
@@ -688,6 +696,7 @@ def main():
     ap.add_argument("--learned", type=int, default=0)
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--compare-steps", type=int, default=20)
+    ap.add_argument("--scale", type=int, default=1, help="shrink the line-source base grid (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

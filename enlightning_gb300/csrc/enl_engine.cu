@@ -37,6 +37,13 @@ constexpr int kBW = kTW + 6, kBH = kTH + 6;      // halo box
 constexpr int kNF = 7;                           // stored fields
 constexpr int kTileElems = kNF * kBH * kBW;      // 3724
 constexpr int kTileBytes64 = kTileElems * 8;     // 29792
+// Shared-memory layout of the stage kernel.  A TMA destination must start on
+// a 128-byte boundary, so every region is padded to a multiple of 128 bytes.
+constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+constexpr int kStageBufBytes = align128(kTileBytes64);            // 29824
+constexpr int kTile32Bytes = align128(kTileElems * 4);            // 14976
+constexpr int kOffTile32 = 2 * kStageBufBytes;
+constexpr int kOffMlp = kOffTile32 + kTile32Bytes;
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
 
 struct StageArgs {
@@ -104,12 +111,11 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
   // next tile's copy overlaps the current tile's compute) + one FP32 tile
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* stage_buf[2] = {reinterpret_cast<double*>(smem_raw),
-                          reinterpret_cast<double*>(smem_raw + kTileBytes64)};
-  float* tile32 = reinterpret_cast<float*>(smem_raw + 2 * kTileBytes64);
+                          reinterpret_cast<double*>(smem_raw + kStageBufBytes)};
+  float* tile32 = reinterpret_cast<float*>(smem_raw + kOffTile32);
   // learned sensor (FAST + hybrid only): network image and feature tile
-  MlpSmem* mlp_s = reinterpret_cast<MlpSmem*>(smem_raw + 2 * kTileBytes64 + kTileElems * 4);
-  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + 2 * kTileBytes64 + kTileElems * 4 +
-                                                          ((sizeof(MlpSmem) + 127) / 128) * 128);
+  MlpSmem* mlp_s = reinterpret_cast<MlpSmem*>(smem_raw + kOffMlp);
+  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + kOffMlp + align128((int)sizeof(MlpSmem)));
   __shared__ unsigned char s_flag[256];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
@@ -119,11 +125,23 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
   const int ntiles = *A.ntiles;
   auto issue = [&](int t, int b) {
     const int4 td = A.tiles[t];
+    // a tiled TMA copy needs x * 8 bytes to be a multiple of 16 (x even);
+    // set_patches only accepts even patch origins and tiles are 32 wide
+    if (td.x & 1) {
+      raise_health(A.health, ENL_ERR_STATE);
+      return false;
+    }
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(&mbar[b], kTileBytes64);
     // canvas column of cell i0-3 is i0 (ghost offset 3); i0 is even
     tma_load_3d(stage_buf[b], &A.tmap[td.z & 0xff], td.x, td.y, 0, &mbar[b]);
+    return true;
   };
+  // TMA destinations must start on 128-byte boundaries; refuse to run otherwise
+  if ((smem_u32(smem_raw) & 127u) != 0u) {
+    if (tid == 0) raise_health(A.health, ENL_ERR_STATE);
+    return;
+  }
   const bool learned = FAST && SCHEME == kHybrid && A.mlp != nullptr;
   if (learned) mlp_stage_params(*mlp_s, A.mlp, tid, 256);
   if (tid == 0) {
@@ -131,8 +149,8 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
     mbar_init(&mbar[1], 1);
     fence_mbar_init();
     int t = atomicAdd(A.counter, 1);
+    if (t < ntiles && !issue(t, 0)) t = ntiles;
     s_t[0] = t;
-    if (t < ntiles) issue(t, 0);
   }
   __syncthreads();
   uint32_t phase[2] = {0u, 0u};
@@ -141,8 +159,8 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
   while (t < ntiles) {
     if (tid == 0) {
       int nt = atomicAdd(A.counter, 1);
+      if (nt < ntiles && !issue(nt, b ^ 1)) nt = ntiles;
       s_t[b ^ 1] = nt;
-      if (nt < ntiles) issue(nt, b ^ 1);
     }
     double* tile = stage_buf[b];
     const int4 td = A.tiles[t];
@@ -1389,9 +1407,9 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMemset(E->d_dt, 0, 2 * sizeof(double));
   cudaMalloc(&E->d_smax, sizeof(unsigned long long));
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
-  E->smem_bytes = 2 * kTileBytes64 + (cfg->precision == ENL_PREC_FP32 ? kTileElems * 4 : 0);
+  E->smem_bytes = 2 * kStageBufBytes + (cfg->precision == ENL_PREC_FP32 ? kTile32Bytes : 0);
   if (cfg->precision == ENL_PREC_FP32 && cfg->learned)
-    E->smem_bytes += ((sizeof(MlpSmem) + 127) / 128) * 128 + 256 * kFeat * sizeof(__nv_bfloat16);
+    E->smem_bytes += align128((int)sizeof(MlpSmem)) + 256 * kFeat * sizeof(__nv_bfloat16);
   StageFn fn = cfg->precision == ENL_PREC_FP32 ? pick_stage<true>(cfg->variant) : pick_stage<false>(cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
   int per_sm = 0;

@@ -228,8 +228,10 @@ int enl_engine_tag(void* engine, int level, int* tags);
  * total, and cells the learned switch left to the plain switch (host array of
  * 3*ENL_MAX_LEVELS long long), then reset. */
 int enl_engine_stats(void* engine, long long* counts);
-/* Health word: 0, or ENL_ERR_NONFINITE / ENL_ERR_TIMEOUT raised by a kernel
- * since the last call (rho <= 0 or non-finite; a bounded wait gave up). */
+/* Health word: 0, or the first code a kernel raised since the last call:
+ * ENL_ERR_NONFINITE (rho <= 0 or non-finite state), ENL_ERR_TIMEOUT (a
+ * bounded wait gave up), ENL_ERR_STATE (a TMA precondition failed and the
+ * copy was not issued). */
 int enl_engine_health(void* engine);
 /* Number of kernel launches one enl_engine_step issues (for accounting). */
 int enl_engine_launches_per_step(void* engine, int plain);
