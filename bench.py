@@ -261,7 +261,7 @@ class LineSource:
             "sigma 2 cells, hybrid_high_llf, regrid every 10 steps")
     REGRID = 10
 
-    def __init__(self, seed=100, learned=False, scale=1):
+    def __init__(self, seed=100, learned=False, scale=1, with_plain=True):
         import torch
 
         from enlightning_gb300 import workloads
@@ -281,7 +281,9 @@ class LineSource:
             from enlightning_gb300 import sensor
             P, margin = sensor.load_weights()
             self.fast.set_mlp(P, margin)
-        self.plain, self.plain_h, _ = workloads.line_source(self.prm, seed=seed, precision=PREC_FP64, **kw)
+        self.plain, self.plain_h = None, None
+        if with_plain:
+            self.plain, self.plain_h, _ = workloads.line_source(self.prm, seed=seed, precision=PREC_FP64, **kw)
         self.steps_done = {"fast": 0, "plain": 0}
         self.graph_ok = False
         self.dt_cap = 1.0
@@ -295,7 +297,7 @@ class LineSource:
         H = self.fast_h if which == "fast" else self.plain_h
         done = 0
         for _ in range(nsteps):
-            if self.steps_done[which] > 0 and self.steps_done[which] % self.REGRID == 0:
+            if self.REGRID and self.steps_done[which] > 0 and self.steps_done[which] % self.REGRID == 0:
                 H.regrid()
                 self.graph_ok = False if which == "fast" else self.graph_ok
             done += E.cells()
@@ -364,7 +366,86 @@ class LineSource:
                           f"steps ({el:.1f} s)"}
 
 
-WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource}
+class PulseBatch(LineSource):
+    """Config 5: 64 independent Gaussian-pulse problems (square sides uniform
+    in 128..1024, multiples of 32; amplitude U(0.01, 0.5) p0; sigma U(4, 16)
+    cells; dx 0.1 m; reflective walls; dt = cfl dx / c) advanced together: one
+    persistent launch per RK stage covers every tile of every problem."""
+
+    name = ("pulses64: 64 independent pulse problems, sides U{128..1024}/32, amp U(0.01,0.5) p0, "
+            "sigma U(4,16) cells, dx 0.1 m, reflect, hybrid_high_llf")
+    REGRID = 0
+
+    def __init__(self, seed=7, learned=False, scale=1, with_plain=True):
+        import torch
+
+        from enlightning_gb300 import workloads
+        from enlightning_gb300.constants import default_params
+        from enlightning_gb300.engine import PREC_FP32, PREC_FP64
+
+        self.torch = torch
+        self.prm = default_params()
+        self.learned = learned
+        n = 64 // scale
+        self.fast, self.boxes, self.info = workloads.pulse_batch(self.prm, seed=seed, n=n, precision=PREC_FP32,
+                                                                 learned=learned)
+        if learned:
+            from enlightning_gb300 import sensor
+            P, margin = sensor.load_weights()
+            self.fast.set_mlp(P, margin)
+        self.plain = None
+        if with_plain:
+            self.plain, _, _ = workloads.pulse_batch(self.prm, seed=seed, n=n, precision=PREC_FP64)
+        self.fast_h = self.plain_h = None
+        self.steps_done = {"fast": 0, "plain": 0}
+        self.graph_ok = False
+        self.dt_cap = self.info["dt"]
+
+    def compare(self):
+        a = self.fast.level_state(0).cpu().numpy()
+        b = self.plain.level_state(0).cpu().numpy()
+        m = np.zeros(a.shape[1:], bool)
+        for bx in self.boxes:
+            m[bx[2]:bx[3] + 1, bx[0]:bx[1] + 1] = True
+        p = self.prm
+        out = {}
+        for k, nme in enumerate(["rho", "rho_u", "rho_v", "rho_s", "rho_Tn", "p", "T"]):
+            out[nme] = float(np.linalg.norm(a[k][m] - b[k][m]) / max(np.linalg.norm(b[k][m]), 1e-300))
+        out["rho-rho0"] = float(np.linalg.norm(a[0][m] - b[0][m]) / np.linalg.norm(b[0][m] - p["rho0"]))
+        out["p-p0"] = float(np.linalg.norm(a[5][m] - b[5][m]) / np.linalg.norm(b[5][m] - p["p0"]))
+        return out
+
+    def cpu_baseline(self, budget_s=12.0, threads=None):
+        """The oracle on four of the problems (one RK3 step each, all threads)."""
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as ora
+        threads = threads or os.cpu_count() or 1
+        ora.set_threads(threads)
+        buf = self.fast.buffer(0, 0).cpu().numpy()
+        sample = []
+        for bx in self.boxes[:4]:
+            s = bx[1] - bx[0] + 1
+            sample.append((s, np.ascontiguousarray(buf[:, bx[2]:bx[3] + 7, bx[0]:bx[1] + 7])))
+        ncell, steps, t0 = 0, 0, time.perf_counter()
+        while True:
+            for s, v in sample:
+                P = ora.Patch((0, s - 1, 0, s - 1), (0.0, 0.0), (0.1, 0.1))
+                P.w_scr[...] = v[0:5]
+                P.w_cur[...] = P.interior(v[0:5])
+                P.pres[...] = v[5]
+                P.temp[...] = v[6]
+                ora.advance(P, self.prm, "hybrid_high_llf", self.dt_cap, 1,
+                            domain=((0, 0), (s * 0.1, s * 0.1)))
+                ncell += s * s
+            steps += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s or steps >= 50:
+                break
+        return {"value": ncell / el, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"4 of the 64 problems ({ncell // steps} cells) x {steps} RK3 steps ({el:.1f} s)"}
+
+
+WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource, "pulses64": PulseBatch}
 
 
 # ---------------------------------------------------------------------------
@@ -581,7 +662,7 @@ def run_linesource(args):
     torch.cuda.set_stream(torch.cuda.Stream())
     hbm_peak, peak_kind = peaks()
     t_build = time.perf_counter()
-    wl = LineSource(learned=args.learned, scale=args.scale)
+    wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=not args.no_plain)
     t_build = time.perf_counter() - t_build
 
     def barrier():
@@ -591,10 +672,12 @@ def run_linesource(args):
 
     # accuracy: both arms from the same initial state, same regrid cadence
     ncmp = args.compare_steps
-    wl.advance("fast", ncmp, use_graph=True)
-    wl.advance("plain", ncmp)
-    barrier()
-    err = wl.compare()
+    err = None
+    if wl.plain is not None:
+        wl.advance("fast", ncmp, use_graph=True)
+        wl.advance("plain", ncmp)
+        barrier()
+        err = wl.compare()
     weno = wl.fast.stats()
     # warm-up, then the timed region (graph replay, regrids included)
     wl.advance("fast", max(3, args.warmup), use_graph=True)
@@ -618,13 +701,15 @@ def run_linesource(args):
     launches = wl.fast.launches_per_step() * args.steps
     # plain arm (per-patch FP64 launches, same hierarchy logic)
     kp = max(1, min(args.steps, args.plain_steps))
-    barrier()
-    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    p0.record()
-    cup = wl.advance("plain", kp)
-    p1.record()
-    barrier()
-    plain_value = cup / (p0.elapsed_time(p1) * 1e-3)
+    plain_value = None
+    if wl.plain is not None:
+        barrier()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record()
+        cup = wl.advance("plain", kp)
+        p1.record()
+        barrier()
+        plain_value = cup / (p0.elapsed_time(p1) * 1e-3)
     # dominant kernel: stage kernel timed with events around each launch
     wl.fast.profile(True)
     wl.advance("fast", 3, use_graph=False)
@@ -669,9 +754,11 @@ def run_linesource(args):
         "config": {"workload": wl.name, "path": "batched: persistent fused stage kernel over all levels, "
                    "FP32 perturbation RHS, CUDA graph" + (", learned sensor" if wl.learned else ", plain sensor"),
                    "cells_per_step": cu / args.steps, "patches": [len(p) for p in wl.fast.patches],
-                   "l2": "inputs larger than L2 (hierarchy state ~1.5 GB)", "regrid_every": wl.REGRID,
-                   "dt": "device CFL reduction, cfl 0.5 on max(|u|+c)", "dt_last": dt_last, "sim_time": sim_t,
-                   "plain_value": plain_value, "plain_steps": kp, "speedup_vs_plain": value / plain_value,
+                   "l2": "inputs larger than L2 (state of every level, > 1 GB)", "regrid_every": wl.REGRID,
+                   "dt": ("device CFL reduction, cfl 0.5 on max(|u|+c)" if wl.REGRID else "cfl*dx/c (reference)"),
+                   "dt_last": dt_last, "sim_time": sim_t,
+                   "plain_value": plain_value, "plain_steps": kp,
+                   "speedup_vs_plain": (value / plain_value) if plain_value else None,
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
                    "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -697,10 +784,11 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--compare-steps", type=int, default=20)
     ap.add_argument("--scale", type=int, default=1, help="shrink the line-source base grid (profiling)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "linesource":
+    elif args.workload in ("linesource", "pulses64"):
         run_linesource(args)
     else:
         run_ours(args)

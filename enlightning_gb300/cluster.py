@@ -48,8 +48,15 @@ def _cut(sig, min_size):
     return int(n // 2) if n // 2 >= lo and n // 2 <= hi else None
 
 
-def cluster_tags(tags: np.ndarray, efficiency=0.7, min_size=8, max_size=128):
+def cluster_tags(tags: np.ndarray, efficiency=0.7, min_size=8, max_size=128, allowed=None):
+    """Boxes covering every tag.  With ``allowed`` (same shape, bool) every
+    box is also kept inside the allowed cells (proper nesting): a box that
+    reaches outside is cut where its columns or rows start or stop leaving
+    the allowed region, down to single cells if need be."""
     tags = np.asarray(tags, dtype=bool)
+    if allowed is not None:
+        allowed = np.asarray(allowed, dtype=bool)
+        tags = tags & allowed
     out = []
     bb = _bbox(tags)
     if bb is None:
@@ -64,6 +71,20 @@ def cluster_tags(tags: np.ndarray, efficiency=0.7, min_size=8, max_size=128):
         ilo, ihi, jlo, jhi = ilo + b[0], ilo + b[1], jlo + b[2], jlo + b[3]
         sub = tags[jlo:jhi + 1, ilo:ihi + 1]
         nxb, nyb = ihi - ilo + 1, jhi - jlo + 1
+        if allowed is not None:
+            bad = ~allowed[jlo:jhi + 1, ilo:ihi + 1]
+            if bad.any():
+                cut = _nesting_cut(bad)
+                if cut is None:
+                    continue
+                ax, c = cut
+                if ax == "x":
+                    stack.append((ilo, ilo + c - 1, jlo, jhi))
+                    stack.append((ilo + c, ihi, jlo, jhi))
+                else:
+                    stack.append((ilo, ihi, jlo, jlo + c - 1))
+                    stack.append((ilo, ihi, jlo + c, jhi))
+                continue
         eff = sub.sum() / float(nxb * nyb)
         if eff >= efficiency:
             out.append((ilo, ihi, jlo, jhi))
@@ -89,6 +110,25 @@ def cluster_tags(tags: np.ndarray, efficiency=0.7, min_size=8, max_size=128):
         if not done:
             out.append((ilo, ihi, jlo, jhi))
     return chop(out, max_size)
+
+
+def _nesting_cut(bad):
+    """Cut separating columns (rows) that contain disallowed cells from those
+    that do not, on the longer side first; None for a 1x1 box."""
+    ny, nx = bad.shape
+    colbad = bad.any(axis=0)
+    rowbad = bad.any(axis=1)
+    for ax, sig, n in sorted((("x", colbad, nx), ("y", rowbad, ny)), key=lambda t: -t[2]):
+        if n < 2:
+            continue
+        ch = np.flatnonzero(sig[1:] != sig[:-1]) + 1
+        if ch.size:
+            return ax, int(ch[np.argmin(np.abs(ch - n / 2.0))])
+    if nx >= ny and nx >= 2:
+        return "x", nx // 2
+    if ny >= 2:
+        return "y", ny // 2
+    return None
 
 
 def chop(boxes, max_size):

@@ -388,6 +388,53 @@ __global__ void physbc_kernel(CanvasView V, int nfields, int bcL, int bcR, int b
   }
 }
 
+// Independent problems: every patch of the table is a domain of its own, and
+// its 3-cell band is filled by the single-patch rule of enlightning.C:830-1008
+// (edges from the first interior cell, corners from the interior corner, the
+// normal momenta negated on REFLECT sides).  One block per patch.
+__global__ void physbc_patches_kernel(CanvasView V, const int4* patches, int off, int cnt, int bcL, int bcR,
+                                      int bcB, int bcT) {
+  for (int p = blockIdx.x; p < cnt; p += gridDim.x) {
+    const int4 b = patches[off + p];
+    const int w = b.y - b.x + 1, h = b.w - b.z + 1;
+    const int nband = 6 * h + 6 * w + 36;
+    for (int t = threadIdx.x; t < nband * kNF; t += blockDim.x) {
+      int k = t % kNF, r = t / kNF;
+      int i, j, si, sj;
+      bool negu = false, negv = false;
+      if (r < 6 * h) {
+        int side = r / (3 * h), q = r % (3 * h);
+        j = b.z + q / 3;
+        int d = q % 3;
+        sj = j;
+        if (side == 0) { i = b.x - 1 - d; si = b.x; negu = bcL == kReflect; }
+        else { i = b.y + 1 + d; si = b.y; negu = bcR == kReflect; }
+      } else if (r < 6 * h + 6 * w) {
+        r -= 6 * h;
+        int side = r / (3 * w), q = r % (3 * w);
+        i = b.x + q / 3;
+        int d = q % 3;
+        si = i;
+        if (side == 0) { j = b.z - 1 - d; sj = b.z; negv = bcB == kReflect; }
+        else { j = b.w + 1 + d; sj = b.w; negv = bcT == kReflect; }
+      } else {
+        r -= 6 * h + 6 * w;
+        int corner = r / 9, q = r % 9;
+        int xs = corner & 1, ys = corner >> 1;
+        i = xs ? b.y + 1 + q % 3 : b.x - 1 - q % 3;
+        j = ys ? b.w + 1 + q / 3 : b.z - 1 - q / 3;
+        si = xs ? b.y : b.x;
+        sj = ys ? b.w : b.z;
+        negu = (xs ? bcR : bcL) == kReflect;
+        negv = (ys ? bcT : bcB) == kReflect;
+      }
+      double v = V.at(k, si, sj);
+      if ((k == 1 && negu) || (k == 2 && negv)) v = -v;
+      V.at(k, i, j) = v;
+    }
+  }
+}
+
 // Coarse-fine ghosts: bilinear interpolation in cell centres from the
 // coarser canvas.  One warp per halo row segment (j, i_begin, i_end).
 __device__ __forceinline__ void refine_weights(int I, int r, int& ic, double& f) {
@@ -1206,7 +1253,13 @@ static int fill_level(Engine* E, int l, int which) {
     interp_kernel<<<E->nsm * 4, 256, 0, s>>>(L.view(which), E->lev[l - 1].view(which), c.ratio, E->d_halo.p,
                                              E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l, kNF);
   }
-  physbc_kernel<<<E->nsm * 2, 256, 0, s>>>(L.view(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+  if (c.independent) {
+    if (E->patch_cnt[l])
+      physbc_patches_kernel<<<E->patch_cnt[l], 256, 0, s>>>(L.view(which), E->d_patchtab.p, E->patch_off[l],
+                                                            E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+  } else {
+    physbc_kernel<<<E->nsm * 2, 256, 0, s>>>(L.view(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+  }
   return ENL_OK;
 }
 
@@ -1361,7 +1414,9 @@ extern "C" {
 
 int enl_engine_create(const enl_engine_config* cfg, void** out) {
   if (!cfg || !out || cfg->nlevels < 1 || cfg->nlevels > kL || cfg->ratio < 2 || cfg->nx0 < 8 || cfg->ny0 < 8 ||
-      cfg->variant < 0 || cfg->variant > 8) {
+      cfg->variant < 0 || cfg->variant > 8 ||
+      (cfg->independent && (cfg->nlevels != 1 || cfg->bc[0] == kAbsorb || cfg->bc[1] == kAbsorb ||
+                            cfg->bc[2] == kAbsorb || cfg->bc[3] == kAbsorb))) {
     set_error(ENL_ERR_ARG);
     return ENL_ERR_ARG;
   }

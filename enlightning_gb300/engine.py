@@ -38,7 +38,8 @@ class Engine:
     """One multi-level canvas engine on the current CUDA device."""
 
     def __init__(self, params: dict, nx0: int, ny0: int, dx0, nlevels=1, ratio=2, xlo=(0.0, 0.0),
-                 bc=(REFLECT,) * 4, variant="hybrid_high_llf", precision=PREC_FP64, learned=False):
+                 bc=(REFLECT,) * 4, variant="hybrid_high_llf", precision=PREC_FP64, learned=False,
+                 independent=False):
         self.L = _lib.lib()
         p = params
         cfg = EngineConfig()
@@ -56,6 +57,7 @@ class Engine:
         cfg.rk_alpha1[:] = list(RK3_ALPHA1)
         cfg.rk_alpha2[:] = list(RK3_ALPHA2)
         cfg.rk_beta[:] = list(RK3_BETA)
+        cfg.independent = int(bool(independent))
         self.cfg = cfg
         self.params = dict(p)
         self.nlevels, self.ratio = nlevels, ratio
@@ -277,10 +279,10 @@ class Hierarchy:
         """Fine boxes (level+1 index space) from the current tags of `level`."""
         E, B, r = self.E, self.block, self.E.ratio
         bmap = E.tag_blocks(level, B, self.tag_buffer)
-        bmap &= self._nesting_blocks(level, bmap.shape[1], bmap.shape[0])
+        nest = self._nesting_blocks(level, bmap.shape[1], bmap.shape[0])
         cell = B * r  # level+1 cells per block side
         cboxes = cluster_tags(bmap, efficiency=self.efficiency, min_size=max(1, self.min_size // cell),
-                              max_size=max(1, self.max_size // cell))
+                              max_size=max(1, self.max_size // cell), allowed=nest)
         nxf, nyf = E.level_shape(level + 1)
         fine = []
         for b in cboxes:

@@ -181,3 +181,60 @@ def mach_shock(prm, seed=0, nx0=1024, ny0=512, dx0=0.1, nlevels=2, mach=1.5, pre
     for l in range(nlevels - 1):
         Hy.regrid_level(l)
     return E, Hy
+
+
+def shelf_pack(sides, width, gap=8):
+    """Origins (x, y) placing squares of the given sides on shelves of a
+    canvas `width` wide, `gap` cells apart (gap >= 6 keeps the 3-cell ghost
+    bands of neighbours disjoint; multiples of 8 keep TMA-friendly origins)."""
+    order = sorted(range(len(sides)), key=lambda k: -sides[k])
+    pos = [None] * len(sides)
+    x = y = gap
+    shelf_h = 0
+    for k in order:
+        s = sides[k]
+        if x + s + gap > width:
+            x = gap
+            y += shelf_h + gap
+            shelf_h = 0
+        pos[k] = (x, y)
+        x += s + gap
+        shelf_h = max(shelf_h, s)
+    height = y + shelf_h + gap
+    return pos, height
+
+
+def pulse_batch(prm, seed=7, n=64, side_range=(128, 1024), precision=1, learned=False, variant="hybrid_high_llf",
+                width=8192, dx=0.1):
+    """Batched independent pulse problems: n square patches with sides drawn
+    uniformly from multiples of 32 in side_range, Gaussian overpressure
+    U(0.01, 0.5) p0 with sigma U(4, 16) cells at each centre, reflective
+    walls, dx = 0.1 m and the reference's dt = cfl*dx/c; all advanced by one
+    engine (independent mode: every patch is its own domain)."""
+    from .constants import REFLECT
+    from .engine import Engine
+
+    rng = np.random.default_rng(seed)
+    sides = [int(32 * rng.integers(side_range[0] // 32, side_range[1] // 32 + 1)) for _ in range(n)]
+    amps = rng.uniform(0.01, 0.5, n)
+    sigmas = rng.uniform(4.0, 16.0, n)
+    pos, height = shelf_pack(sides, width)
+    height = int(-(-height // 8) * 8)
+    E = Engine(prm, width, height, (dx, dx), nlevels=1, bc=(REFLECT,) * 4, variant=variant, precision=precision,
+               learned=learned, independent=True)
+    boxes = [(x, x + s - 1, y, y + s - 1) for (x, y), s in zip(pos, sides)]
+    E.set_patches(0, boxes)
+    buf = E.buffer(0, 0)
+    k = (prm["gamma1"] - 1.0) / (2.0 * prm["rho0"])
+    import torch
+    for (x, y), s, a, sg in zip(pos, sides, amps, sigmas):
+        dp = gaussian_dp(s, s, a * prm["p0"], sg)
+        w = state_from_dp(dp, prm)
+        drho = w[0] - prm["rho0"]
+        p = prm["c"] ** 2 * (drho + k * drho ** 2) + prm["p0"]
+        T = w[4] / w[0]
+        buf[0:5, 3 + y:3 + y + s, 3 + x:3 + x + s].copy_(torch.from_numpy(w))
+        buf[5, 3 + y:3 + y + s, 3 + x:3 + x + s].copy_(torch.from_numpy(p))
+        buf[6, 3 + y:3 + y + s, 3 + x:3 + x + s].copy_(torch.from_numpy(T))
+    dt = pulse_dt(prm, (dx, dx))
+    return E, boxes, dict(sides=sides, amps=amps, sigmas=sigmas, dt=dt)

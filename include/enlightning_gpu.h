@@ -192,6 +192,10 @@ typedef struct {
   double rho0, gamma1, c_p, p0, T0, c_v;
   double absorb_width;
   double rk_alpha1[3], rk_alpha2[3], rk_beta[3];
+  int independent;        /* 1: every level-0 patch is its own domain whose
+                             sides are physical boundaries (batched independent
+                             problems; nlevels must be 1, patches >= 6 cells
+                             apart on the canvas)                         */
 } enl_engine_config;
 
 /* Create / destroy.  Allocates the canvases of every level (device memory). */

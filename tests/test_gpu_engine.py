@@ -255,3 +255,27 @@ def test_line_source_hierarchy_small():
     for k in (0, 1, 2, 4, 5):
         assert relL2(a[k], b[k]) <= 1e-3
     assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) <= 1e-3
+
+
+def test_independent_problems_match_single_patch_oracle(ora):
+    """Batched independent pulse problems (one engine, one persistent launch
+    per stage) equal separate single-patch oracle runs (FP64, 1e-12)."""
+    prm = default_params()
+    E, boxes, info = workloads.pulse_batch(prm, seed=3, n=3, side_range=(32, 96), precision=PREC_FP64, width=512)
+    st0 = E.level_state(0).cpu().numpy().copy()
+    for _ in range(6):
+        E.step(info["dt"])
+    torch.cuda.synchronize()
+    assert E.health() == 0
+    got = E.level_state(0).cpu().numpy()
+    for b in boxes:
+        s = b[1] - b[0] + 1
+        P = ora.Patch((0, s - 1, 0, s - 1), (0.0, 0.0), (0.1, 0.1))
+        v = st0[:, b[2]:b[3] + 1, b[0]:b[1] + 1]
+        P.w_scr[:, G:-G, G:-G] = v[0:5]
+        P.w_cur[...] = v[0:5]
+        P.pres[G:-G, G:-G] = v[5]
+        P.temp[G:-G, G:-G] = v[6]
+        ora.advance(P, prm, "hybrid_high_llf", info["dt"], 6, domain=((0, 0), (s * 0.1, s * 0.1)))
+        for k in range(5):
+            assert relL2(got[k, b[2]:b[3] + 1, b[0]:b[1] + 1], P.w_cur[k]) <= 1e-12
