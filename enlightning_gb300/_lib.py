@@ -74,6 +74,8 @@ ENGINE_SIGNATURES = {
     "enl_engine_state_from_overpressure": (C.c_int, [C.c_void_p, C.c_int]),
     "enl_engine_set_adaptive_dt": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "enl_engine_packed_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "enl_cfl_dt_static": (C.c_int, [C.c_int] * 6 + [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_double,
+                                                  C.c_double, C.c_void_p]),
     "enl_mlp_nparams": (C.c_int, []),
     "enl_mlp_forward": (C.c_int, [C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]),
     "enl_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -318,6 +318,23 @@ int enl_engine_state_from_overpressure(void* engine, int level);
 int enl_engine_tag_blocks(void* engine, int level, int block, int buffer,
                           unsigned char* map_host, int* nbx, int* nby);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free stable time step of one patch.  No counterpart in the
+ * reference (its dt, enlightning.C:433-456, needs no reduction); it is for
+ * callers that cannot allocate device memory when they need a time step.
+ * dt_out (device, 1 double) = min(dt_max, cfl * min(dx) / max over the patch
+ * interior of max(|u|,|v|) + c), the same value as the engine's device CFL
+ * reduction.  w_n as in rhs_ (SAMRAI layout, ghosts gcw0/gcw1).  Scratch is a
+ * static device array of 4096 partial maxima, one per 32x8 tile: patches of
+ * more than 4096 tiles (1,048,576 cells) are refused with ENL_ERR_ARG.  All
+ * calls share that array, so calls that overlap on the GPU race; the first
+ * call on a device looks up its address and belongs before any stream
+ * capture.  Runs on the stream set with enl_set_stream.
+ * ------------------------------------------------------------------------- */
+int enl_cfl_dt_static(int ifirst0, int ilast0, int ifirst1, int ilast1,
+                      int gcw0, int gcw1, const double* w_n, const double* dx,
+                      double c, double cfl, double dt_max, double* dt_out);
+
 #ifdef __cplusplus
 }
 #endif
