@@ -39,6 +39,11 @@ RHS_BYTES_PER_CELL = (5 + 3 + 5) * 8
 # stage 1 reads u^n and writes w1 (80 B), stages 2 and 3 read w, u^n and write
 # (120 B each).
 STEP_BYTES_PER_CELL = 320
+# engine storage/arithmetic modes (include/enlightning_gpu.h ENL_PREC_*)
+PREC_NAMES = {0: "fp64", 1: "fp32rhs_fp64state", 2: "fp32state"}
+PREC_DTYPE = {0: "f64", 1: "f32 rhs / f64 state", 2: "f32 (perturbation state and rhs)"}
+PREC_PATH = {0: "FP64 RHS", 1: "FP32 perturbation RHS on FP64 state",
+             2: "FP32 perturbation state and RHS"}
 
 
 def peaks():
@@ -261,21 +266,22 @@ class LineSource:
             "sigma 2 cells, hybrid_high_llf, regrid every 10 steps")
     REGRID = 10
 
-    def __init__(self, seed=100, learned=False, scale=1, with_plain=True):
+    def __init__(self, seed=100, learned=False, scale=1, with_plain=True, precision=2):
         import torch
 
         from enlightning_gb300 import workloads
         from enlightning_gb300.constants import default_params
-        from enlightning_gb300.engine import PREC_FP32, PREC_FP64
+        from enlightning_gb300.engine import PREC_FP64
 
         self.torch = torch
         self.prm = default_params()
         self.learned = learned
+        self.precision = precision
         # scale > 1 shrinks the base grid (same dx, smaller domain) for profiling captures
         kw = dict(nx0=4096 // scale, ny0=2048 // scale, nseg=max(20, 200 // scale)) if scale > 1 else {}
         if scale > 1:
             self.name = self.name.replace("4096x2048", f"{4096 // scale}x{2048 // scale}")
-        self.fast, self.fast_h, self.segs = workloads.line_source(self.prm, seed=seed, precision=PREC_FP32,
+        self.fast, self.fast_h, self.segs = workloads.line_source(self.prm, seed=seed, precision=precision,
                                                                   learned=learned, **kw)
         if learned:
             from enlightning_gb300 import sensor
@@ -285,6 +291,9 @@ class LineSource:
         if with_plain:
             self.plain, self.plain_h, _ = workloads.line_source(self.prm, seed=seed, precision=PREC_FP64, **kw)
         self.steps_done = {"fast": 0, "plain": 0}
+        self.regrid_s = {"fast": 0.0, "plain": 0.0}
+        self.regrids = {"fast": 0, "plain": 0}
+        self.captures = 0
         self.graph_ok = False
         self.dt_cap = 1.0
 
@@ -298,12 +307,17 @@ class LineSource:
         done = 0
         for _ in range(nsteps):
             if self.REGRID and self.steps_done[which] > 0 and self.steps_done[which] % self.REGRID == 0:
+                t0 = time.perf_counter()
                 H.regrid()
-                self.graph_ok = False if which == "fast" else self.graph_ok
+                self.regrid_s[which] += time.perf_counter() - t0
+                self.regrids[which] += 1
+                if which == "fast" and not E.graph_valid():
+                    self.graph_ok = False
             done += E.cells()
             if which == "fast" and use_graph:
                 if not self.graph_ok:
                     E.capture(self.dt_cap)
+                    self.captures += 1
                     self.graph_ok = True
                 E.replay(1)
             else:
@@ -340,7 +354,7 @@ class LineSource:
         for l in range(E.nlevels):
             k = max(1, int(round(12 * cells_l[l] / tot))) if E.patches[l] else 0
             idx = rng.choice(len(E.patches[l]), size=min(k, len(E.patches[l])), replace=False) if k else []
-            buf = E.buffer(l, 0).cpu().numpy()
+            buf = E.canvas_state(l)
             for q in idx:
                 b = E.patches[l][q]
                 v = np.ascontiguousarray(buf[:, b[2]:b[3] + 7, b[0]:b[1] + 7])
@@ -376,18 +390,19 @@ class PulseBatch(LineSource):
             "sigma U(4,16) cells, dx 0.1 m, reflect, hybrid_high_llf")
     REGRID = 0
 
-    def __init__(self, seed=7, learned=False, scale=1, with_plain=True):
+    def __init__(self, seed=7, learned=False, scale=1, with_plain=True, precision=2):
         import torch
 
         from enlightning_gb300 import workloads
         from enlightning_gb300.constants import default_params
-        from enlightning_gb300.engine import PREC_FP32, PREC_FP64
+        from enlightning_gb300.engine import PREC_FP64
 
         self.torch = torch
         self.prm = default_params()
         self.learned = learned
+        self.precision = precision
         n = 64 // scale
-        self.fast, self.boxes, self.info = workloads.pulse_batch(self.prm, seed=seed, n=n, precision=PREC_FP32,
+        self.fast, self.boxes, self.info = workloads.pulse_batch(self.prm, seed=seed, n=n, precision=precision,
                                                                  learned=learned)
         if learned:
             from enlightning_gb300 import sensor
@@ -398,6 +413,9 @@ class PulseBatch(LineSource):
             self.plain, _, _ = workloads.pulse_batch(self.prm, seed=seed, n=n, precision=PREC_FP64)
         self.fast_h = self.plain_h = None
         self.steps_done = {"fast": 0, "plain": 0}
+        self.regrid_s = {"fast": 0.0, "plain": 0.0}
+        self.regrids = {"fast": 0, "plain": 0}
+        self.captures = 0
         self.graph_ok = False
         self.dt_cap = self.info["dt"]
 
@@ -421,7 +439,7 @@ class PulseBatch(LineSource):
         import oracle as ora
         threads = threads or os.cpu_count() or 1
         ora.set_threads(threads)
-        buf = self.fast.buffer(0, 0).cpu().numpy()
+        buf = self.fast.canvas_state(0)
         sample = []
         for bx in self.boxes[:4]:
             s = bx[1] - bx[0] + 1
@@ -662,7 +680,9 @@ def run_linesource(args):
     torch.cuda.set_stream(torch.cuda.Stream())
     hbm_peak, peak_kind = peaks()
     t_build = time.perf_counter()
-    wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=not args.no_plain)
+    wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=not args.no_plain,
+                                  precision=args.precision)
+    esize = 4 if args.precision == 2 else 8
     t_build = time.perf_counter() - t_build
 
     def barrier():
@@ -684,6 +704,8 @@ def run_linesource(args):
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     wl.fast.stats()
+    rg0, rn0, cap0 = wl.regrid_s["fast"], wl.regrids["fast"], wl.captures
+    ph0 = dict(wl.fast_h.timing) if wl.fast_h is not None else {}
     with ClockSampler(local) as clk:
         e0.record()
         cu = wl.advance("fast", args.steps, use_graph=True)
@@ -695,6 +717,10 @@ def run_linesource(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = cu * ws / (ms * 1e-3)
+    regrid_info = {"regrids": wl.regrids["fast"] - rn0, "host_ms": 1e3 * (wl.regrid_s["fast"] - rg0),
+                   "graph_captures": wl.captures - cap0}
+    if wl.fast_h is not None:
+        regrid_info["phases_ms"] = {k: 1e3 * (v - ph0.get(k, 0.0)) for k, v in wl.fast_h.timing.items()}
     st = wl.fast.stats()
     weno_frac = {f"L{l}": float(st[l, 0] / max(1, st[l, 1])) for l in range(st.shape[0])}
     weno_frac["all"] = float(st[:, 0].sum() / max(1, st[:, 1].sum()))
@@ -717,10 +743,12 @@ def run_linesource(args):
     kms, kl, kcells = wl.fast.profile(False)
     per_launch_ms = kms / max(1, kl)
     cells_per_launch = kcells / max(1, kl)
-    achieved = cells_per_launch * (STEP_BYTES_PER_CELL / 3.0) / (per_launch_ms * 1e-3) / 1e9
+    # 320 B per RK3 cell-update with FP64 fields; FP32 storage moves half of it
+    bytes_per_cell_launch = STEP_BYTES_PER_CELL / 3.0 * esize / 8.0
+    achieved = cells_per_launch * bytes_per_cell_launch / (per_launch_ms * 1e-3) / 1e9
     # e2e: hierarchy state through the public API from pinned host memory
     n = wl.fast.packed_size()
-    host = torch.empty(n, dtype=torch.float64).pin_memory()
+    host = wl.fast.packed_host(pin=True)
     wl.fast.download(host)
     barrier()
     ke = max(1, min(args.steps, 10))
@@ -734,27 +762,33 @@ def run_linesource(args):
     q1.record()
     barrier()
     e2e_value = cue * ws / (q0.elapsed_time(q1) * 1e-3)
-    nbytes = int(n * 8)
+    nbytes = int(n * esize)
     if rank != 0:
         return
     health = wl.fast.health()
     cb = wl.cpu_baseline() if not args.no_cpu_baseline else None
+    # DRAM bytes of one stage launch from an ncu capture, per cell, scaled to
+    # this workload's launch (the capture ran a smaller case of the same kernel)
     traffic = None
     tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get("linesource")
+            rec = json.load(open(tf)).get(PREC_NAMES[args.precision])
+            if rec:
+                traffic = rec["dram_bytes_per_cell_launch"] * cells_per_launch
         except Exception:
             traffic = None
     dt_last, sim_t = wl.fast.time()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 rhs / f64 state", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": PREC_DTYPE[args.precision], "data": "synthetic",
         "config": {"workload": wl.name, "path": "batched: persistent fused stage kernel over all levels, "
-                   "FP32 perturbation RHS, CUDA graph" + (", learned sensor" if wl.learned else ", plain sensor"),
+                   + PREC_PATH[args.precision] + ", CUDA graph"
+                   + (", learned sensor" if wl.learned else ", plain sensor"),
                    "cells_per_step": cu / args.steps, "patches": [len(p) for p in wl.fast.patches],
                    "l2": "inputs larger than L2 (state of every level, > 1 GB)", "regrid_every": wl.REGRID,
+                   "timed_regrids": regrid_info,
                    "dt": ("device CFL reduction, cfl 0.5 on max(|u|+c)" if wl.REGRID else "cfl*dx/c (reference)"),
                    "dt_last": dt_last, "sim_time": sim_t,
                    "plain_value": plain_value, "plain_steps": kp,
@@ -762,8 +796,9 @@ def run_linesource(args):
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
                    "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "stage_kernel (FP32)",
-                     "peak_kind": peak_kind, "bytes_per_cell_launch": STEP_BYTES_PER_CELL / 3.0,
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "kernel": "stage_kernel (" + PREC_NAMES[args.precision] + ")",
+                     "peak_kind": peak_kind, "bytes_per_cell_launch": bytes_per_cell_launch,
                      "kernel_ms": per_launch_ms, "cells_per_launch": cells_per_launch},
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
@@ -785,6 +820,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=20)
     ap.add_argument("--scale", type=int, default=1, help="shrink the line-source base grid (profiling)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm (profiling)")
+    ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
+                    help="engine mode: 0 FP64, 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

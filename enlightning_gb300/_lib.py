@@ -74,6 +74,13 @@ ENGINE_SIGNATURES = {
     "enl_engine_state_from_overpressure": (C.c_int, [C.c_void_p, C.c_int]),
     "enl_engine_set_adaptive_dt": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "enl_engine_packed_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "enl_engine_storage": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "enl_engine_graph_valid": (C.c_int, [C.c_void_p]),
+    "enl_engine_set_mics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.c_int]),
+    "enl_engine_mic_records": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_longlong)]),
+    "enl_cluster_tags": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                   C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "enl_cfl_dt_static": (C.c_int, [C.c_int] * 6 + [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_double,
                                                   C.c_double, C.c_void_p]),
     "enl_mlp_nparams": (C.c_int, []),

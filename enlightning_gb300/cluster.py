@@ -131,6 +131,40 @@ def _nesting_cut(bad):
     return None
 
 
+def erode_allowed(allowed, passes):
+    """Proper-nesting mask: `passes` erosions by the 3x3 square, the outside
+    of the map counting as allowed."""
+    if passes <= 0:
+        return np.asarray(allowed, bool)
+    from scipy.ndimage import binary_erosion
+    return binary_erosion(allowed, structure=np.ones((3, 3), bool), iterations=passes, border_value=1)
+
+
+def cluster_tags_native(tags, efficiency=0.7, min_size=8, max_size=128, allowed=None, nest_erode=0):
+    """cluster_tags(tags, ..., allowed=erode_allowed(allowed, nest_erode)) in
+    the library's C++ (enl_cluster_tags): the same boxes in the same order,
+    with summed-area tables instead of array scans."""
+    import ctypes as C
+
+    from . import _lib
+    t = np.ascontiguousarray(np.asarray(tags, dtype=np.uint8))
+    ny, nx = t.shape
+    a = None if allowed is None else np.ascontiguousarray(np.asarray(allowed, dtype=np.uint8))
+    cap = 1024
+    while True:
+        out = np.zeros((cap, 4), np.int32)
+        n = C.c_int()
+        st = _lib.lib().enl_cluster_tags(t.ctypes.data_as(C.c_void_p),
+                                         None if a is None else a.ctypes.data_as(C.c_void_p), nx, ny,
+                                         int(nest_erode), float(efficiency), int(min_size), int(max_size),
+                                         out.ctypes.data_as(C.c_void_p), cap, C.byref(n))
+        if st == 0:
+            return [tuple(int(v) for v in b) for b in out[: n.value]]
+        if n.value <= cap:
+            _lib.check(st, "enl_cluster_tags")
+        cap = n.value
+
+
 def chop(boxes, max_size):
     out = []
     for ilo, ihi, jlo, jhi in boxes:

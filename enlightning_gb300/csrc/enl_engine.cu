@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <type_traits>
 #include <vector>
 
 #include "enl_fast.cuh"
@@ -37,25 +38,89 @@ constexpr int kBW = kTW + 6, kBH = kTH + 6;      // halo box
 constexpr int kNF = 7;                           // stored fields
 constexpr int kTileElems = kNF * kBH * kBW;      // 3724
 constexpr int kTileBytes64 = kTileElems * 8;     // 29792
+// The single-precision tile has rows of 40 (a TMA box row must span a
+// multiple of 16 bytes: 38 floats do not, 40 do); columns 38, 39 are unused.
+constexpr int kBW32 = 40;
+constexpr int kPlane32 = kBH * kBW32;            // 560
+constexpr int kTile32Elems = kNF * kPlane32;     // 3920
+constexpr int kTileBytes32 = kTile32Elems * 4;   // 15680
 // Shared-memory layout of the stage kernel.  A TMA destination must start on
 // a 128-byte boundary, so every region is padded to a multiple of 128 bytes.
+//   FP64 state:  [FP64 box A][FP64 box B][FP32 tile (FAST)][MLP]
+//   FP32 state:  [FP32 tile A][FP32 tile B][MLP]
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
 constexpr int kStageBufBytes = align128(kTileBytes64);            // 29824
-constexpr int kTile32Bytes = align128(kTileElems * 4);            // 14976
+constexpr int kTile32Bytes = align128(kTileBytes32);              // 15744
+// per-tile planes of the FP32 path: u and v over the whole halo box (rows of
+// kBW32), the x-fluxes F_0..4 on the 8 interior rows (rows of kBW32), the
+// y-fluxes G_0..4 on the 32 interior columns (rows of 32)
+constexpr int kPlaneF = kTH * kBW32;             // 320
+constexpr int kPlaneG = kBH * kTW;               // 448
+constexpr int kPlOffV = kPlane32, kPlOffF = 2 * kPlane32, kPlOffG = kPlOffF + 5 * kPlaneF;
+constexpr int kPlanesBytes = align128((kPlOffG + 5 * kPlaneG) * 4);   // 19840
+// FP32 storage prefetches u^n (5 fields) and H0 of the tile interior with the
+// halo box: boxes of 40 x 8 (x starts at the aligned column of cell i0 - 3)
+constexpr int kUnBytes = 5 * kTH * kBW32 * 4;    // 6400
+constexpr int kH0Bytes = kTH * kBW32 * 4;        // 1280
+constexpr int kBufS = kTile32Bytes + kUnBytes + kH0Bytes;  // 23424 per staging buffer
 constexpr int kOffTile32 = 2 * kStageBufBytes;
-constexpr int kOffMlp = kOffTile32 + kTile32Bytes;
+constexpr int kOffPlanes = kOffTile32 + kTile32Bytes;
+constexpr int kOffMlp = kOffPlanes + kPlanesBytes;
+constexpr int kOffPlanesS = 2 * kBufS;
+constexpr int kOffMlpS = kOffPlanesS + kPlanesBytes;
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
 
+// Absorbing envelope (enlightning.C:634-786) as per-level tables: for each
+// side, env[i] = 1 - exp(-ln2 d^2 / w^2) at the distance d of cell centre i
+// (column for L/R, row for B/T) from that side of the domain; null where the
+// side is not ABSORB.  The tables are computed on the host once per engine.
+struct AbsorbTables {
+  const double* env[kL][4];
+  const float* envf[kL][4];           // the same factors rounded to float
+  const unsigned char* cont[kL][4];   // |1 - env| > 1e-8: the walk goes on past this cell
+};
+
+// The reference walks every patch row from the L (R) side inwards and stops
+// after the first cell whose factor is within 1e-8 of 1 (on the first row it
+// does not start at all when the edge cell's factor is); B and T do the same
+// with whole rows.  The factors grow monotonically inwards, so whether cell
+// (i, j) of patch b is reached follows from its neighbour towards the side:
+// the walk is evaluated per cell.  The sides that reach the cell are returned
+// (0..3 = L, R, B, T) in the reference's order.
+__device__ __forceinline__ int absorb_walk(const AbsorbTables& T, int lvl, int i, int j, const int4& b,
+                                           int q[4]) {
+  int n = 0;
+  const unsigned char* c = T.cont[lvl][0];
+  if (c && (j != b.z || c[b.x]) && (i == b.x || c[i - 1])) q[n++] = 0;
+  c = T.cont[lvl][1];
+  if (c && (j != b.z || c[b.y]) && (i == b.y || c[i + 1])) q[n++] = 1;
+  c = T.cont[lvl][2];
+  if (c && c[b.z] && (j == b.z || c[j - 1])) q[n++] = 2;
+  c = T.cont[lvl][3];
+  if (c && c[b.w] && (j == b.w || c[j + 1])) q[n++] = 3;
+  return n;
+}
+
+// (q - ambient) * tmp + ambient, rounding like the reference's statement
+__device__ __forceinline__ double relax_(double q, double amb, double tmp) {
+  return __dadd_rn(__dmul_rn(__dsub_rn(q, amb), tmp), amb);
+}
+
 struct StageArgs {
-  CUtensorMap tmap[kL];  // input buffer, per level
-  double* in[kL];
-  double* out[kL];
-  const double* un[kL];  // u^n (current buffer)
-  const double* h0[kL];
+  CUtensorMap tmap[kL];     // input buffer, per level (halo box)
+  CUtensorMap tmap_un[kL];  // FP32 storage: u^n interior box
+  CUtensorMap tmap_h0[kL];  // FP32 storage: H0 interior box
+  int un_is_in;             // stage 1: u^n is the staged input itself
+  // canvases in the engine's storage type (double, or float perturbations)
+  void* in[kL];
+  void* out[kL];
+  const void* un[kL];  // u^n (current buffer)
+  const void* h0[kL];
   long pitch[kL], fstride[kL];
   RhsConst P[kL];
   FastConst F[kL];
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
+  float gm1_over_2rho0_f, inv_c_p_f, inv_c_v_f, R_f, inv_rho0_f;  // FP32-storage epilogue
   double a1, a2, bdt, beta;
   const double* dt_dev;  // adaptive time step in device memory (or null)
   const int4* tiles;
@@ -63,6 +128,9 @@ struct StageArgs {
   int* counter;
   int* health;
   unsigned long long* stats;  // [level][3]: weno cells, cells, cells decided by the plain-sensor fallback
+  AbsorbTables absorb;        // absorbing envelope, applied to each finished cell
+  bool any_absorb;
+  const int4* patchtab;       // patch boxes of all levels (tile .w = index)
   const float* mlp;           // learned-sensor parameters (FP32 vector) or null
   float margin;               // |p - 0.5| <= margin -> plain sensor decides
   float feat_eps, feat_eps_p, feat_inv_sqrt_eps;
@@ -83,18 +151,31 @@ struct SAcc64R {  // adapter with the accessor names rhs_cell expects
   __device__ double p(int di, int dj) const { return a.p(di, dj); }
   __device__ double t(int di, int dj) const { return a.tT(di, dj); }
 };
-struct SAcc32 {
+struct SAcc32 {  // single-precision tile and its planes
   const float* t;
-  int c;
-  __device__ float w(int k, int di, int dj) const { return t[k * (kBH * kBW) + c + dj * kBW + di]; }
-  __device__ float p(int di, int dj) const { return t[5 * (kBH * kBW) + c + dj * kBW + di]; }
-  __device__ float t_(int di, int dj) const { return t[6 * (kBH * kBW) + c + dj * kBW + di]; }
+  const float* pl;  // u, v, F_0..4, G_0..4
+  int c;            // (row)*kBW32 + col of the centre in the halo box
+  int cf, cg;       // the centre in the F planes (cy*kBW32 + cx + 3) and G planes ((cy+3)*32 + cx)
+  __device__ float w(int k, int di, int dj) const { return t[k * kPlane32 + c + dj * kBW32 + di]; }
+  __device__ float p(int di, int dj) const { return t[5 * kPlane32 + c + dj * kBW32 + di]; }
+  __device__ float t_(int di, int dj) const { return t[6 * kPlane32 + c + dj * kBW32 + di]; }
+  __device__ float u(int di, int dj) const { return pl[c + dj * kBW32 + di]; }
+  __device__ float v(int di, int dj) const { return pl[kPlOffV + c + dj * kBW32 + di]; }
+  __device__ float fx(int k, int di) const { return pl[kPlOffF + k * kPlaneF + cf + di]; }
+  __device__ float gy(int k, int dj) const { return pl[kPlOffG + k * kPlaneG + cg + dj * kTW]; }
 };
+__device__ __forceinline__ SAcc32 acc32(const float* t, const float* pl, int cx, int cy) {
+  return SAcc32{t, pl, (cy + 3) * kBW32 + (cx + 3), cy * kBW32 + cx + 3, (cy + 3) * kTW + cx};
+}
 struct SAcc32R {
   SAcc32 a;
   __device__ float w(int k, int di, int dj) const { return a.w(k, di, dj); }
   __device__ float p(int di, int dj) const { return a.p(di, dj); }
   __device__ float t(int di, int dj) const { return a.t_(di, dj); }
+  __device__ float u(int di, int dj) const { return a.u(di, dj); }
+  __device__ float v(int di, int dj) const { return a.v(di, dj); }
+  __device__ float fx(int k, int di) const { return a.fx(k, di); }
+  __device__ float gy(int k, int dj) const { return a.gy(k, dj); }
 };
 
 __device__ __forceinline__ void raise_health(int* h, int code) { atomicCAS(h, 0, code); }
@@ -104,18 +185,27 @@ __device__ __forceinline__ void raise_health(int* h, int code) { atomicCAS(h, 0,
 // of all 7 fields, decide WENO/DRP per cell, compact the cells so that each
 // warp runs one branch, compute KK, and finish the cell in place:
 // w = a1*u^n + a2*w + beta*dt*KK, then p and T (update_state).
+//
+// S is the storage type of the canvases.  S = double: absolute values, the
+// right-hand side in FP64 (FAST = false) or in FP32 perturbation form after a
+// conversion of the staged box (FAST = true).  S = float (FAST only): the
+// canvases hold perturbations about the ambient state, the box is staged
+// straight into the FP32 tile and the whole cell update is single precision.
 // ---------------------------------------------------------------------------
-template <int SCHEME, int ORDER, bool LLF, bool FAST>
-__global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ StageArgs A) {
-  // dynamic shared memory: two FP64 staging buffers (TMA destinations, the
-  // next tile's copy overlaps the current tile's compute) + one FP32 tile
+template <int SCHEME, int ORDER, bool LLF, bool FAST, typename S>
+__global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) stage_kernel(const __grid_constant__ StageArgs A) {
+  constexpr bool kF32S = std::is_same<S, float>::value;
+  static_assert(!kF32S || FAST, "single-precision storage runs the FP32 right-hand side");
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  double* stage_buf[2] = {reinterpret_cast<double*>(smem_raw),
-                          reinterpret_cast<double*>(smem_raw + kStageBufBytes)};
-  float* tile32 = reinterpret_cast<float*>(smem_raw + kOffTile32);
+  // TMA destinations: two FP64 boxes (FP64 storage) or two FP32 tiles (FP32
+  // storage); the next tile's copy overlaps the current tile's compute
+  unsigned char* dst[2] = {smem_raw, smem_raw + (kF32S ? kBufS : kStageBufBytes)};
+  float* tile32_conv = reinterpret_cast<float*>(smem_raw + kOffTile32);  // FP64 storage, FAST
+  float* planes = reinterpret_cast<float*>(smem_raw + (kF32S ? kOffPlanesS : kOffPlanes));  // FAST
   // learned sensor (FAST + hybrid only): network image and feature tile
-  MlpSmem* mlp_s = reinterpret_cast<MlpSmem*>(smem_raw + kOffMlp);
-  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + kOffMlp + align128((int)sizeof(MlpSmem)));
+  constexpr int kMlpOff = kF32S ? kOffMlpS : kOffMlp;
+  MlpSmem* mlp_s = reinterpret_cast<MlpSmem*>(smem_raw + kMlpOff);
+  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpOff + align128((int)sizeof(MlpSmem)));
   __shared__ unsigned char s_flag[256];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
@@ -125,16 +215,27 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
   const int ntiles = *A.ntiles;
   auto issue = [&](int t, int b) {
     const int4 td = A.tiles[t];
-    // a tiled TMA copy needs x * 8 bytes to be a multiple of 16 (x even);
-    // set_patches only accepts even patch origins and tiles are 32 wide
-    if (td.x & 1) {
+    // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
+    // doubles, a multiple of 4 for floats; set_patches only accepts such
+    // patch origins and tiles are 32 wide
+    if (td.x & (kF32S ? 3 : 1)) {
       raise_health(A.health, ENL_ERR_STATE);
       return false;
     }
     fence_proxy_async_smem();
-    mbar_arrive_expect_tx(&mbar[b], kTileBytes64);
-    // canvas column of cell i0-3 is i0 (ghost offset 3); i0 is even
-    tma_load_3d(stage_buf[b], &A.tmap[td.z & 0xff], td.x, td.y, 0, &mbar[b]);
+    const int lv = td.z & 0xff;
+    if constexpr (kF32S) {
+      // halo box, and the interior rows of u^n (unless u^n is the input) and H0;
+      // canvas column of cell i0-3 is i0, canvas row of cell j0 is j0+3
+      mbar_arrive_expect_tx(&mbar[b], kTileBytes32 + (A.un_is_in ? 0 : kUnBytes) + kH0Bytes);
+      tma_load_3d(dst[b], &A.tmap[lv], td.x, td.y, 0, &mbar[b]);
+      if (!A.un_is_in) tma_load_3d(dst[b] + kTile32Bytes, &A.tmap_un[lv], td.x, td.y + 3, 0, &mbar[b]);
+      tma_load_3d(dst[b] + kTile32Bytes + kUnBytes, &A.tmap_h0[lv], td.x, td.y + 3, 0, &mbar[b]);
+    } else {
+      mbar_arrive_expect_tx(&mbar[b], kTileBytes64);
+      // canvas column of cell i0-3 is i0 (ghost offset 3)
+      tma_load_3d(dst[b], &A.tmap[lv], td.x, td.y, 0, &mbar[b]);
+    }
     return true;
   };
   // TMA destinations must start on 128-byte boundaries; refuse to run otherwise
@@ -162,7 +263,8 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
       if (nt < ntiles && !issue(nt, b ^ 1)) nt = ntiles;
       s_t[b ^ 1] = nt;
     }
-    double* tile = stage_buf[b];
+    const double* tile = reinterpret_cast<const double*>(dst[b]);  // FP64 storage
+    float* tile32 = kF32S ? reinterpret_cast<float*>(dst[b]) : tile32_conv;
     const int4 td = A.tiles[t];
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     const int i0 = td.x, j0 = td.y;
@@ -175,62 +277,108 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
     }
     phase[b] ^= 1u;
     const double bdt = A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt;
-    if (FAST) {
-      const float rho0 = (float)A.rho0;
+    if (FAST && !kF32S) {
+      // FP64 box (rows of kBW) -> FP32 perturbations (rows of kBW32)
       for (int e = tid; e < kTileElems; e += 256) {
-        int k = e / (kBH * kBW);
+        const int k = e / (kBH * kBW), r = e - k * (kBH * kBW);
+        const int row = r / kBW, col = r - row * kBW;
         double v = tile[e];
         double amb = k == 0 ? A.rho0 : (k == 4 ? A.rho0 * A.T0 : (k == 5 ? A.p0 : (k == 6 ? A.T0 : 0.0)));
-        tile32[e] = (float)(v - amb);
+        tile32[k * kPlane32 + row * kBW32 + col] = (float)(v - amb);
       }
-      (void)rho0;
+      __syncthreads();
+    }
+    if (FAST) {
+      // planes of u, v and the fluxes at every halo position of the tile
+      const float rho0f = A.F[lvl].rho0, rT0f = A.F[lvl].rho0T0;
+      for (int e = tid; e < kBH * kBW; e += 256) {
+        const int row = e / kBW, col = e - row * kBW, o = row * kBW32 + col;
+        const float ir = rcp_approx(rho0f + tile32[o]);
+        const float u = tile32[kPlane32 + o] * ir, v = tile32[2 * kPlane32 + o] * ir;
+        const float pp = tile32[5 * kPlane32 + o];
+        planes[o] = u;
+        planes[kPlOffV + o] = v;
+        float wk[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) wk[k] = tile32[k * kPlane32 + o] + (k == 0 ? rho0f : (k == 4 ? rT0f : 0.0f));
+        if (row >= 3 && row < 3 + kTH) {  // x-fluxes on the interior rows
+#pragma unroll
+          for (int k = 0; k < 5; ++k)
+            planes[kPlOffF + k * kPlaneF + (row - 3) * kBW32 + col] = fmaf(u, wk[k], k == 1 ? pp : 0.0f);
+        }
+        if (col >= 3 && col < 3 + kTW) {  // y-fluxes on the interior columns
+#pragma unroll
+          for (int k = 0; k < 5; ++k)
+            planes[kPlOffG + k * kPlaneG + row * kTW + (col - 3)] = fmaf(v, wk[k], k == 2 ? pp : 0.0f);
+        }
+      }
       __syncthreads();
     }
     const int tx = lane, ty = warp;
     const bool valid = tx < w && ty < h;
     const int cc = (ty + 3) * kBW + (tx + 3);
+    const int cc32 = (ty + 3) * kBW32 + (tx + 3);
     int flag = 0;
     int fallback = 0;
     if (learned && lvl == 0) {
-      // learned switch: features -> BF16 MLP on the tensor cores (one warp per
-      // tile row, two m16 tiles) -> p; cells with |p - 0.5| <= margin fall
-      // back to the plain sensor
-      float fv[kFeat];
+      // learned switch: it refines the plain one and can only send cells the
+      // plain switch puts on WENO back to DRP.  Those cells are compacted,
+      // their features go through the BF16 MLP on the tensor cores (one warp
+      // per 16 cells), and cells with |logit| <= margin keep the plain
+      // decision.  Tiles without such cells skip the network.
+      int plain = 0;
       if (valid) {
-        SAcc32R acc{SAcc32{tile32, cc}};
-        cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
-      } else {
-#pragma unroll
-        for (int q = 0; q < kFeat; ++q) fv[q] = 0.f;
+        SAcc32R acc{acc32(tile32, planes, tx, ty)};
+        plain = sensor_fast(acc, A.F[lvl]);
       }
+      const unsigned bf = __ballot_sync(0xffffffffu, plain);
+      if (lane == 0) s_cnt[0][warp] = __popc(bf);
+      __syncthreads();
+      int nflag = 0, slot = 0;
 #pragma unroll
-      for (int q = 0; q < kFeat; q += 2)
-        *reinterpret_cast<uint32_t*>(feat + tid * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
-      __syncwarp();
+      for (int q = 0; q < 8; ++q) {
+        if (q < warp) slot += s_cnt[0][q];
+        nflag += s_cnt[0][q];
+      }
+      slot += __popc(bf & ((1u << lane) - 1u));
+      if (nflag > 0) {
+        if (plain) {
+          float fv[kFeat];
+          SAcc32R acc{acc32(tile32, planes, tx, ty)};
+          cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        MlpFwd16 F;
-        mlp_forward16(*mlp_s, feat + (warp * 32 + half * 16) * kFeat, kFeat, lane, F);
-        if ((lane & 3) == 0) {
-          int c0 = warp * 32 + half * 16 + (lane >> 2);
-          s_flag[c0] = (unsigned char)(F.logit[0] > 0.f ? 2 : 1) | (fabsf(F.logit[0]) <= A.margin ? 4 : 0);
-          s_flag[c0 + 8] = (unsigned char)(F.logit[1] > 0.f ? 2 : 1) | (fabsf(F.logit[1]) <= A.margin ? 4 : 0);
+          for (int q = 0; q < kFeat; q += 2)
+            *reinterpret_cast<uint32_t*>(feat + slot * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
+          s_list[slot] = tid;
         }
-      }
-      __syncwarp();
-      if (valid) {
-        unsigned char d = s_flag[tid];
-        if (d & 4) {
-          SAcc32R acc{SAcc32{tile32, cc}};
-          flag = sensor_fast(acc, A.F[lvl]);
-          fallback = 1;
-        } else {
-          flag = (d & 2) ? 1 : 0;
+        __syncthreads();
+        for (int g0 = warp * 16; g0 < nflag; g0 += 8 * 16) {
+          MlpFwd16 F;
+          mlp_forward16(*mlp_s, feat + g0 * kFeat, kFeat, lane, F);
+          if ((lane & 3) == 0) {
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const int sl = g0 + (lane >> 2) + 8 * hh;
+              if (sl < nflag)
+                s_flag[s_list[sl]] =
+                    (unsigned char)(F.logit[hh] > 0.f ? 2 : 1) | (fabsf(F.logit[hh]) <= A.margin ? 4 : 0);
+            }
+          }
+        }
+        __syncthreads();
+        if (plain) {
+          const unsigned char d = s_flag[tid];
+          if (d & 4) {
+            flag = 1;
+            fallback = 1;
+          } else {
+            flag = (d & 2) ? 1 : 0;
+          }
         }
       }
     } else if (valid) {
       if (FAST) {
-        SAcc32R acc{SAcc32{tile32, cc}};
+        SAcc32R acc{acc32(tile32, planes, tx, ty)};
         flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
       } else {
         SAcc64R acc{SAcc64{tile, cc}};
@@ -271,58 +419,126 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
       const int e = s_list[tid];
       const int cx = e & 31, cy = (e >> 5) & 0xff, f = (e >> 16) & 1;
       const int c2 = (cy + 3) * kBW + (cx + 3);
+      const int c32 = (cy + 3) * kBW32 + (cx + 3);
       const int gi = i0 + cx, gj = j0 + cy;  // level index
       const long g = (long)(gj + 3) * A.pitch[lvl] + (gi + 3);
       const long fs = A.fstride[lvl];
-      const double* un = A.un[lvl];
-      double* out = A.out[lvl];
-      double wn[5];
-      if (FAST) {
-        SAcc32R acc{SAcc32{tile32, c2}};
-        float H[5], K[5];
-        H[0] = (float)A.h0[lvl][g];
+      if constexpr (kF32S) {
+        // single precision throughout: perturbations in, perturbations out
+        // u^n and H0 of this cell from the prefetched interior boxes
+        const float* unb = reinterpret_cast<const float*>(dst[b] + kTile32Bytes);
+        const float* h0b = reinterpret_cast<const float*>(dst[b] + kTile32Bytes + kUnBytes);
+        const int ci = cy * kBW32 + cx + 3;
+        float* out = static_cast<float*>(A.out[lvl]);
+        SAcc32R acc{acc32(tile32, planes, cx, cy)};
+        float H[5], K[5], wn[5];
+        H[0] = h0b[ci];
         sources_fast(acc, A.F[lvl], H);
         fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
+        const float a1 = (float)A.a1, a2 = (float)A.a2, bdtf = (float)bdt;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-          double win = tile[k * (kBH * kBW) + c2];
-          wn[k] = fma(bdt, (double)K[k], fma(A.a1, un[k * fs + g], A.a2 * win));
+          const float w = tile32[k * kPlane32 + c32];
+          const float u0 = A.un_is_in ? w : unb[k * (kTH * kBW32) + ci];
+          wn[k] = fmaf(bdtf, K[k], fmaf(a1, u0, a2 * w));
         }
         // update_state in perturbation form (update_state.m4:90-105)
-        const float rp = (float)(wn[0] - A.rho0);
-        const float inv_r = 1.0f / (float)wn[0];
-        const float s = (float)wn[3] * inv_r;
-        const float h = (float)(A.ylo + A.dy[lvl] * ((double)gj + 0.5));
-        const float ccl = (float)A.c + (float)A.c_lr * h;
-        const float pp = (ccl * ccl) * ((rp + (float)A.gm1_over_2rho0 * (rp * rp)) + (float)wn[3] / (float)A.c_p);
-        const float x = (s + (float)A.R * log1pf(rp / (float)A.rho0)) / (float)A.c_v;
-        const float tp = (float)A.T0 * expm1f(x);
-        out[5 * fs + g] = A.p0 + (double)pp;
-        out[6 * fs + g] = A.T0 + (double)tp;
-      } else {
-        SAcc64R acc{SAcc64{tile, c2}};
-        double H[5], K[5];
-        H[0] = A.h0[lvl][g];
-        rhs_sources(acc, A.P[lvl], H);
-        rhs_fluxes<SCHEME, ORDER, LLF>(acc, A.P[lvl], gj, f, H, K);
+        const FastConst& F = A.F[lvl];
+        const float rp = wn[0];
+        const float rho = F.rho0 + rp;
+        const float s = wn[3] * rcp_approx(rho);
+        const float hgt = F.ylo + F.dy * ((float)gj + 0.5f);
+        const float ccl = F.c + F.c_lr * hgt;
+        const float pp = (ccl * ccl) * ((rp + A.gm1_over_2rho0_f * (rp * rp)) + wn[3] * A.inv_c_p_f);
+        const float x = (s + A.R_f * log1pf(rp * A.inv_rho0_f)) * A.inv_c_v_f;
+        float tp = F.T0 * expm1f(x);
+        float pq = pp;
+        if (A.any_absorb) {  // perturbations relax towards 0
+          int side[4];
+          const int na = absorb_walk(A.absorb, lvl, gi, gj, A.patchtab[td.w], side);
+          for (int q = 0; q < na; ++q) {
+            const float t_ = A.absorb.envf[lvl][side[q]][side[q] < 2 ? gi : gj];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          double win = tile[k * (kBH * kBW) + c2];
-          wn[k] = __dadd_rn(__dadd_rn(__dmul_rn(A.a1, un[k * fs + g]), __dmul_rn(A.a2, win)),
-                            __dmul_rn(bdt, K[k]));
+            for (int k = 0; k < 5; ++k) wn[k] *= t_;
+            pq *= t_;
+            tp *= t_;
+          }
         }
-        const double hgt = __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)gj + 0.5));
-        const double cc_ = __dadd_rn(A.c, __dmul_rn(A.c_lr, hgt));
-        const double d = __dsub_rn(wn[0], A.rho0);
-        const double s = __ddiv_rn(wn[3], wn[0]);
-        const double inner = __dadd_rn(__dadd_rn(d, __dmul_rn(A.gm1_over_2rho0, __dmul_rn(d, d))),
-                                       __dmul_rn(__ddiv_rn(wn[0], A.c_p), s));
-        out[5 * fs + g] = __dadd_rn(__dmul_rn(__dmul_rn(cc_, cc_), inner), A.p0);
-        out[6 * fs + g] = A.T0 * exp((s - A.R * log(A.rho0 / wn[0])) / A.c_v);
-      }
 #pragma unroll
-      for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
-      if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
+        for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
+        out[5 * fs + g] = pq;
+        out[6 * fs + g] = tp;
+        if (!(rho > 0.f) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
+      } else {
+        const double* un = static_cast<const double*>(A.un[lvl]);
+        double* out = static_cast<double*>(A.out[lvl]);
+        double wn[5], pv, tv;
+        if (FAST) {
+          SAcc32R acc{acc32(tile32, planes, cx, cy)};
+          float H[5], K[5];
+          H[0] = (float)static_cast<const double*>(A.h0[lvl])[g];
+          sources_fast(acc, A.F[lvl], H);
+          fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            double win = tile[k * (kBH * kBW) + c2];
+            wn[k] = fma(bdt, (double)K[k], fma(A.a1, un[k * fs + g], A.a2 * win));
+          }
+          // update_state in perturbation form (update_state.m4:90-105)
+          const float rp = (float)(wn[0] - A.rho0);
+          const float inv_r = 1.0f / (float)wn[0];
+          const float s = (float)wn[3] * inv_r;
+          const float h = (float)(A.ylo + A.dy[lvl] * ((double)gj + 0.5));
+          const float ccl = (float)A.c + (float)A.c_lr * h;
+          const float pp = (ccl * ccl) * ((rp + (float)A.gm1_over_2rho0 * (rp * rp)) + (float)wn[3] / (float)A.c_p);
+          const float x = (s + (float)A.R * log1pf(rp / (float)A.rho0)) / (float)A.c_v;
+          const float tp = (float)A.T0 * expm1f(x);
+          pv = A.p0 + (double)pp;
+          tv = A.T0 + (double)tp;
+        } else {
+          SAcc64R acc{SAcc64{tile, c2}};
+          double H[5], K[5];
+          H[0] = static_cast<const double*>(A.h0[lvl])[g];
+          rhs_sources(acc, A.P[lvl], H);
+          rhs_fluxes<SCHEME, ORDER, LLF>(acc, A.P[lvl], gj, f, H, K);
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            double win = tile[k * (kBH * kBW) + c2];
+            wn[k] = __dadd_rn(__dadd_rn(__dmul_rn(A.a1, un[k * fs + g]), __dmul_rn(A.a2, win)),
+                              __dmul_rn(bdt, K[k]));
+          }
+          const double hgt = __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)gj + 0.5));
+          const double cc_ = __dadd_rn(A.c, __dmul_rn(A.c_lr, hgt));
+          const double d = __dsub_rn(wn[0], A.rho0);
+          const double s = __ddiv_rn(wn[3], wn[0]);
+          const double inner = __dadd_rn(__dadd_rn(d, __dmul_rn(A.gm1_over_2rho0, __dmul_rn(d, d))),
+                                         __dmul_rn(__ddiv_rn(wn[0], A.c_p), s));
+          pv = __dadd_rn(__dmul_rn(__dmul_rn(cc_, cc_), inner), A.p0);
+          tv = A.T0 * exp((s - A.R * log(A.rho0 / wn[0])) / A.c_v);
+        }
+        if (A.any_absorb) {  // absolute values relax towards the ambient state
+          int side[4];
+          double fa[4];
+          const int na = absorb_walk(A.absorb, lvl, gi, gj, A.patchtab[td.w], side);
+          for (int q = 0; q < na; ++q) fa[q] = A.absorb.env[lvl][side[q]][side[q] < 2 ? gi : gj];
+          const double rT = __dmul_rn(A.T0, A.rho0);
+          for (int q = 0; q < na; ++q) {
+            pv = relax_(pv, A.p0, fa[q]);
+            tv = relax_(tv, A.T0, fa[q]);
+            wn[0] = relax_(wn[0], A.rho0, fa[q]);
+            wn[1] = __dmul_rn(wn[1], fa[q]);
+            wn[2] = __dmul_rn(wn[2], fa[q]);
+            wn[3] = __dmul_rn(wn[3], fa[q]);
+            wn[4] = relax_(wn[4], rT, fa[q]);
+          }
+        }
+        out[5 * fs + g] = pv;
+        out[6 * fs + g] = tv;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
+        if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4]))
+          raise_health(A.health, ENL_ERR_NONFINITE);
+      }
     }
     __syncthreads();  // this staging buffer is refilled two tiles later
     t = s_t[b ^ 1];
@@ -333,18 +549,23 @@ __global__ void __launch_bounds__(256, 2) stage_kernel(const __grid_constant__ S
 // ---------------------------------------------------------------------------
 // Ghost fill and transfer kernels (canvas form)
 // ---------------------------------------------------------------------------
-struct CanvasView {
-  double* base;
+// A level canvas in storage type S: absolute values (double) or
+// perturbations about the ambient state (float).
+template <typename S>
+struct CanvasT {
+  S* base;
   long pitch, fstride;
   int nx, ny;
-  __device__ double& at(int k, int i, int j) const { return base[k * fstride + (long)(j + 3) * pitch + (i + 3)]; }
+  __device__ S& at(int k, int i, int j) const { return base[k * fstride + (long)(j + 3) * pitch + (i + 3)]; }
 };
+using CanvasView = CanvasT<double>;
 
 // Physical ghost band of one level (enlightning.C:830-1008 for the patch that
 // touches each side): edge ghosts copy the first interior cell of their row or
 // column, corners copy the interior corner cell; the normal momentum is
 // negated on REFLECT sides (both momenta in a corner of two REFLECT sides).
-__global__ void physbc_kernel(CanvasView V, int nfields, int bcL, int bcR, int bcB, int bcT) {
+template <typename S>
+__global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int bcB, int bcT) {
   const int nx = V.nx, ny = V.ny;
   const long nedge_x = 3L * ny, nedge_y = 3L * nx;
   const long total = (2 * nedge_x + 2 * nedge_y + 36) * nfields;
@@ -382,7 +603,7 @@ __global__ void physbc_kernel(CanvasView V, int nfields, int bcL, int bcR, int b
       negu = (xs ? bcR : bcL) == kReflect;
       negv = (ys ? bcT : bcB) == kReflect;
     }
-    double v = V.at(k, si, sj);
+    S v = V.at(k, si, sj);
     if ((k == 1 && negu) || (k == 2 && negv)) v = -v;
     V.at(k, i, j) = v;
   }
@@ -392,7 +613,8 @@ __global__ void physbc_kernel(CanvasView V, int nfields, int bcL, int bcR, int b
 // its 3-cell band is filled by the single-patch rule of enlightning.C:830-1008
 // (edges from the first interior cell, corners from the interior corner, the
 // normal momenta negated on REFLECT sides).  One block per patch.
-__global__ void physbc_patches_kernel(CanvasView V, const int4* patches, int off, int cnt, int bcL, int bcR,
+template <typename S>
+__global__ void physbc_patches_kernel(CanvasT<S> V, const int4* patches, int off, int cnt, int bcL, int bcR,
                                       int bcB, int bcT) {
   for (int p = blockIdx.x; p < cnt; p += gridDim.x) {
     const int4 b = patches[off + p];
@@ -428,7 +650,7 @@ __global__ void physbc_patches_kernel(CanvasView V, const int4* patches, int off
         negu = (xs ? bcR : bcL) == kReflect;
         negv = (ys ? bcT : bcB) == kReflect;
       }
-      double v = V.at(k, si, sj);
+      S v = V.at(k, si, sj);
       if ((k == 1 && negu) || (k == 2 && negv)) v = -v;
       V.at(k, i, j) = v;
     }
@@ -437,15 +659,19 @@ __global__ void physbc_patches_kernel(CanvasView V, const int4* patches, int off
 
 // Coarse-fine ghosts: bilinear interpolation in cell centres from the
 // coarser canvas.  One warp per halo row segment (j, i_begin, i_end).
-__device__ __forceinline__ void refine_weights(int I, int r, int& ic, double& f) {
+// Weights in the storage type: for a power-of-two ratio every step is exact
+// in float as well as in double (I < 2^22).
+template <typename S>
+__device__ __forceinline__ void refine_weights(int I, int r, int& ic, S& f) {
   // fine cell centre in coarse index coordinates: (I + 0.5)/r - 0.5
-  double xc = ((double)I + 0.5) / (double)r - 0.5;
-  double fl = floor(xc);
+  S xc = ((S)I + (S)0.5) / (S)r - (S)0.5;
+  S fl = floor(xc);
   ic = (int)fl;
   f = xc - fl;
 }
 
-__global__ void interp_kernel(CanvasView F, CanvasView C, int ratio, const int4* segs, const int* meta, int moff,
+template <typename S>
+__global__ void interp_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4* segs, const int* meta, int moff,
                               int mcnt, int nfields) {
   const int off = meta[moff], cnt = meta[mcnt];
   const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -454,17 +680,17 @@ __global__ void interp_kernel(CanvasView F, CanvasView C, int ratio, const int4*
     int4 sg = segs[off + s];
     int J = sg.x;
     int jc;
-    double fy;
+    S fy;
     refine_weights(J, ratio, jc, fy);
     for (int I = sg.y + lane; I <= sg.z; I += 32) {
       int ic;
-      double fx;
+      S fx;
       refine_weights(I, ratio, ic, fx);
       for (int k = 0; k < nfields; ++k) {
-        double c00 = C.at(k, ic, jc), c10 = C.at(k, ic + 1, jc), c01 = C.at(k, ic, jc + 1), c11 = C.at(k, ic + 1, jc + 1);
-        double lo = (1.0 - fx) * c00 + fx * c10;
-        double hi = (1.0 - fx) * c01 + fx * c11;
-        F.at(k, I, J) = (1.0 - fy) * lo + fy * hi;
+        S c00 = C.at(k, ic, jc), c10 = C.at(k, ic + 1, jc), c01 = C.at(k, ic, jc + 1), c11 = C.at(k, ic + 1, jc + 1);
+        S lo = ((S)1 - fx) * c00 + fx * c10;
+        S hi = ((S)1 - fx) * c01 + fx * c11;
+        F.at(k, I, J) = ((S)1 - fy) * lo + fy * hi;
       }
     }
   }
@@ -472,7 +698,8 @@ __global__ void interp_kernel(CanvasView F, CanvasView C, int ratio, const int4*
 
 // Generic tile-list kernels: one block of 256 threads per 32x8 tile.
 // Coarsening: coarse cell = mean of its ratio x ratio fine cells (7 fields).
-__global__ void coarsen_kernel(CanvasView C, CanvasView F, int ratio, const int4* tiles, const int* meta, int moff,
+template <typename S>
+__global__ void coarsen_kernel(CanvasT<S> C, CanvasT<S> F, int ratio, const int4* tiles, const int* meta, int moff,
                                int mcnt) {
   const int off = meta[moff], cnt = meta[mcnt];
   for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
@@ -481,9 +708,9 @@ __global__ void coarsen_kernel(CanvasView C, CanvasView F, int ratio, const int4
     int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx >= w || ty >= h) continue;
     int I = td.x + tx, J = td.y + ty;
-    double inv = 1.0 / (double)(ratio * ratio);
+    S inv = (S)1 / (S)(ratio * ratio);
     for (int k = 0; k < kNF; ++k) {
-      double s = 0.0;
+      S s = 0;
       for (int b = 0; b < ratio; ++b)
         for (int a = 0; a < ratio; ++a) s += F.at(k, I * ratio + a, J * ratio + b);
       C.at(k, I, J) = s * inv;
@@ -492,7 +719,8 @@ __global__ void coarsen_kernel(CanvasView C, CanvasView F, int ratio, const int4
 }
 
 // Copy patch interiors between two buffers of the same level (7 fields).
-__global__ void copy_tiles_kernel(CanvasView dst, CanvasView src, const int4* tiles, int off, int cnt) {
+template <typename S>
+__global__ void copy_tiles_kernel(CanvasT<S> dst, CanvasT<S> src, const int4* tiles, int off, int cnt) {
   for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
     int4 td = tiles[off + t];
     int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
@@ -503,18 +731,19 @@ __global__ void copy_tiles_kernel(CanvasView dst, CanvasView src, const int4* ti
 }
 
 // Bilinear fill of whole boxes (new fine data after a regrid).
-__global__ void refine_box_kernel(CanvasView F, CanvasView C, int ratio, int ilo, int jlo, int w, int h) {
+template <typename S>
+__global__ void refine_box_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, int ilo, int jlo, int w, int h) {
   long n = (long)w * h;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     int I = ilo + (int)(t % w), J = jlo + (int)(t / w);
     int ic, jc;
-    double fx, fy;
+    S fx, fy;
     refine_weights(I, ratio, ic, fx);
     refine_weights(J, ratio, jc, fy);
     for (int k = 0; k < kNF; ++k) {
-      double lo = (1.0 - fx) * C.at(k, ic, jc) + fx * C.at(k, ic + 1, jc);
-      double hi = (1.0 - fx) * C.at(k, ic, jc + 1) + fx * C.at(k, ic + 1, jc + 1);
-      F.at(k, I, J) = (1.0 - fy) * lo + fy * hi;
+      S lo = ((S)1 - fx) * C.at(k, ic, jc) + fx * C.at(k, ic + 1, jc);
+      S hi = ((S)1 - fx) * C.at(k, ic, jc + 1) + fx * C.at(k, ic + 1, jc + 1);
+      F.at(k, I, J) = ((S)1 - fy) * lo + fy * hi;
     }
   }
 }
@@ -528,7 +757,10 @@ __device__ __forceinline__ bool ratio_below_e(double fm, double f0, double fp, d
   return __ddiv_rn(num, den) < Lit::c0_9999;
 }
 
-__global__ void tag_tiles_kernel(int* tags, CanvasView W, CanvasView H, const int4* tiles, int off, int cnt,
+// The ratio test depends on differences only, so it reads perturbation
+// storage as it is.
+template <typename S>
+__global__ void tag_tiles_kernel(int* tags, CanvasT<S> W, CanvasT<S> H, const int4* tiles, int off, int cnt,
                                  double ep0, double ep1) {
   for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
     int4 td = tiles[off + t];
@@ -544,71 +776,39 @@ __global__ void tag_tiles_kernel(int* tags, CanvasView W, CanvasView H, const in
   }
 }
 
-// Absorbing envelope per patch (enlightning.C:634-786, loop-exit rules kept):
-// one thread per patch row (L/R) or column (B/T).  Patches come from a table
-// (ilo, ihi, jlo, jhi); the envelope distance uses the level's cell centres.
-struct AbsorbArgs {
-  double dx0, dx1, gxlo0, gxlo1, gxhi0, gxhi1, w2, p0, T0, rho0;
+// Absorbing envelope of the plain path (enlightning.C:634-786): one thread
+// per patch cell of every level, the same per-cell rule and tables as the
+// fused stage kernel; amb[] is the ambient state in storage terms.
+struct AbsorbTileArgs {
+  AbsorbTables T;
+  CanvasView lev[kL];
+  const int4* tiles;
+  const int4* patchtab;
+  int ntiles;
+  double p0, T0, rho0;
 };
 
-__device__ __forceinline__ double env_(double d, double w2) {
-  return __dadd_rn(-exp(__dmul_rn(__ddiv_rn(-log(2.0), w2), __dmul_rn(d, d))), 1.0);
-}
-__device__ __forceinline__ double relax_(double q, double amb, double tmp) {
-  return __dadd_rn(__dmul_rn(__dsub_rn(q, amb), tmp), amb);
-}
-
-__global__ void absorb_patches_kernel(CanvasView V, const int4* patches, int off, int cnt, int dir, AbsorbArgs A) {
-  const double ep = 1.0e-8;
-  // grid-stride over (patch, row/column); the host passes a bound on rows
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x;; t += (long)gridDim.x * blockDim.x) {
-    long acc = 0;
-    int p = -1, r = 0;
-    for (int q = 0; q < cnt; ++q) {
-      int4 b = patches[off + q];
-      int n = dir < 2 ? (b.w - b.z + 1) : (b.y - b.x + 1);
-      if (t < acc + n) {
-        p = q;
-        r = (int)(t - acc);
-        break;
-      }
-      acc += n;
-    }
-    if (p < 0) return;
-    int4 b = patches[off + p];
-    auto apply = [&](int i, int j, double tmp) {
-      V.at(5, i, j) = relax_(V.at(5, i, j), A.p0, tmp);
-      V.at(6, i, j) = relax_(V.at(6, i, j), A.T0, tmp);
-      V.at(0, i, j) = relax_(V.at(0, i, j), A.rho0, tmp);
-      V.at(1, i, j) = __dmul_rn(V.at(1, i, j), tmp);
-      V.at(2, i, j) = __dmul_rn(V.at(2, i, j), tmp);
-      V.at(3, i, j) = __dmul_rn(V.at(3, i, j), tmp);
-      V.at(4, i, j) = relax_(V.at(4, i, j), __dmul_rn(A.T0, A.rho0), tmp);
-    };
-    if (dir < 2) {
-      int j = b.z + r;
-      auto dist = [&](int i) {
-        double xc = A.gxlo0 + A.dx0 * ((double)i + 0.5);
-        return dir == 0 ? (xc - A.gxlo0) : (A.gxhi0 - xc);
-      };
-      double tmp = (r == 0) ? env_(dist(dir == 0 ? b.x : b.y), A.w2) : 0.0;
-      for (int n = 0; fabs(1.0 - tmp) > ep && n <= b.y - b.x; ++n) {
-        int i = dir == 0 ? b.x + n : b.y - n;
-        tmp = env_(dist(i), A.w2);
-        apply(i, j, tmp);
-      }
-    } else {
-      int i = b.x + r;
-      auto dist = [&](int j) {
-        double yc = A.gxlo1 + A.dx1 * ((double)j + 0.5);
-        return dir == 2 ? (yc - A.gxlo1) : (A.gxhi1 - yc);
-      };
-      double tmp = env_(dist(dir == 2 ? b.z : b.w), A.w2);
-      for (int n = 0; fabs(1.0 - tmp) > ep && n <= b.w - b.z; ++n) {
-        int j = dir == 2 ? b.z + n : b.w - n;
-        tmp = env_(dist(j), A.w2);
-        apply(i, j, tmp);
-      }
+__global__ void absorb_tiles_kernel(AbsorbTileArgs A) {
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const int4 td = A.tiles[t];
+    const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    if (tx >= w || ty >= h) continue;
+    const int i = td.x + tx, j = td.y + ty;
+    int side[4];
+    double fa[4];
+    const int na = absorb_walk(A.T, lvl, i, j, A.patchtab[td.w], side);
+    for (int q = 0; q < na; ++q) fa[q] = A.T.env[lvl][side[q]][side[q] < 2 ? i : j];
+    const CanvasView& V = A.lev[lvl];
+    const double rT = __dmul_rn(A.T0, A.rho0);
+    for (int q = 0; q < na; ++q) {
+      V.at(5, i, j) = relax_(V.at(5, i, j), A.p0, fa[q]);
+      V.at(6, i, j) = relax_(V.at(6, i, j), A.T0, fa[q]);
+      V.at(0, i, j) = relax_(V.at(0, i, j), A.rho0, fa[q]);
+      V.at(1, i, j) = __dmul_rn(V.at(1, i, j), fa[q]);
+      V.at(2, i, j) = __dmul_rn(V.at(2, i, j), fa[q]);
+      V.at(3, i, j) = __dmul_rn(V.at(3, i, j), fa[q]);
+      V.at(4, i, j) = relax_(V.at(4, i, j), rT, fa[q]);
     }
   }
 }
@@ -695,7 +895,8 @@ __device__ double capsule_union(double H, double xc0, double xc1, const PaintArg
   return H;
 }
 
-__global__ void paint_kernel(CanvasView H, const int4* tiles, int off, int cnt, PaintArgs A) {
+template <typename S>
+__global__ void paint_kernel(CanvasT<S> H, const int4* tiles, int off, int cnt, PaintArgs A) {
   for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
     int4 td = tiles[off + t];
     int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
@@ -705,15 +906,15 @@ __global__ void paint_kernel(CanvasView H, const int4* tiles, int off, int cnt, 
     double xc0 = A.xlo0 + A.dx0 * ((double)i + 0.5);
     double xc1 = A.xlo1 + A.dx1 * ((double)j + 0.5);
     double x0 = xc0 - A.pos0, x1 = xc1 - A.pos1;
-    double& out = H.at(0, i, j);
+    S& out = H.at(0, i, j);
     if (A.type == 10) {  // POINT (PULSE) / DRIVEN point
       double v = A.amp * exp(-A.inv_s2ln2 * (x0 * x0 + x1 * x1));
-      out = A.mode == 20 ? v * A.drive : v;
+      out = (S)(A.mode == 20 ? v * A.drive : v);
     } else if (A.type == 20) {  // SINE
       double d = x0 - A.sine_amp * sin(A.sine_freq * x1);
-      out = A.amp * exp(-A.inv_s2ln2 * (d * d));
+      out = (S)(A.amp * exp(-A.inv_s2ln2 * (d * d)));
     } else {  // LIGHTNING
-      out = capsule_union(out, xc0, xc1, A);
+      out = (S)capsule_union((double)out, xc0, xc1, A);
     }
   }
 }
@@ -721,9 +922,11 @@ __global__ void paint_kernel(CanvasView H, const int4* tiles, int off, int cnt, 
 // Overpressure dp (read from H0) -> state at s = 0, c_lr = 0, inverting
 // update_state.m4:90-94: dp/c^2 = drho + (gamma-1)/(2 rho0) drho^2; T from
 // update_state.m4:103-105; rho*T_n = rho*T (nitrogen mode in equilibrium).
-__global__ void overpressure_state_kernel(CanvasView S, CanvasView H, const int4* tiles, int off, int cnt,
+template <typename S>
+__global__ void overpressure_state_kernel(CanvasT<S> V, CanvasT<S> H, const int4* tiles, int off, int cnt,
                                           double rho0, double c, double gm1_over_2rho0, double p0, double T0,
-                                          double R, double c_v) {
+                                          double R, double c_v, double a0, double a4,
+                                          double a5, double a6) {
   for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
     int4 td = tiles[off + t];
     int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
@@ -736,14 +939,15 @@ __global__ void overpressure_state_kernel(CanvasView S, CanvasView H, const int4
     double drho = (-1.0 + sqrt(1.0 + 4.0 * k * x)) / (2.0 * k);
     double rho = rho0 + drho;
     double T = T0 * exp((0.0 - R * log(rho0 / rho)) / c_v);
-    S.at(0, i, j) = rho;
-    S.at(1, i, j) = 0.0;
-    S.at(2, i, j) = 0.0;
-    S.at(3, i, j) = 0.0;
-    S.at(4, i, j) = rho * T;
-    S.at(5, i, j) = (c * c) * (drho + k * (drho * drho)) + p0;
-    S.at(6, i, j) = T;
-    H.at(0, i, j) = 0.0;
+    // a0, a4, a5, a6: ambient parts held out of the storage (0 for absolute)
+    V.at(0, i, j) = (S)(rho - a0);
+    V.at(1, i, j) = 0;
+    V.at(2, i, j) = 0;
+    V.at(3, i, j) = 0;
+    V.at(4, i, j) = (S)(rho * T - a4);
+    V.at(5, i, j) = (S)(((c * c) * (drho + k * (drho * drho)) + p0) - a5);
+    V.at(6, i, j) = (S)(T - a6);
+    H.at(0, i, j) = 0;
   }
 }
 
@@ -773,15 +977,21 @@ __global__ void tag_block_kernel(const int* tags, int nx, int ny, int B, int buf
 // .m4:270-284, with c_lr = 0).  Block-level max with warp shuffles, one
 // 64-bit atomicMax per block (non-negative doubles order like their bits).
 // ---------------------------------------------------------------------------
+template <typename S>
 struct SpeedArgs {
-  CanvasView lev[kL];
+  CanvasT<S> lev[kL];
   const int4* tiles;
   const int* ntiles;
   double c;
+  double rho_off;  // ambient density held out of the storage (0 for absolute)
   unsigned long long* smax_bits;
 };
 
-__global__ void speed_kernel(SpeedArgs A) {
+// max(|rho u|, |rho v|) / |rho| is max(|u|, |v|) bit for bit (a correctly
+// rounded division is monotonic), with one division instead of two.  With
+// perturbation storage the speed is formed in single precision.
+template <typename S>
+__global__ void speed_kernel(SpeedArgs<S> A) {
   __shared__ double s_w[8];
   const int n = *A.ntiles;
   double m = 0.0;
@@ -790,10 +1000,16 @@ __global__ void speed_kernel(SpeedArgs A) {
     int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx < w && ty < h) {
-      const CanvasView& V = A.lev[lvl];
+      const CanvasT<S>& V = A.lev[lvl];
       int i = td.x + tx, j = td.y + ty;
-      double r = V.at(0, i, j);
-      double s = fmax(fabs(V.at(1, i, j) / r), fabs(V.at(2, i, j) / r)) + A.c;
+      double s;
+      if constexpr (std::is_same<S, float>::value) {
+        const float r = (float)A.rho_off + V.at(0, i, j);
+        s = (double)(fmaxf(fabsf(V.at(1, i, j)), fabsf(V.at(2, i, j))) / fabsf(r) + (float)A.c);
+      } else {
+        const double r = V.at(0, i, j);
+        s = fmax(fabs(V.at(1, i, j)), fabs(V.at(2, i, j))) / fabs(r) + A.c;
+      }
       if (!(s == s)) s = 1e300;  // NaN state: force a tiny dt, health check reports it
       m = fmax(m, s);
     }
@@ -819,31 +1035,99 @@ __global__ void dt_kernel(unsigned long long* smax_bits, double* dt, double* tim
   *smax_bits = 0ull;
 }
 
+// ---------------------------------------------------------------------------
+// Virtual microphones, enlightning::recordAudio (enlightning.C:2392-2506):
+// after a step, every patch of every level whose physical extent
+// [xlo, xhi] x [ylo, yhi] (closed) contains a microphone records the
+// pressure at i = int((x - xlo)/dx), j = int((y - ylo)/dy), read as element
+// j*nx + i of the patch interior, as the reference indexes it (a microphone
+// on a patch's upper edge therefore reads the first cell of the next row;
+// past the last row the reference reads outside the array, recorded here as
+// NaN).  One thread per (microphone, patch); matches are appended to a
+// device buffer with the iteration, level and patch index, so the host can
+// restore the reference's file order (level, then patch, per microphone).
+// ---------------------------------------------------------------------------
+struct MicRecord {
+  int iteration, mic, level, patch;
+  double p;
+};
+
+template <typename S>
+struct MicArgs {
+  CanvasT<S> lev[kL];
+  double dx[kL][2];
+  double xlo0, xlo1, p_off;
+  const int4* patchtab;
+  const int* patch_first;       // device: first patch-table index per level, then the total
+  int nmics;
+  const double* mics;           // x, y per microphone
+  const int* iteration;         // device counter of completed steps
+  MicRecord* rec;
+  unsigned long long* count;
+  long long cap;
+};
+
+template <typename S>
+__global__ void mic_kernel(MicArgs<S> A) {
+  const int it = *A.iteration + 1;  // the step just completed
+  const int npatch = A.patch_first[kL];
+  const long long n = (long long)A.nmics * npatch;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(t % A.nmics), pi = (int)(t / A.nmics);
+    int lvl = 0;
+    while (lvl + 1 < kL && pi >= A.patch_first[lvl + 1]) ++lvl;
+    const int4 b = A.patchtab[pi];
+    const double dx = A.dx[lvl][0], dy = A.dx[lvl][1];
+    // patch extent as SAMRAI's CartesianPatchGeometry forms it (no fused multiply-add)
+    const double xl = __dadd_rn(A.xlo0, __dmul_rn(dx, (double)b.x));
+    const double xh = __dadd_rn(A.xlo0, __dmul_rn(dx, (double)(b.y + 1)));
+    const double yl = __dadd_rn(A.xlo1, __dmul_rn(dy, (double)b.z));
+    const double yh = __dadd_rn(A.xlo1, __dmul_rn(dy, (double)(b.w + 1)));
+    const double mx = A.mics[2 * k], my = A.mics[2 * k + 1];
+    if (!(mx >= xl && mx <= xh && my >= yl && my <= yh)) continue;
+    const int nx = b.y - b.x + 1, ny = b.w - b.z + 1;
+    const int i = (int)__ddiv_rn(__dsub_rn(mx, xl), dx), j = (int)__ddiv_rn(__dsub_rn(my, yl), dy);
+    const long long idx = (long long)j * nx + i;
+    double p = __longlong_as_double(0x7ff8000000000000LL);  // NaN
+    if (idx >= 0 && idx < (long long)nx * ny)
+      p = A.p_off + (double)A.lev[lvl].at(5, b.x + (int)(idx % nx), b.z + (int)(idx / nx));
+    const unsigned long long slot = atomicAdd(A.count, 1ull);
+    if ((long long)slot < A.cap) A.rec[slot] = MicRecord{it, k, lvl, pi, p};
+  }
+}
+
+// Advances the device iteration counter after mic_kernel has read it (the
+// next launch on the stream).
+__global__ void mic_advance_kernel(int* iteration) { *iteration += 1; }
+
 // Pack / unpack the patch interiors of every level (7 fields) into a dense
 // buffer: field k of the cell (tx, ty) of tile t sits at
 // k*total + off[t] + ty*w + tx.  Used to exchange the hierarchy state with
 // host memory.
+template <typename S>
 struct PackArgs {
-  CanvasView lev[kL];
+  CanvasT<S> lev[kL];
   const int4* tiles;
   const long long* off;
   int ntiles;
   long long total;
-  double* packed;
+  S* packed;
   int unpack;
 };
 
-__global__ void pack_kernel(PackArgs A) {
+template <typename S>
+__global__ void pack_kernel(PackArgs<S> A) {
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
     int4 td = A.tiles[t];
     int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx >= w || ty >= h) continue;
     long long o = A.off[t] + ty * w + tx;
-    const CanvasView& V = A.lev[lvl];
+    const CanvasT<S>& V = A.lev[lvl];
     for (int k = 0; k < kNF; ++k) {
-      double& c = V.at(k, td.x + tx, td.y + ty);
-      double& p = A.packed[k * A.total + o];
+      S& c = V.at(k, td.x + tx, td.y + ty);
+      S& p = A.packed[k * A.total + o];
       if (A.unpack) c = p;
       else p = c;
     }
@@ -859,11 +1143,14 @@ __global__ void pack_kernel(PackArgs A) {
 // Every WENO-flagged cell is kept; DRP cells are kept with probability
 // keep0 (hash of the cell and `seed`).
 // ---------------------------------------------------------------------------
+template <typename S>
 struct HarvestArgs {
-  CanvasView V;
-  CanvasView H;
+  CanvasT<S> V;
+  CanvasT<S> H;
+  double amb_off[kNF];  // ambient parts held out of the storage (0 for absolute)
   RhsConst P;
   float eps, eps_p, inv_sqrt_eps, rho0, p0, T0;
+  double rho0_d, p0_d;
   const int4* tiles;
   int off, cnt;
   double dt;
@@ -875,29 +1162,40 @@ struct HarvestArgs {
   long cap;
 };
 
+// Absolute values: the storage plus its held-out ambient part (adding 0.0
+// to a double is exact).
+template <typename S>
 struct CanvasAcc64 {
-  const CanvasView* V;
+  const CanvasT<S>* V;
+  const double* off;
   int i, j;
-  __device__ double w(int k, int di, int dj) const { return V->at(k, i + di, j + dj); }
-  __device__ double p(int di, int dj) const { return V->at(5, i + di, j + dj); }
-  __device__ double t(int di, int dj) const { return V->at(6, i + di, j + dj); }
+  __device__ double w(int k, int di, int dj) const { return off[k] + (double)V->at(k, i + di, j + dj); }
+  __device__ double p(int di, int dj) const { return off[5] + (double)V->at(5, i + di, j + dj); }
+  __device__ double t(int di, int dj) const { return off[6] + (double)V->at(6, i + di, j + dj); }
 };
+// Perturbations of rho and p as the stage kernel's FP32 tile holds them;
+// d0 = off[0] - rho0 and d5 = off[5] - p0 are exactly 0 for perturbation
+// storage and -rho0, -p0 for absolute storage.
+template <typename S>
 struct CanvasAcc32 {
-  const CanvasView* V;
+  const CanvasT<S>* V;
   int i, j;
-  double rho0, p0;
-  __device__ float w(int k, int di, int dj) const { return (float)(V->at(k, i + di, j + dj) - (k == 0 ? rho0 : 0.0)); }
-  __device__ float p(int di, int dj) const { return (float)(V->at(5, i + di, j + dj) - p0); }
+  double d0, d5;
+  __device__ float w(int k, int di, int dj) const {
+    return (float)((double)V->at(k, i + di, j + dj) + (k == 0 ? d0 : 0.0));
+  }
+  __device__ float p(int di, int dj) const { return (float)((double)V->at(5, i + di, j + dj) + d5); }
 };
 
-__global__ void harvest_kernel(HarvestArgs A) {
+template <typename S>
+__global__ void harvest_kernel(HarvestArgs<S> A) {
   for (int t = blockIdx.x; t < A.cnt; t += gridDim.x) {
     int4 td = A.tiles[A.off + t];
     int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx >= w || ty >= h) continue;
     int i = td.x + tx, j = td.y + ty;
-    CanvasAcc64 a64{&A.V, i, j};
+    CanvasAcc64<S> a64{&A.V, A.amb_off, i, j};
     int flag = rhs_switch<kHybrid, 5, true>(a64, A.P);
     if (!flag) {
       unsigned hsh = (unsigned)i * 73856093u ^ (unsigned)j * 19349663u ^ A.seed * 83492791u;
@@ -907,7 +1205,7 @@ __global__ void harvest_kernel(HarvestArgs A) {
       if (hsh > A.keep0) continue;
     }
     double H[5], Kd[5], Kw[5];
-    H[0] = A.H.at(0, i, j);
+    H[0] = (double)A.H.at(0, i, j);
     rhs_sources(a64, A.P, H);
     double H2[5] = {H[0], H[1], H[2], H[3], H[4]};
     rhs_fluxes<kHybrid, 5, true>(a64, A.P, j, 0, H, Kd);
@@ -917,7 +1215,7 @@ __global__ void harvest_kernel(HarvestArgs A) {
     for (int k = 0; k < 5; ++k) err = fmax(err, A.dt * fabs(Kd[k] - Kw[k]) * A.inv_scale[k]);
     unsigned long long idx = atomicAdd(A.count, 1ull);
     if ((long)idx >= A.cap) continue;
-    CanvasAcc32 a32{&A.V, i, j, (double)A.rho0, (double)A.p0};
+    CanvasAcc32<S> a32{&A.V, i, j, A.amb_off[0] - A.rho0_d, A.amb_off[5] - A.p0_d};
     float fv[kFeat];
     cell_features(a32, A.eps, A.eps_p, A.inv_sqrt_eps, fv);
     for (int q = 0; q < kFeat; ++q) A.X[(long)idx * kFeat + q] = __float2bfloat16_rn(fv[q]);
@@ -936,16 +1234,19 @@ int launch_rhs_pitched(int variant, const double* w, const double* pres, const d
 struct Level {
   int nx = 0, ny = 0;
   long pitch = 0, fstride = 0;
-  double* buf[3] = {nullptr, nullptr, nullptr};
-  double* h0 = nullptr;
-  double* kk = nullptr;
+  void* buf[3] = {nullptr, nullptr, nullptr};  // storage type of the engine
+  void* h0 = nullptr;
+  double* kk = nullptr;                        // plain path (FP64 storage only)
   double dx[2] = {0, 0};
   std::vector<int4> patches;
   CUtensorMap tmap[3];
-  CanvasView view(int which) const {
-    double* b = which < 3 ? buf[which] : h0;
-    return CanvasView{b, pitch, fstride, nx, ny};
+  CUtensorMap tmap_un, tmap_h0;  // FP32 storage: interior boxes of u^n and H0
+  template <typename S>
+  CanvasT<S> view(int which) const {
+    void* b = which < 3 ? buf[which] : h0;
+    return CanvasT<S>{static_cast<S*>(b), pitch, fstride, nx, ny};
   }
+  double* buf64(int which) const { return static_cast<double*>(buf[which]); }
 };
 
 // meta layout (device ints)
@@ -955,7 +1256,8 @@ enum {
   M_HALO_CNT = 1 + kL,
   M_CT_OFF = 1 + 2 * kL,
   M_CT_CNT = 1 + 3 * kL,
-  M_SIZE = 1 + 4 * kL
+  M_PATCH_OFF = 1 + 4 * kL,  // kL + 1 entries: first patch-table index of each level, then the total
+  M_SIZE = 2 + 5 * kL
 };
 
 template <typename T>
@@ -1008,12 +1310,27 @@ struct Engine {
   long long prof_launches = 0, prof_cells = 0;
   DevArray<long long> d_tileoff;
   std::vector<long long> h_tileoff;
-  double* d_packed = nullptr;
-  size_t packed_cap = 0;
+  void* d_packed = nullptr;
+  size_t packed_cap = 0;  // bytes
   unsigned long long* d_smax = nullptr;
+  // virtual microphones
+  int nmics = 0;
+  double* d_mics = nullptr;
+  int* d_mic_it = nullptr;
+  MicRecord* d_mic_rec = nullptr;
+  unsigned long long* d_mic_count = nullptr;
+  long long mic_cap = 0;
   int nsm = 148;
   int stage_blocks = 0;
   size_t smem_bytes = 0;
+  // storage: FP64 absolute values, or FP32 perturbations about the ambient
+  // state (absolute = off[k] + stored)
+  bool f32s = false;
+  size_t esize = 8;
+  double* d_env[kL][4] = {};  // absorbing-envelope tables (null: side not ABSORB)
+  float* d_envf[kL][4] = {};
+  unsigned char* d_cont[kL][4] = {};
+  double off[kNF] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -1029,14 +1346,21 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-static int make_tmap(CUtensorMap* m, double* base, long pitch, long fstride, int nyc) {
+// Halo-box tensor map of one canvas: a (38 or 40) x 14 x 7 box of doubles
+// (rows of kBW) or floats (rows of kBW32, so that a row spans 160 bytes).
+// Any other box: `fields` planes of the canvas, a box_w x box_h x box_f box.
+static int make_tmap(CUtensorMap* m, void* base, long pitch, long fstride, int nyc, bool f32, int fields = kNF,
+                     int box_w = 0, int box_h = kBH, int box_f = kNF) {
   auto fn = encode_fn();
   if (!fn) return ENL_ERR_CUDA;
-  cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)nyc, (cuuint64_t)kNF};
-  cuuint64_t strides[2] = {(cuuint64_t)(pitch * 8), (cuuint64_t)(fstride * 8)};
-  cuuint32_t box[3] = {(cuuint32_t)kBW, (cuuint32_t)kBH, (cuuint32_t)kNF};
+  const cuuint64_t es = f32 ? 4 : 8;
+  if (box_w == 0) box_w = f32 ? kBW32 : kBW;
+  cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)nyc, (cuuint64_t)fields};
+  cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)(fstride * es)};
+  cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, (cuuint32_t)box_f};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box, estr,
+  CUresult r = fn(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims,
+                  strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? ENL_OK : ENL_ERR_CUDA;
@@ -1100,9 +1424,9 @@ static int rebuild_tables(Engine* E) {
   for (int l = 0; l < nl; ++l) {
     E->tile_off[l] = (int)E->h_tiles.size();
     E->patch_off[l] = (int)E->h_patchtab.size();
-    int pid = 0;
     for (auto& b : E->lev[l].patches) {
-      tiles_of_box(b, l, pid++, E->h_tiles);
+      // tile .w = index of the patch in the all-level patch table
+      tiles_of_box(b, l, (int)E->h_patchtab.size(), E->h_tiles);
       E->h_patchtab.push_back(b);
     }
     E->tile_cnt[l] = (int)E->h_tiles.size() - E->tile_off[l];
@@ -1121,6 +1445,8 @@ static int rebuild_tables(Engine* E) {
     E->h_meta[M_CT_CNT + l] = (int)E->h_ctiles.size() - E->h_meta[M_CT_OFF + l];
   }
   E->h_meta[M_NTILES] = (int)E->h_tiles.size();
+  for (int l = 0; l < kL; ++l) E->h_meta[M_PATCH_OFF + l] = l < nl ? E->patch_off[l] : (int)E->h_patchtab.size();
+  E->h_meta[M_PATCH_OFF + kL] = (int)E->h_patchtab.size();
   E->h_tileoff.resize(E->h_tiles.size());
   long long acc = 0;
   for (size_t q = 0; q < E->h_tiles.size(); ++q) {
@@ -1155,6 +1481,9 @@ static int rebuild_tables(Engine* E) {
   return check_launch("engine tables");
 }
 
+static bool any_absorb(const Engine* E);
+static AbsorbTables absorb_tables(const Engine* E);
+
 static StageArgs stage_args(Engine* E, int stage, double dt) {
   StageArgs A;
   memset(&A, 0, sizeof(A));
@@ -1164,6 +1493,8 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   for (int l = 0; l < c.nlevels; ++l) {
     Level& L = E->lev[l];
     A.tmap[l] = L.tmap[in];
+    A.tmap_un[l] = L.tmap_un;
+    A.tmap_h0[l] = L.tmap_h0;
     A.in[l] = L.buf[in];
     A.out[l] = L.buf[out];
     A.un[l] = L.buf[0];
@@ -1196,6 +1527,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
     F.sensor_eps = (float)P.sensor_eps;
     F.rho0 = (float)c.rho0;
     F.T0 = (float)c.T0;
+    F.rho0T0 = F.rho0 * F.T0;
     F.level = l;
     A.F[l] = F;
     A.dy[l] = L.dx[1];
@@ -1210,17 +1542,26 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.c_v = c.c_v;
   A.R = c.R;
   A.ylo = c.xlo[1];
+  A.un_is_in = in == 0 ? 1 : 0;
   A.a1 = c.rk_alpha1[stage];
   A.a2 = c.rk_alpha2[stage];
   A.bdt = c.rk_beta[stage] * dt;
   A.beta = c.rk_beta[stage];
+  A.gm1_over_2rho0_f = (float)A.gm1_over_2rho0;
+  A.inv_c_p_f = (float)(1.0 / c.c_p);
+  A.inv_c_v_f = (float)(1.0 / c.c_v);
+  A.R_f = (float)c.R;
+  A.inv_rho0_f = (float)(1.0 / c.rho0);
   A.dt_dev = E->adaptive ? E->d_dt : nullptr;
+  A.absorb = absorb_tables(E);
+  A.any_absorb = any_absorb(E);
+  A.patchtab = E->d_patchtab.p;
   A.tiles = E->d_tiles.p;
   A.ntiles = E->d_meta + M_NTILES;
   A.counter = E->d_counters + stage;
   A.health = E->d_health;
   A.stats = E->d_stats;
-  A.mlp = (E->cfg.learned && E->cfg.precision == ENL_PREC_FP32) ? E->d_mlp : nullptr;
+  A.mlp = (E->cfg.learned && E->cfg.precision != ENL_PREC_FP64) ? E->d_mlp : nullptr;
   A.margin = E->margin;
   A.feat_eps = (float)A.P[0].sensor_eps;
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
@@ -1230,74 +1571,135 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
 
 typedef void (*StageFn)(StageArgs);
 
-template <bool FAST>
-static StageFn pick_stage(int variant) {
+template <bool FAST, typename S>
+static StageFn pick_stage_t(int variant) {
   switch (variant) {
-    case 0: return stage_kernel<kHybrid, 5, true, FAST>;
-    case 1: return stage_kernel<kHybrid, 5, false, FAST>;
-    case 2: return stage_kernel<kHybrid, 3, true, FAST>;
-    case 3: return stage_kernel<kHybrid, 3, false, FAST>;
-    case 4: return stage_kernel<kWeno, 5, true, FAST>;
-    case 5: return stage_kernel<kWeno, 5, false, FAST>;
-    case 6: return stage_kernel<kWeno, 3, true, FAST>;
-    case 7: return stage_kernel<kWeno, 3, false, FAST>;
-    default: return stage_kernel<kDrp, 5, false, FAST>;
+    case 0: return stage_kernel<kHybrid, 5, true, FAST, S>;
+    case 1: return stage_kernel<kHybrid, 5, false, FAST, S>;
+    case 2: return stage_kernel<kHybrid, 3, true, FAST, S>;
+    case 3: return stage_kernel<kHybrid, 3, false, FAST, S>;
+    case 4: return stage_kernel<kWeno, 5, true, FAST, S>;
+    case 5: return stage_kernel<kWeno, 5, false, FAST, S>;
+    case 6: return stage_kernel<kWeno, 3, true, FAST, S>;
+    case 7: return stage_kernel<kWeno, 3, false, FAST, S>;
+    default: return stage_kernel<kDrp, 5, false, FAST, S>;
   }
 }
 
+static StageFn pick_stage(int precision, int variant) {
+  if (precision == ENL_PREC_FP32_STATE) return pick_stage_t<true, float>(variant);
+  if (precision == ENL_PREC_FP32) return pick_stage_t<true, double>(variant);
+  return pick_stage_t<false, double>(variant);
+}
+
+template <typename S>
 static int fill_level(Engine* E, int l, int which) {
   cudaStream_t s = stream();
   const auto& c = E->cfg;
   Level& L = E->lev[l];
   if (l > 0) {
-    interp_kernel<<<E->nsm * 4, 256, 0, s>>>(L.view(which), E->lev[l - 1].view(which), c.ratio, E->d_halo.p,
-                                             E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l, kNF);
+    interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(which), c.ratio,
+                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l, kNF);
   }
   if (c.independent) {
     if (E->patch_cnt[l])
-      physbc_patches_kernel<<<E->patch_cnt[l], 256, 0, s>>>(L.view(which), E->d_patchtab.p, E->patch_off[l],
-                                                            E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+      physbc_patches_kernel<S><<<E->patch_cnt[l], 256, 0, s>>>(L.view<S>(which), E->d_patchtab.p, E->patch_off[l],
+                                                               E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
   } else {
-    physbc_kernel<<<E->nsm * 2, 256, 0, s>>>(L.view(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+    physbc_kernel<S><<<E->nsm * 2, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
   }
   return ENL_OK;
 }
 
 static int fill_all(Engine* E, int which) {
-  for (int l = 0; l < E->cfg.nlevels; ++l) fill_level(E, l, which);
+  for (int l = 0; l < E->cfg.nlevels; ++l) {
+    if (E->f32s) fill_level<float>(E, l, which);
+    else fill_level<double>(E, l, which);
+  }
   return check_launch("fill");
 }
 
-static int absorb_all(Engine* E, int which) {
+static bool any_absorb(const Engine* E) {
   const auto& c = E->cfg;
-  if (!(c.bc[0] == kAbsorb || c.bc[1] == kAbsorb || c.bc[2] == kAbsorb || c.bc[3] == kAbsorb)) return ENL_OK;
-  cudaStream_t s = stream();
+  return c.bc[0] == kAbsorb || c.bc[1] == kAbsorb || c.bc[2] == kAbsorb || c.bc[3] == kAbsorb;
+}
+
+static AbsorbTables absorb_tables(const Engine* E) {
+  AbsorbTables T;
+  for (int l = 0; l < kL; ++l)
+    for (int d = 0; d < 4; ++d) {
+      T.env[l][d] = E->d_env[l][d];
+      T.envf[l][d] = E->d_envf[l][d];
+      T.cont[l][d] = E->d_cont[l][d];
+    }
+  return T;
+}
+
+// Envelope tables of every level, host-computed with the reference's formula
+// 1 - exp(-ln2 / w^2 * d^2) and the level's cell centres.
+static int build_absorb_tables(Engine* E) {
+  const auto& c = E->cfg;
+  const double W2 = c.absorb_width * c.absorb_width;
   for (int l = 0; l < c.nlevels; ++l) {
     Level& L = E->lev[l];
-    if (E->patch_cnt[l] == 0) continue;
-    AbsorbArgs A{L.dx[0], L.dx[1], c.xlo[0], c.xlo[1], c.xlo[0] + L.dx[0] * L.nx, c.xlo[1] + L.dx[1] * L.ny,
-                 c.absorb_width * c.absorb_width, c.p0, c.T0, c.rho0};
-    long rows = 0, cols = 0;
-    for (int q = 0; q < E->patch_cnt[l]; ++q) {
-      int4 b = E->h_patchtab[E->patch_off[l] + q];
-      rows += b.w - b.z + 1;
-      cols += b.y - b.x + 1;
-    }
-    for (int dir = 0; dir < 4; ++dir) {
-      if (c.bc[dir] != kAbsorb) continue;
-      long n = dir < 2 ? rows : cols;
-      absorb_patches_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(L.view(which), E->d_patchtab.p,
-                                                                       E->patch_off[l], E->patch_cnt[l], dir, A);
+    const int n[4] = {L.nx, L.nx, L.ny, L.ny};
+    for (int d = 0; d < 4; ++d) {
+      if (c.bc[d] != kAbsorb) continue;
+      std::vector<double> h(n[d]);
+      const int ax = d < 2 ? 0 : 1;
+      const double lo = c.xlo[ax], hi = c.xlo[ax] + L.dx[ax] * (ax == 0 ? L.nx : L.ny);
+      for (int q = 0; q < n[d]; ++q) {
+        const double xc = lo + L.dx[ax] * ((double)q + 0.5);
+        const double dist = (d == 0 || d == 2) ? (xc - lo) : (hi - xc);
+        h[q] = -std::exp(-std::log(2.0) / W2 * (dist * dist)) + 1.0;
+      }
+      std::vector<float> hf(n[d]);
+      std::vector<unsigned char> hc(n[d]);
+      for (int q = 0; q < n[d]; ++q) {
+        hf[q] = (float)h[q];
+        hc[q] = std::fabs(1.0 - h[q]) > 1.0e-8 ? 1 : 0;  // the reference's loop test
+      }
+      if (cudaMalloc(&E->d_env[l][d], n[d] * sizeof(double)) != cudaSuccess ||
+          cudaMalloc(&E->d_envf[l][d], n[d] * sizeof(float)) != cudaSuccess ||
+          cudaMalloc(&E->d_cont[l][d], n[d]) != cudaSuccess)
+        return ENL_ERR_CUDA;
+      cudaMemcpy(E->d_env[l][d], h.data(), n[d] * sizeof(double), cudaMemcpyHostToDevice);
+      cudaMemcpy(E->d_envf[l][d], hf.data(), n[d] * sizeof(float), cudaMemcpyHostToDevice);
+      cudaMemcpy(E->d_cont[l][d], hc.data(), n[d], cudaMemcpyHostToDevice);
     }
   }
+  return ENL_OK;
+}
+
+// Plain path only (FP64 storage); the fused path applies the envelope in the
+// stage kernel.
+static int absorb_all(Engine* E, int which) {
+  if (!any_absorb(E) || E->h_tiles.empty()) return ENL_OK;
+  const auto& c = E->cfg;
+  AbsorbTileArgs A;
+  memset(&A, 0, sizeof(A));
+  A.T = absorb_tables(E);
+  for (int l = 0; l < c.nlevels; ++l) A.lev[l] = E->lev[l].view<double>(which);
+  A.tiles = E->d_tiles.p;
+  A.patchtab = E->d_patchtab.p;
+  A.ntiles = (int)E->h_tiles.size();
+  A.p0 = c.p0;
+  A.T0 = c.T0;
+  A.rho0 = c.rho0;
+  absorb_tiles_kernel<<<std::min(A.ntiles, E->nsm * 16), 256, 0, stream()>>>(A);
   return check_launch("absorb");
 }
 
-static int coarsen_all(Engine* E) {
-  cudaStream_t s = stream();
+template <typename S>
+static void coarsen_all_t(Engine* E) {
   for (int l = E->cfg.nlevels - 1; l > 0; --l)
-    coarsen_kernel<<<E->nsm * 4, 256, 0, s>>>(E->lev[l - 1].view(0), E->lev[l].view(0), E->cfg.ratio, E->d_ctiles.p,
-                                             E->d_meta, M_CT_OFF + l, M_CT_CNT + l);
+    coarsen_kernel<S><<<E->nsm * 4, 256, 0, stream()>>>(E->lev[l - 1].view<S>(0), E->lev[l].view<S>(0), E->cfg.ratio,
+                                                       E->d_ctiles.p, E->d_meta, M_CT_OFF + l, M_CT_CNT + l);
+}
+
+static int coarsen_all(Engine* E) {
+  if (E->f32s) coarsen_all_t<float>(E);
+  else coarsen_all_t<double>(E);
   return check_launch("coarsen");
 }
 
@@ -1306,24 +1708,63 @@ static double finest_dx(Engine* E) {
   return L.dx[0] < L.dx[1] ? L.dx[0] : L.dx[1];
 }
 
+template <typename S>
+static void speed_t(Engine* E) {
+  SpeedArgs<S> A;
+  memset(&A, 0, sizeof(A));
+  for (int l = 0; l < E->cfg.nlevels; ++l) A.lev[l] = E->lev[l].view<S>(0);
+  A.tiles = E->d_tiles.p;
+  A.ntiles = E->d_meta + M_NTILES;
+  A.c = E->cfg.c;
+  A.rho_off = E->off[0];
+  A.smax_bits = E->d_smax;
+  speed_kernel<S><<<E->nsm * 4, 256, 0, stream()>>>(A);
+}
+
 static void adaptive_dt(Engine* E, double dt_max) {
   if (!E->adaptive) return;
-  SpeedArgs S;
-  memset(&S, 0, sizeof(S));
-  for (int l = 0; l < E->cfg.nlevels; ++l) S.lev[l] = E->lev[l].view(0);
-  S.tiles = E->d_tiles.p;
-  S.ntiles = E->d_meta + M_NTILES;
-  S.c = E->cfg.c;
-  S.smax_bits = E->d_smax;
-  speed_kernel<<<E->nsm * 4, 256, 0, stream()>>>(S);
+  if (E->f32s) speed_t<float>(E);
+  else speed_t<double>(E);
   dt_kernel<<<1, 1, 0, stream()>>>(E->d_smax, E->d_dt, E->d_dt + 1, E->cfl * finest_dx(E), dt_max);
+}
+
+template <typename S>
+static void mics_t(Engine* E) {
+  MicArgs<S> A;
+  memset(&A, 0, sizeof(A));
+  for (int l = 0; l < E->cfg.nlevels; ++l) {
+    A.lev[l] = E->lev[l].view<S>(0);
+    A.dx[l][0] = E->lev[l].dx[0];
+    A.dx[l][1] = E->lev[l].dx[1];
+  }
+  A.xlo0 = E->cfg.xlo[0];
+  A.xlo1 = E->cfg.xlo[1];
+  A.p_off = E->off[5];
+  A.patchtab = E->d_patchtab.p;
+  A.patch_first = E->d_meta + M_PATCH_OFF;
+  A.nmics = E->nmics;
+  A.mics = E->d_mics;
+  A.iteration = E->d_mic_it;
+  A.rec = E->d_mic_rec;
+  A.count = E->d_mic_count;
+  A.cap = E->mic_cap;
+  mic_kernel<S><<<E->nsm, 256, 0, stream()>>>(A);
+  mic_advance_kernel<<<1, 1, 0, stream()>>>(E->d_mic_it);
+}
+
+// Microphones sample the state a step leaves (after coarsening), as the
+// reference calls recordAudio after advanceHierarchy (main.C:482-486).
+static void record_mics(Engine* E) {
+  if (E->nmics <= 0) return;
+  if (E->f32s) mics_t<float>(E);
+  else mics_t<double>(E);
 }
 
 static int step_fused(Engine* E, double dt) {
   cudaStream_t s = stream();
   cudaMemsetAsync(E->d_counters, 0, 3 * sizeof(int), s);
   adaptive_dt(E, dt);
-  StageFn fn = E->cfg.precision == ENL_PREC_FP32 ? pick_stage<true>(E->cfg.variant) : pick_stage<false>(E->cfg.variant);
+  StageFn fn = pick_stage(E->cfg.precision, E->cfg.variant);
   for (int st = 0; st < 3; ++st) {
     int in = st == 0 ? 0 : st;
     int out = st == 2 ? 0 : st + 1;
@@ -1333,9 +1774,10 @@ static int step_fused(Engine* E, double dt) {
     if (E->profile) cudaEventRecord(E->pev[2 * st], s);
     cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
     if (E->profile) cudaEventRecord(E->pev[2 * st + 1], s);
-    absorb_all(E, out);
+    (void)out;
   }
   coarsen_all(E);
+  record_mics(E);
   if (E->profile) {
     cudaEventSynchronize(E->pev[5]);
     long long cells = 0;
@@ -1351,6 +1793,7 @@ static int step_fused(Engine* E, double dt) {
   return check_launch("engine step");
 }
 
+// Plain path: FP64 storage only (enl_engine_step_plain refuses FP32 storage).
 static int step_plain(Engine* E, double dt) {
   cudaStream_t s = stream();
   const auto& c = E->cfg;
@@ -1359,8 +1802,8 @@ static int step_plain(Engine* E, double dt) {
   // copy current -> scratch (patch interiors)
   for (int l = 0; l < nl; ++l)
     if (E->tile_cnt[l])
-      copy_tiles_kernel<<<E->tile_cnt[l], 256, 0, s>>>(E->lev[l].view(1), E->lev[l].view(0), E->d_tiles.p,
-                                                       E->tile_off[l], E->tile_cnt[l]);
+      copy_tiles_kernel<double><<<E->tile_cnt[l], 256, 0, s>>>(E->lev[l].view<double>(1), E->lev[l].view<double>(0),
+                                                               E->d_tiles.p, E->tile_off[l], E->tile_cnt[l]);
   for (int st = 0; st < 3; ++st) {
     fill_all(E, 1);
     // rhs of every patch first (each patch reads its neighbours' cells as
@@ -1378,8 +1821,9 @@ static int step_plain(Engine* E, double dt) {
         // patch; shift ylo to the patch's lower edge
         RhsConst Pp = P;
         Pp.ylo = c.xlo[1] + L.dx[1] * (double)b.z;
-        launch_rhs_pitched(c.variant, L.buf[1] + g0, L.buf[1] + 5 * L.fstride + g0, L.buf[1] + 6 * L.fstride + g0,
-                           L.pitch, L.fstride, L.h0 + c0, L.kk + c0, L.pitch, L.fstride, nx, ny, Pp);
+        const double* b1 = L.buf64(1);
+        launch_rhs_pitched(c.variant, b1 + g0, b1 + 5 * L.fstride + g0, b1 + 6 * L.fstride + g0, L.pitch, L.fstride,
+                           static_cast<const double*>(L.h0) + c0, L.kk + c0, L.pitch, L.fstride, nx, ny, Pp);
       }
     }
     for (int l = 0; l < nl; ++l) {
@@ -1390,19 +1834,20 @@ static int step_plain(Engine* E, double dt) {
       for (auto& b : L.patches) {
         int nx = b.y - b.x + 1, ny = b.w - b.z + 1;
         dim3 blk(32, 4), grd((nx + 31) / 32, (ny + 3) / 4);
-        rk_plain_kernel<<<grd, blk, 0, s>>>(L.view(1), L.view(0), K, b.x, b.z, nx, ny, c.rk_alpha1[st],
-                                            c.rk_alpha2[st], c.rk_beta[st] * dt, c.rk_beta[st],
+        rk_plain_kernel<<<grd, blk, 0, s>>>(L.view<double>(1), L.view<double>(0), K, b.x, b.z, nx, ny,
+                                            c.rk_alpha1[st], c.rk_alpha2[st], c.rk_beta[st] * dt, c.rk_beta[st],
                                             E->adaptive ? E->d_dt : nullptr);
-        eos_plain_kernel<<<grd, blk, 0, s>>>(L.view(1), b.x, b.z, nx, ny, Ea);
+        eos_plain_kernel<<<grd, blk, 0, s>>>(L.view<double>(1), b.x, b.z, nx, ny, Ea);
       }
     }
     absorb_all(E, 1);
   }
   for (int l = 0; l < nl; ++l)
     if (E->tile_cnt[l])
-      copy_tiles_kernel<<<E->tile_cnt[l], 256, 0, s>>>(E->lev[l].view(0), E->lev[l].view(1), E->d_tiles.p,
-                                                       E->tile_off[l], E->tile_cnt[l]);
+      copy_tiles_kernel<double><<<E->tile_cnt[l], 256, 0, s>>>(E->lev[l].view<double>(0), E->lev[l].view<double>(1),
+                                                               E->d_tiles.p, E->tile_off[l], E->tile_cnt[l]);
   coarsen_all(E);
+  record_mics(E);
   return check_launch("engine plain step");
 }
 
@@ -1410,11 +1855,47 @@ static int step_plain(Engine* E, double dt) {
 
 using namespace enl;
 
+template <typename S>
+static int harvest_t(Engine* E, int level, double dt, const double* scale, double keep0, unsigned seed, void* X,
+                     float* labels, long capacity, unsigned long long* count_dev) {
+  const auto& c = E->cfg;
+  Level& L = E->lev[level];
+  HarvestArgs<S> A;
+  memset(&A, 0, sizeof(A));
+  A.V = L.view<S>(0);
+  A.H = L.view<S>(3);
+  for (int k = 0; k < kNF; ++k) A.amb_off[k] = E->off[k];
+  double xlo[2] = {c.xlo[0], c.xlo[1]};
+  A.P = make_rhs_const(xlo, L.dx, c.weno_alpha, c.kappa, c.mu, c.muB, c.R, c.T_star_n, c.tau_n, c.tol, 0, c.c,
+                       c.c_lr);
+  A.eps = (float)A.P.sensor_eps;
+  A.eps_p = (float)(A.P.sensor_eps * (c.c * c.c) * (c.c * c.c));
+  A.inv_sqrt_eps = (float)(1.0 / sqrt(A.P.sensor_eps));
+  A.rho0 = (float)c.rho0;
+  A.p0 = (float)c.p0;
+  A.rho0_d = c.rho0;
+  A.p0_d = c.p0;
+  A.T0 = (float)c.T0;
+  A.tiles = E->d_tiles.p;
+  A.off = E->tile_off[level];
+  A.cnt = E->tile_cnt[level];
+  A.dt = dt;
+  for (int k = 0; k < 5; ++k) A.inv_scale[k] = 1.0 / scale[k];
+  A.keep0 = (unsigned)(std::min(1.0, std::max(0.0, keep0)) * 4294967295.0);
+  A.seed = seed;
+  A.X = (__nv_bfloat16*)X;
+  A.lab = labels;
+  A.count = count_dev;
+  A.cap = capacity;
+  if (A.cnt) harvest_kernel<S><<<std::min(A.cnt, E->nsm * 16), 256, 0, stream()>>>(A);
+  return check_launch("harvest");
+}
+
 extern "C" {
 
 int enl_engine_create(const enl_engine_config* cfg, void** out) {
   if (!cfg || !out || cfg->nlevels < 1 || cfg->nlevels > kL || cfg->ratio < 2 || cfg->nx0 < 8 || cfg->ny0 < 8 ||
-      cfg->variant < 0 || cfg->variant > 8 ||
+      cfg->variant < 0 || cfg->variant > 8 || cfg->precision < ENL_PREC_FP64 || cfg->precision > ENL_PREC_FP32_STATE ||
       (cfg->independent && (cfg->nlevels != 1 || cfg->bc[0] == kAbsorb || cfg->bc[1] == kAbsorb ||
                             cfg->bc[2] == kAbsorb || cfg->bc[3] == kAbsorb))) {
     set_error(ENL_ERR_ARG);
@@ -1422,6 +1903,14 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   }
   Engine* E = new Engine();
   E->cfg = *cfg;
+  E->f32s = cfg->precision == ENL_PREC_FP32_STATE;
+  E->esize = E->f32s ? sizeof(float) : sizeof(double);
+  if (E->f32s) {
+    E->off[0] = cfg->rho0;
+    E->off[4] = cfg->rho0 * cfg->T0;
+    E->off[5] = cfg->p0;
+    E->off[6] = cfg->T0;
+  }
   cudaDeviceGetAttribute(&E->nsm, cudaDevAttrMultiProcessorCount, 0);
   int rr = 1;
   for (int l = 0; l < cfg->nlevels; ++l) {
@@ -1433,7 +1922,7 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
     L.pitch = ((L.nx + 6 + 15) / 16) * 16;
     long rows = L.ny + 6;
     L.fstride = ((L.pitch * rows + 31) / 32) * 32;
-    size_t bytes = (size_t)L.fstride * kNF * sizeof(double);
+    size_t bytes = (size_t)L.fstride * kNF * E->esize;
     for (int b = 0; b < 3; ++b) {
       if (cudaMalloc(&L.buf[b], bytes) != cudaSuccess) {
         set_error(ENL_ERR_CUDA);
@@ -1441,15 +1930,26 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
         return ENL_ERR_CUDA;
       }
       cudaMemset(L.buf[b], 0, bytes);
-      if (make_tmap(&L.tmap[b], L.buf[b], L.pitch, L.fstride, (int)rows) != ENL_OK) {
+      if (make_tmap(&L.tmap[b], L.buf[b], L.pitch, L.fstride, (int)rows, E->f32s) != ENL_OK) {
         set_error(ENL_ERR_CUDA);
         enl_engine_destroy(E);
         return ENL_ERR_CUDA;
       }
     }
-    cudaMalloc(&L.h0, (size_t)L.fstride * sizeof(double));
-    cudaMemset(L.h0, 0, (size_t)L.fstride * sizeof(double));
+    cudaMalloc(&L.h0, (size_t)L.fstride * E->esize);
+    cudaMemset(L.h0, 0, (size_t)L.fstride * E->esize);
+    if (E->f32s && (make_tmap(&L.tmap_un, L.buf[0], L.pitch, L.fstride, (int)rows, true, kNF, kBW32, kTH, 5) != ENL_OK ||
+                    make_tmap(&L.tmap_h0, L.h0, L.pitch, L.fstride, (int)rows, true, 1, kBW32, kTH, 1) != ENL_OK)) {
+      set_error(ENL_ERR_CUDA);
+      enl_engine_destroy(E);
+      return ENL_ERR_CUDA;
+    }
     rr *= cfg->ratio;
+  }
+  if (any_absorb(E) && build_absorb_tables(E) != ENL_OK) {
+    set_error(ENL_ERR_CUDA);
+    enl_engine_destroy(E);
+    return ENL_ERR_CUDA;
   }
   cudaMalloc(&E->d_meta, sizeof(E->h_meta));
   cudaMemset(E->d_meta, 0, sizeof(E->h_meta));
@@ -1462,10 +1962,11 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMemset(E->d_dt, 0, 2 * sizeof(double));
   cudaMalloc(&E->d_smax, sizeof(unsigned long long));
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
-  E->smem_bytes = 2 * kStageBufBytes + (cfg->precision == ENL_PREC_FP32 ? kTile32Bytes : 0);
-  if (cfg->precision == ENL_PREC_FP32 && cfg->learned)
+  if (E->f32s) E->smem_bytes = kOffMlpS;
+  else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kOffMlp : 2 * kStageBufBytes;
+  if (cfg->precision != ENL_PREC_FP64 && cfg->learned)
     E->smem_bytes += align128((int)sizeof(MlpSmem)) + 256 * kFeat * sizeof(__nv_bfloat16);
-  StageFn fn = cfg->precision == ENL_PREC_FP32 ? pick_stage<true>(cfg->variant) : pick_stage<false>(cfg->variant);
+  StageFn fn = pick_stage(cfg->precision, cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, 256, E->smem_bytes);
@@ -1491,6 +1992,13 @@ int enl_engine_destroy(void* e) {
     if (E->lev[l].h0) cudaFree(E->lev[l].h0);
     if (E->lev[l].kk) cudaFree(E->lev[l].kk);
   }
+  for (int l = 0; l < kL; ++l)
+    for (int d = 0; d < 4; ++d)
+    {
+      if (E->d_env[l][d]) cudaFree(E->d_env[l][d]);
+      if (E->d_envf[l][d]) cudaFree(E->d_envf[l][d]);
+      if (E->d_cont[l][d]) cudaFree(E->d_cont[l][d]);
+    }
   if (E->d_meta) cudaFree(E->d_meta);
   if (E->d_counters) cudaFree(E->d_counters);
   if (E->d_health) cudaFree(E->d_health);
@@ -1504,13 +2012,17 @@ int enl_engine_destroy(void* e) {
   for (int q = 0; q < 6; ++q)
     if (E->pev[q]) cudaEventDestroy(E->pev[q]);
   if (E->d_smax) cudaFree(E->d_smax);
+  if (E->d_mics) cudaFree(E->d_mics);
+  if (E->d_mic_it) cudaFree(E->d_mic_it);
+  if (E->d_mic_rec) cudaFree(E->d_mic_rec);
+  if (E->d_mic_count) cudaFree(E->d_mic_count);
   if (E->d_segs) cudaFree(E->d_segs);
   if (E->graph) cudaGraphExecDestroy(E->graph);
   delete E;
   return ENL_OK;
 }
 
-int enl_engine_buffer(void* e, int level, int which, double** base, long* pitch, long* fstride, int* nx, int* ny) {
+int enl_engine_buffer(void* e, int level, int which, void** base, long* pitch, long* fstride, int* nx, int* ny) {
   Engine* E = (Engine*)e;
   if (!E || level < 0 || level >= E->cfg.nlevels || which < 0 || which > 3) {
     set_error(ENL_ERR_ARG);
@@ -1535,7 +2047,9 @@ int enl_engine_set_patches(void* e, int level, int npatch, const int* boxes) {
   std::vector<int4> P;
   for (int q = 0; q < npatch; ++q) {
     int4 b = make_int4(boxes[4 * q], boxes[4 * q + 1], boxes[4 * q + 2], boxes[4 * q + 3]);
-    if (b.x < 0 || b.z < 0 || b.y >= L.nx || b.w >= L.ny || b.y < b.x || b.w < b.z || (b.x & 1)) {
+    // tile origins feed TMA x coordinates: 16-byte aligned rows of the box
+    const int xmask = E->f32s ? 3 : 1;
+    if (b.x < 0 || b.z < 0 || b.y >= L.nx || b.w >= L.ny || b.y < b.x || b.w < b.z || (b.x & xmask)) {
       set_error(ENL_ERR_ARG);
       return ENL_ERR_ARG;
     }
@@ -1560,8 +2074,13 @@ int enl_engine_refine_init(void* e, int level, int nbox, const int* boxes) {
       return ENL_ERR_ARG;
     }
     long n = (long)(ihi - ilo + 1) * (jhi - jlo + 1);
-    refine_box_kernel<<<(unsigned)std::min<long>((n + 255) / 256, 4096), 256, 0, s>>>(
-        L.view(0), E->lev[level - 1].view(0), E->cfg.ratio, ilo, jlo, ihi - ilo + 1, jhi - jlo + 1);
+    const unsigned g = (unsigned)std::min<long>((n + 255) / 256, 4096);
+    if (E->f32s)
+      refine_box_kernel<float><<<g, 256, 0, s>>>(L.view<float>(0), E->lev[level - 1].view<float>(0), E->cfg.ratio,
+                                                 ilo, jlo, ihi - ilo + 1, jhi - jlo + 1);
+    else
+      refine_box_kernel<double><<<g, 256, 0, s>>>(L.view<double>(0), E->lev[level - 1].view<double>(0),
+                                                   E->cfg.ratio, ilo, jlo, ihi - ilo + 1, jhi - jlo + 1);
   }
   return check_launch("refine_init");
 }
@@ -1588,7 +2107,7 @@ int enl_engine_step(void* e, double dt) {
 int enl_engine_step_plain(void* e, double dt) {
   Engine* E = (Engine*)e;
   if (!E) return ENL_ERR_ARG;
-  if (E->h_tiles.empty()) {
+  if (E->h_tiles.empty() || E->f32s) {
     set_error(ENL_ERR_STATE);
     return ENL_ERR_STATE;
   }
@@ -1638,6 +2157,12 @@ int enl_engine_graph_capture(void* e, double dt) {
   return ENL_OK;
 }
 
+int enl_engine_graph_valid(void* e) {
+  Engine* E = (Engine*)e;
+  if (!E) return 0;
+  return (E->graph && E->graph_valid) ? 1 : 0;
+}
+
 int enl_engine_graph_replay(void* e, int nsteps) {
   Engine* E = (Engine*)e;
   if (!E || !E->graph || !E->graph_valid) {
@@ -1663,15 +2188,26 @@ int enl_engine_tag(void* e, int level, int* tags) {
   Level& L = E->lev[level];
   fill_all(E, 0);
   // source ghosts: the same physical rule on the H0 canvas (one field)
-  physbc_kernel<<<E->nsm, 256, 0, s>>>(L.view(3), 1, E->cfg.bc[0], E->cfg.bc[1], E->cfg.bc[2], E->cfg.bc[3]);
+  if (E->f32s)
+    physbc_kernel<float><<<E->nsm, 256, 0, s>>>(L.view<float>(3), 1, E->cfg.bc[0], E->cfg.bc[1], E->cfg.bc[2],
+                                                E->cfg.bc[3]);
+  else
+    physbc_kernel<double><<<E->nsm, 256, 0, s>>>(L.view<double>(3), 1, E->cfg.bc[0], E->cfg.bc[1], E->cfg.bc[2],
+                                                 E->cfg.bc[3]);
   cudaMemsetAsync(tags, 0, (size_t)L.nx * L.ny * sizeof(int), s);
   const double xi = 1.0;
   const double* tol = E->cfg.tol;
   double ep0 = ((Lit::c0_9 * tol[0]) * (xi * xi)) / (1.0 - Lit::c0_9 * (tol[0] * tol[0]));
   double ep1 = ((Lit::c0_9 * tol[1]) * (xi * xi)) / (1.0 - Lit::c0_9 * (tol[1] * tol[1]));
   if (E->tile_cnt[level])
-    tag_tiles_kernel<<<E->tile_cnt[level], 256, 0, s>>>(tags, L.view(0), L.view(3), E->d_tiles.p, E->tile_off[level],
-                                                        E->tile_cnt[level], ep0, ep1);
+    if (E->f32s)
+      tag_tiles_kernel<float><<<E->tile_cnt[level], 256, 0, s>>>(tags, L.view<float>(0), L.view<float>(3),
+                                                                 E->d_tiles.p, E->tile_off[level],
+                                                                 E->tile_cnt[level], ep0, ep1);
+    else
+      tag_tiles_kernel<double><<<E->tile_cnt[level], 256, 0, s>>>(tags, L.view<double>(0), L.view<double>(3),
+                                                                  E->d_tiles.p, E->tile_off[level],
+                                                                  E->tile_cnt[level], ep0, ep1);
   return check_launch("engine tag");
 }
 
@@ -1702,17 +2238,16 @@ int enl_engine_launches_per_step(void* e, int plain) {
   const auto& c = E->cfg;
   int nl = c.nlevels;
   int fills = nl + (nl - 1);  // physbc per level + interp per fine level
-  int nabs = 0;
-  for (int d = 0; d < 4; ++d) nabs += c.bc[d] == kAbsorb;
-  int absorbs = 0;
-  for (int l = 0; l < nl; ++l) absorbs += E->patch_cnt[l] ? nabs : 0;
-  if (!plain) return 3 * (fills + 1 + absorbs) + (nl - 1);
+  const int dt = (E->adaptive ? 2 : 0) + (E->nmics > 0 ? 2 : 0);  // speed + dt update; microphones
+  // fused: the stage kernel applies the absorbing envelope itself
+  if (!plain) return 3 * (fills + 1) + (nl - 1) + dt;
+  const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;
   for (int l = 0; l < nl; ++l) {
     npatch += (int)E->lev[l].patches.size();
     copies += E->tile_cnt[l] ? 1 : 0;
   }
-  return 3 * (fills + 3 * npatch + absorbs) + 2 * copies + (nl - 1);
+  return 3 * (fills + 3 * npatch + absorbs) + 2 * copies + (nl - 1) + dt;
 }
 
 int enl_engine_paint_source(void* e, int level, int type, int mode, double amp, double spread, const double* pos,
@@ -1786,8 +2321,12 @@ int enl_engine_paint_source(void* e, int level, int type, int mode, double amp, 
     A.nseg = nseg;
   }
   if (E->tile_cnt[level])
-    paint_kernel<<<E->tile_cnt[level], 256, 0, s>>>(L.view(3), E->d_tiles.p, E->tile_off[level], E->tile_cnt[level],
-                                                    A);
+    if (E->f32s)
+      paint_kernel<float><<<E->tile_cnt[level], 256, 0, s>>>(L.view<float>(3), E->d_tiles.p, E->tile_off[level],
+                                                             E->tile_cnt[level], A);
+    else
+      paint_kernel<double><<<E->tile_cnt[level], 256, 0, s>>>(L.view<double>(3), E->d_tiles.p, E->tile_off[level],
+                                                              E->tile_cnt[level], A);
   return check_launch("paint_source");
 }
 
@@ -1799,10 +2338,18 @@ int enl_engine_state_from_overpressure(void* e, int level) {
   }
   const auto& c = E->cfg;
   Level& L = E->lev[level];
-  if (E->tile_cnt[level])
-    overpressure_state_kernel<<<E->tile_cnt[level], 256, 0, stream()>>>(
-        L.view(0), L.view(3), E->d_tiles.p, E->tile_off[level], E->tile_cnt[level], c.rho0, c.c,
-        (c.gamma1 - 1.0) / (2.0 * c.rho0), c.p0, c.T0, c.R, c.c_v);
+  if (E->tile_cnt[level]) {
+    const unsigned g = (unsigned)E->tile_cnt[level];
+    const double k = (c.gamma1 - 1.0) / (2.0 * c.rho0);
+    if (E->f32s)
+      overpressure_state_kernel<float><<<g, 256, 0, stream()>>>(
+          L.view<float>(0), L.view<float>(3), E->d_tiles.p, E->tile_off[level], E->tile_cnt[level], c.rho0, c.c, k,
+          c.p0, c.T0, c.R, c.c_v, E->off[0], E->off[4], E->off[5], E->off[6]);
+    else
+      overpressure_state_kernel<double><<<g, 256, 0, stream()>>>(
+          L.view<double>(0), L.view<double>(3), E->d_tiles.p, E->tile_off[level], E->tile_cnt[level], c.rho0, c.c,
+          k, c.p0, c.T0, c.R, c.c_v, 0.0, 0.0, 0.0, 0.0);
+  }
   return check_launch("state_from_overpressure");
 }
 
@@ -1845,6 +2392,61 @@ int enl_engine_tag_blocks(void* e, int level, int block, int buffer, unsigned ch
   return check_launch("tag_blocks");
 }
 
+int enl_engine_set_mics(void* e, int nmics, const double* xy, long long capacity, int iteration) {
+  Engine* E = (Engine*)e;
+  if (!E || nmics < 0 || (nmics > 0 && (!xy || capacity < 1))) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  if (E->d_mics) cudaFree(E->d_mics);
+  if (E->d_mic_rec) cudaFree(E->d_mic_rec);
+  E->d_mics = nullptr;
+  E->d_mic_rec = nullptr;
+  E->nmics = 0;
+  E->mic_cap = 0;
+  E->graph_valid = false;  // the step gains or loses the sampling launches
+  if (nmics == 0) return ENL_OK;
+  if (!E->d_mic_it && cudaMalloc(&E->d_mic_it, sizeof(int)) != cudaSuccess) E->d_mic_it = nullptr;
+  if (!E->d_mic_count && cudaMalloc(&E->d_mic_count, sizeof(unsigned long long)) != cudaSuccess)
+    E->d_mic_count = nullptr;
+  if (!E->d_mic_it || !E->d_mic_count || cudaMalloc(&E->d_mics, 2 * nmics * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&E->d_mic_rec, capacity * sizeof(MicRecord)) != cudaSuccess) {
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  cudaStream_t s = stream();
+  cudaMemcpyAsync(E->d_mics, xy, 2 * nmics * sizeof(double), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(E->d_mic_it, &iteration, sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(E->d_mic_count, 0, sizeof(unsigned long long), s);
+  cudaStreamSynchronize(s);
+  E->nmics = nmics;
+  E->mic_cap = capacity;
+  return check_launch("set_mics");
+}
+
+int enl_engine_mic_records(void* e, void* host, long long max, long long* n, long long* dropped) {
+  Engine* E = (Engine*)e;
+  if (!E || !n || max < 0 || (max > 0 && !host)) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  *n = 0;
+  if (dropped) *dropped = 0;
+  if (E->nmics <= 0) return ENL_OK;
+  cudaStream_t s = stream();
+  unsigned long long cnt = 0;
+  cudaMemcpyAsync(&cnt, E->d_mic_count, sizeof(cnt), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const long long stored = std::min<long long>((long long)cnt, E->mic_cap);
+  const long long take = std::min(stored, max);
+  if (take > 0) cudaMemcpyAsync(host, E->d_mic_rec, take * sizeof(MicRecord), cudaMemcpyDeviceToHost, s);
+  cudaMemsetAsync(E->d_mic_count, 0, sizeof(unsigned long long), s);
+  cudaStreamSynchronize(s);
+  *n = take;
+  if (dropped) *dropped = (long long)cnt - take;
+  return check_launch("mic_records");
+}
+
 int enl_engine_set_adaptive_dt(void* e, int on, double cfl) {
   Engine* E = (Engine*)e;
   if (!E || cfl <= 0.0 || cfl >= 1.0) {
@@ -1874,53 +2476,75 @@ static long long packed_cells(Engine* E) {
   return E->h_tileoff.back() + (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
 }
 
-int enl_engine_packed_size(void* e, long long* ndoubles) {
+int enl_engine_packed_size(void* e, long long* nelems) {
   Engine* E = (Engine*)e;
-  if (!E || !ndoubles) return ENL_ERR_ARG;
-  *ndoubles = packed_cells(E) * kNF;
+  if (!E || !nelems) return ENL_ERR_ARG;
+  *nelems = packed_cells(E) * kNF;
   return ENL_OK;
 }
 
-static int pack_common(Engine* E, double* host, int unpack) {
+int enl_engine_storage(void* e, int* elem_bytes, double* offsets) {
+  Engine* E = (Engine*)e;
+  if (!E) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  if (elem_bytes) *elem_bytes = (int)E->esize;
+  if (offsets)
+    for (int k = 0; k < kNF; ++k) offsets[k] = E->off[k];
+  return ENL_OK;
+}
+
+}  // extern "C"
+
+template <typename S>
+static void pack_t(Engine* E, long long cells, int unpack) {
+  PackArgs<S> A;
+  memset(&A, 0, sizeof(A));
+  for (int l = 0; l < E->cfg.nlevels; ++l) A.lev[l] = E->lev[l].view<S>(0);
+  A.tiles = E->d_tiles.p;
+  A.off = E->d_tileoff.p;
+  A.ntiles = (int)E->h_tiles.size();
+  A.total = cells;
+  A.packed = static_cast<S*>(E->d_packed);
+  A.unpack = unpack;
+  pack_kernel<S><<<std::min(A.ntiles, E->nsm * 8), 256, 0, stream()>>>(A);
+}
+
+extern "C" {
+
+static int pack_common(Engine* E, void* host, int unpack) {
   long long cells = packed_cells(E);
   if (cells == 0) return ENL_OK;
-  size_t need = (size_t)cells * kNF;
-  if (need > E->packed_cap) {
+  const size_t bytes = (size_t)cells * kNF * E->esize;
+  if (bytes > E->packed_cap) {
     if (E->d_packed) cudaFree(E->d_packed);
-    if (cudaMalloc(&E->d_packed, need * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&E->d_packed, bytes) != cudaSuccess) {
       E->d_packed = nullptr;
       E->packed_cap = 0;
       set_error(ENL_ERR_CUDA);
       return ENL_ERR_CUDA;
     }
-    E->packed_cap = need;
+    E->packed_cap = bytes;
   }
   cudaStream_t s = stream();
-  PackArgs A;
-  memset(&A, 0, sizeof(A));
-  for (int l = 0; l < E->cfg.nlevels; ++l) A.lev[l] = E->lev[l].view(0);
-  A.tiles = E->d_tiles.p;
-  A.off = E->d_tileoff.p;
-  A.ntiles = (int)E->h_tiles.size();
-  A.total = cells;
-  A.packed = E->d_packed;
-  A.unpack = unpack;
-  if (unpack) cudaMemcpyAsync(E->d_packed, host, need * sizeof(double), cudaMemcpyHostToDevice, s);
-  pack_kernel<<<std::min(A.ntiles, E->nsm * 8), 256, 0, s>>>(A);
-  if (!unpack) cudaMemcpyAsync(host, E->d_packed, need * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (unpack) cudaMemcpyAsync(E->d_packed, host, bytes, cudaMemcpyHostToDevice, s);
+  if (E->f32s) pack_t<float>(E, cells, unpack);
+  else pack_t<double>(E, cells, unpack);
+  if (!unpack) cudaMemcpyAsync(host, E->d_packed, bytes, cudaMemcpyDeviceToHost, s);
   return check_launch(unpack ? "engine upload" : "engine download");
 }
 
-int enl_engine_download(void* e, double* host) {
+int enl_engine_download(void* e, void* host) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
   return pack_common(E, host, 0);
 }
 
-int enl_engine_upload(void* e, const double* host) {
+int enl_engine_upload(void* e, const void* host) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, const_cast<double*>(host), 1);
+  return pack_common(E, const_cast<void*>(host), 1);
 }
 
 int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, long long* cells) {
@@ -1944,7 +2568,7 @@ int enl_engine_set_mlp(void* e, const float* params_host, float margin) {
     set_error(ENL_ERR_ARG);
     return ENL_ERR_ARG;
   }
-  if (!(E->cfg.precision == ENL_PREC_FP32 && E->cfg.learned)) {
+  if (!(E->cfg.precision != ENL_PREC_FP64 && E->cfg.learned)) {
     set_error(ENL_ERR_STATE);
     return ENL_ERR_STATE;
   }
@@ -1955,6 +2579,7 @@ int enl_engine_set_mlp(void* e, const float* params_host, float margin) {
   }
   cudaMemcpyAsync(E->d_mlp, params_host, kNParams * sizeof(float), cudaMemcpyHostToDevice, stream());
   cudaStreamSynchronize(stream());
+  if (E->margin != margin) E->graph_valid = false;  // the margin is a kernel argument
   E->margin = margin;
   return check_launch("set_mlp");
 }
@@ -1966,35 +2591,10 @@ int enl_engine_harvest(void* e, int level, double dt, const double* scale, doubl
     set_error(ENL_ERR_ARG);
     return ENL_ERR_ARG;
   }
-  const auto& c = E->cfg;
-  Level& L = E->lev[level];
   fill_all(E, 0);
-  HarvestArgs A;
-  memset(&A, 0, sizeof(A));
-  A.V = L.view(0);
-  A.H = L.view(3);
-  double xlo[2] = {c.xlo[0], c.xlo[1]};
-  A.P = make_rhs_const(xlo, L.dx, c.weno_alpha, c.kappa, c.mu, c.muB, c.R, c.T_star_n, c.tau_n, c.tol, 0, c.c,
-                       c.c_lr);
-  A.eps = (float)A.P.sensor_eps;
-  A.eps_p = (float)(A.P.sensor_eps * (c.c * c.c) * (c.c * c.c));
-  A.inv_sqrt_eps = (float)(1.0 / sqrt(A.P.sensor_eps));
-  A.rho0 = (float)c.rho0;
-  A.p0 = (float)c.p0;
-  A.T0 = (float)c.T0;
-  A.tiles = E->d_tiles.p;
-  A.off = E->tile_off[level];
-  A.cnt = E->tile_cnt[level];
-  A.dt = dt;
-  for (int k = 0; k < 5; ++k) A.inv_scale[k] = 1.0 / scale[k];
-  A.keep0 = (unsigned)(std::min(1.0, std::max(0.0, keep0)) * 4294967295.0);
-  A.seed = seed;
-  A.X = (__nv_bfloat16*)X;
-  A.lab = labels;
-  A.count = count_dev;
-  A.cap = capacity;
-  if (A.cnt) harvest_kernel<<<std::min(A.cnt, E->nsm * 16), 256, 0, stream()>>>(A);
-  return check_launch("harvest");
+  if (E->f32s) return harvest_t<float>(E, level, dt, scale, keep0, seed, X, labels, capacity, count_dev);
+  return harvest_t<double>(E, level, dt, scale, keep0, seed, X, labels, capacity, count_dev);
 }
+
 
 }  // extern "C"

@@ -10,22 +10,36 @@
 //   * T - T_n and T / T_n - 1 are formed from perturbations
 //     ((rho T_n - rho0 T0) - (rho - rho0) T0) / rho, which avoids cancellation;
 //   * the hybrid switch uses the division-free form of the ratio test.
-// The RK combination and p, T reconstruction are done in FP64 by the caller.
+// The caller stages per-tile planes of the velocities u = rho u / rho,
+// v = rho v / rho and of the fluxes F_k = u w_k (+ p for k = 1) and
+// G_k = v w_k (+ p for k = 2) at every halo position, so each cell reads
+// them instead of recomputing them for every stencil point.
 #pragma once
 #include "enl_physics.cuh"
 
 namespace enl {
+
+// Single-precision reciprocal of the hardware (rcp.approx, within 1 ulp);
+// every use is inside the FP32 perturbation path, whose error budget is
+// orders of magnitude above that.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 struct FastConst {
   float inv_dx0, inv_dx1, inv_dx0sq, inv_dx1sq, inv_2dx0, inv_2dx1, inv_4dxdy;
   float kappa, mu, muB, R078, T_star_n, inv_tau_n;
   float alpha, c, c_lr, ylo, dy;
   float sensor_eps;
-  float rho0, T0;
+  float rho0, T0, rho0T0;
   int level;
 };
 
-// acc.w(k, di, dj): perturbation field k (0..4), acc.p: p - p0, acc.t: T - T0.
+// acc.w(k, di, dj): perturbation field k (0..4), acc.p: p - p0, acc.t: T - T0,
+// acc.u / acc.v: velocities, acc.fx(k, di) / acc.gy(k, dj): fluxes F_k, G_k
+// along the cell's row / column.
 template <class ACC>
 __device__ __forceinline__ int sensor_fast(const ACC& A, const FastConst& P) {
   if (P.level != 0) return 1;
@@ -49,16 +63,15 @@ __device__ __forceinline__ int sensor_fast(const ACC& A, const FastConst& P) {
 
 template <class ACC>
 __device__ __forceinline__ void sources_fast(const ACC& A, const FastConst& P, float H[5]) {
-  float u[3][3], v[3][3], inv_c = 0.f;
+  float u[3][3], v[3][3];
 #pragma unroll
   for (int dj = -1; dj <= 1; ++dj)
 #pragma unroll
     for (int di = -1; di <= 1; ++di) {
-      float ir = __frcp_rn(P.rho0 + A.w(0, di, dj));
-      u[dj + 1][di + 1] = A.w(1, di, dj) * ir;
-      v[dj + 1][di + 1] = A.w(2, di, dj) * ir;
-      if (di == 0 && dj == 0) inv_c = ir;
+      u[dj + 1][di + 1] = A.u(di, dj);
+      v[dj + 1][di + 1] = A.v(di, dj);
     }
+  const float inv_c = rcp_approx(P.rho0 + A.w(0, 0, 0));
   const float c43 = 4.0f / 3.0f, c23 = 2.0f / 3.0f;
   float u_dxx = ((u[1][0] - 2.0f * u[1][1]) + u[1][2]) * P.inv_dx0sq;
   float u_dyy = ((u[0][1] - 2.0f * u[1][1]) + u[2][1]) * P.inv_dx1sq;
@@ -85,12 +98,12 @@ __device__ __forceinline__ void sources_fast(const ACC& A, const FastConst& P, f
   float T_n = P.T0 + Tn_p;
   float dT = tp - Tn_p;                                 // T - T_n
   float Mn = dT * P.inv_tau_n;
-  float inv_Tn = __frcp_rn(T_n);
+  float inv_Tn = rcp_approx(T_n);
   float tmp1 = P.T_star_n * inv_Tn;
   float c_vn = (P.R078 * (tmp1 * tmp1)) * __expf(-tmp1);
   float A_n = (dT * inv_Tn) * c_vn;
   float phi_xx = c43 * ux - c23 * vy, phi_xy = uy + vx, phi_yy = c43 * vy - c23 * ux;
-  float inv_T = __frcp_rn(Tc), inv_T2 = inv_T * inv_T;
+  float inv_T = rcp_approx(Tc), inv_T2 = inv_T * inv_T;
   float s0 = ux + vy;
   float sigma = (((P.muB * inv_T) * (s0 * s0) +
                   (P.mu * 0.5f * inv_T) * ((phi_xx * phi_xx + 2.0f * (phi_xy * phi_xy)) + phi_yy * phi_yy)) +
@@ -105,38 +118,28 @@ __device__ __forceinline__ void sources_fast(const ACC& A, const FastConst& P, f
 template <int ORDER, bool LLF, class ACC>
 __device__ __forceinline__ void fluxes_fast(const ACC& A, const FastConst& P, int row, int tag, float H[5],
                                             float KK[5]) {
-  float ux[7], vy[7];
-#pragma unroll
-  for (int q = 0; q < 7; ++q) {
-    ux[q] = A.w(1, q - 3, 0) * __frcp_rn(P.rho0 + A.w(0, q - 3, 0));
-    vy[q] = A.w(2, 0, q - 3) * __frcp_rn(P.rho0 + A.w(0, 0, q - 3));
-  }
   // ambient parts of w_k: only rho (k = 0) and rho T_n (k = 4) have one;
-  // u * w_k needs the full value, the split and the stencil use variations.
+  // the fluxes (staged planes) use the full value, the split and the
+  // stencil use variations.
   if (tag == 0) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      const float amb = k == 0 ? P.rho0 : (k == 4 ? P.rho0 * P.T0 : 0.0f);
       float fx = 0.f, gy = 0.f;
 #pragma unroll
       for (int m = 3; m >= 1; --m) {
         const float a = m == 1 ? (float)Lit::a1 : (m == 2 ? (float)Lit::a2 : (float)Lit::a3);
-        float fp = ux[3 + m] * (A.w(k, m, 0) + amb), fm = ux[3 - m] * (A.w(k, -m, 0) + amb);
-        float gp = vy[3 + m] * (A.w(k, 0, m) + amb), gm = vy[3 - m] * (A.w(k, 0, -m) + amb);
-        if (k == 1) {
-          fp += A.p(m, 0);
-          fm += A.p(-m, 0);
-        }
-        if (k == 2) {
-          gp += A.p(0, m);
-          gm += A.p(0, -m);
-        }
-        fx = fmaf(a, fp - fm, fx);
-        gy = fmaf(a, gp - gm, gy);
+        fx = fmaf(a, A.fx(k, m) - A.fx(k, -m), fx);
+        gy = fmaf(a, A.gy(k, m) - A.gy(k, -m), gy);
       }
       KK[k] = (H[k] - fx * P.inv_dx0) - gy * P.inv_dx1;
     }
     return;
+  }
+  float ux[7], vy[7];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    ux[q] = A.u(q - 3, 0);
+    vy[q] = A.v(0, q - 3);
   }
   float af, ag;
   if (LLF) {
@@ -155,14 +158,11 @@ __device__ __forceinline__ void fluxes_fast(const ACC& A, const FastConst& P, in
   }
 #pragma unroll 1
   for (int k = 0; k < 5; ++k) {
-    const float amb = k == 0 ? P.rho0 : (k == 4 ? P.rho0 * P.T0 : 0.0f);
     float fp[7], fm[7], gp[7], gm[7];
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
       float wx = A.w(k, q - 3, 0), wy = A.w(k, 0, q - 3);
-      float F = ux[q] * (wx + amb), G = vy[q] * (wy + amb);
-      if (k == 1) F += A.p(q - 3, 0);
-      if (k == 2) G += A.p(0, q - 3);
+      float F = A.fx(k, q - 3), G = A.gy(k, q - 3);
       fp[q] = 0.5f * fmaf(af, wx, F);
       fm[q] = 0.5f * fmaf(-af, wx, F);
       gp[q] = 0.5f * fmaf(ag, wy, G);

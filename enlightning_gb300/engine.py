@@ -9,21 +9,24 @@ cells into patches, proper nesting, and initialisation of new fine cells.
 
 Canvas convention: field k of level cell (i, j) is at
 ``base[k*fstride + (j+3)*pitch + (i+3)]``; fields are rho, rho*u, rho*v,
-rho*s, rho*T_n, p, T.
+rho*s, rho*T_n, p, T.  With PREC_FP32_STATE the canvases hold float32
+perturbations about the ambient state (``offsets`` per field);
+``level_state`` and ``set_level_state`` always speak absolute float64.
 """
 from __future__ import annotations
 
 import ctypes as C
+import time
 
 import numpy as np
 import torch
 
 from . import _lib
 from .constants import REFLECT, RK3_ALPHA1, RK3_ALPHA2, RK3_BETA, VARIANTS
-from .cluster import cluster_tags
+from .cluster import cluster_tags_native
 
 MAX_LEVELS = 4
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_FP32_STATE = 0, 1, 2
 
 
 from ._lib import ENGINE_SIGNATURES, EngineConfig  # noqa: E402
@@ -68,6 +71,11 @@ class Engine:
         _lib.check(self.L.enl_engine_create(C.byref(cfg), C.byref(h)), "enl_engine_create")
         self.h = h
         self.patches = [[] for _ in range(nlevels)]
+        eb = C.c_int()
+        off = (C.c_double * 7)()
+        _lib.check(self.L.enl_engine_storage(h, C.byref(eb), off), "enl_engine_storage")
+        self.dtype = torch.float32 if eb.value == 4 else torch.float64
+        self.offsets = np.array(off[:], np.float64)
 
     def close(self):
         if self.h:
@@ -98,7 +106,7 @@ class Engine:
                                             C.byref(nx), C.byref(ny)), "enl_engine_buffer")
         nf = 1 if which == 3 else 7
         n = fstride.value * nf
-        storage = _DeviceMemory(base.value, n)
+        storage = _DeviceMemory(base.value, n, "<f4" if self.dtype == torch.float32 else "<f8")
         t = torch.as_tensor(storage, device="cuda")
         t = t.as_strided((nf, ny.value + 6, nx.value + 6), (fstride.value, pitch.value, 1))
         return t
@@ -129,6 +137,11 @@ class Engine:
 
     def capture(self, dt):
         _lib.check(self.L.enl_engine_graph_capture(self.h, float(dt)), "enl_engine_graph_capture")
+
+    def graph_valid(self):
+        """True while the captured graph can be replayed (it survives regrids
+        unless a device table had to grow)."""
+        return bool(self.L.enl_engine_graph_valid(self.h))
 
     def replay(self, nsteps):
         _lib.check(self.L.enl_engine_graph_replay(self.h, int(nsteps)), "enl_engine_graph_replay")
@@ -170,10 +183,17 @@ class Engine:
         _lib.check(self.L.enl_engine_packed_size(self.h, C.byref(n)), "enl_engine_packed_size")
         return n.value
 
+    def packed_host(self, pin=True):
+        """Host tensor sized for download/upload (storage dtype)."""
+        t = torch.empty(self.packed_size(), dtype=self.dtype)
+        return t.pin_memory() if pin else t
+
     def download(self, host: torch.Tensor):
+        assert host.dtype == self.dtype
         _lib.check(self.L.enl_engine_download(self.h, C.c_void_p(host.data_ptr())), "enl_engine_download")
 
     def upload(self, host: torch.Tensor):
+        assert host.dtype == self.dtype
         _lib.check(self.L.enl_engine_upload(self.h, C.c_void_p(host.data_ptr())), "enl_engine_upload")
 
     def set_adaptive_dt(self, on=True, cfl=0.5):
@@ -194,6 +214,27 @@ class Engine:
             float(sine_freq), nseg, segarr.ctypes.data_as(C.POINTER(C.c_double)), float(drive)),
             "enl_engine_paint_source")
 
+    # -- microphones (enlightning.C:2392-2506) ---------------------------------
+    MIC_DTYPE = np.dtype([("iteration", "<i4"), ("mic", "<i4"), ("level", "<i4"), ("patch", "<i4"), ("p", "<f8")])
+
+    def set_mics(self, positions, capacity=1 << 20, iteration=0):
+        """Sample the pressure at these (x, y) positions after every step."""
+        xy = np.ascontiguousarray(np.asarray(positions, np.float64).reshape(-1))
+        _lib.check(self.L.enl_engine_set_mics(self.h, xy.size // 2, xy.ctypes.data_as(C.c_void_p) if xy.size else None,
+                                              int(capacity), int(iteration)), "enl_engine_set_mics")
+        self.nmics = xy.size // 2
+
+    def mic_records(self, max_records=1 << 20):
+        """Drain the device record buffer: structured array in the reference's
+        file order (iteration, microphone, level, patch) and the dropped count."""
+        out = np.zeros(max_records, self.MIC_DTYPE)
+        n, dropped = C.c_longlong(), C.c_longlong()
+        _lib.check(self.L.enl_engine_mic_records(self.h, out.ctypes.data_as(C.c_void_p), int(max_records),
+                                                 C.byref(n), C.byref(dropped)), "enl_engine_mic_records")
+        rec = out[: n.value]
+        order = np.lexsort((rec["patch"], rec["level"], rec["mic"], rec["iteration"]))
+        return rec[order], dropped.value
+
     def state_from_overpressure(self, level):
         _lib.check(self.L.enl_engine_state_from_overpressure(self.h, level), "enl_engine_state_from_overpressure")
 
@@ -207,24 +248,53 @@ class Engine:
 
     # -- state I/O ----------------------------------------------------------
     def set_level_state(self, level, w, pres, temp, which=0):
-        """Write interior (5, ny, nx) state and p, T (ny, nx) of a level."""
+        """Write interior (5, ny, nx) state and p, T (ny, nx) of a level (absolute values)."""
         buf = self.buffer(level, which)
         ny, nx = pres.shape
-        buf[0:5, 3:3 + ny, 3:3 + nx].copy_(torch.as_tensor(w, device="cuda"))
-        buf[5, 3:3 + ny, 3:3 + nx].copy_(torch.as_tensor(pres, device="cuda"))
-        buf[6, 3:3 + ny, 3:3 + nx].copy_(torch.as_tensor(temp, device="cuda"))
+        full = torch.empty((7, ny, nx), dtype=torch.float64, device="cuda")
+        full[0:5] = torch.as_tensor(w, device="cuda")
+        full[5] = torch.as_tensor(pres, device="cuda")
+        full[6] = torch.as_tensor(temp, device="cuda")
+        if self.dtype == torch.float32:
+            full -= torch.as_tensor(self.offsets, device="cuda")[:, None, None]
+        buf[:, 3:3 + ny, 3:3 + nx].copy_(full)
+
+    def set_box_state(self, level, i0, j0, w, pres, temp, which=0):
+        """Write absolute state (5, h, w) and p, T (h, w) into the cells
+        starting at level cell (i0, j0)."""
+        buf = self.buffer(level, which)
+        h, wd = pres.shape
+        full = torch.empty((7, h, wd), dtype=torch.float64, device="cuda")
+        full[0:5] = torch.as_tensor(w, device="cuda")
+        full[5] = torch.as_tensor(pres, device="cuda")
+        full[6] = torch.as_tensor(temp, device="cuda")
+        if self.dtype == torch.float32:
+            full -= torch.as_tensor(self.offsets, device="cuda")[:, None, None]
+        buf[:, 3 + j0:3 + j0 + h, 3 + i0:3 + i0 + wd].copy_(full)
+
+    def canvas_state(self, level, which=0):
+        """Whole canvas (7, ny+6, nx+6) with ghosts as absolute float64 (host numpy)."""
+        v = self.buffer(level, which).double()
+        if self.dtype == torch.float32:
+            v = v + torch.as_tensor(self.offsets, device="cuda")[:, None, None]
+        return v.cpu().numpy()
 
     def level_state(self, level, which=0):
+        """Interior (7, ny, nx) of a level: a view of the canvas with FP64
+        storage, an absolute float64 copy with FP32 perturbation storage."""
         buf = self.buffer(level, which)
         nx, ny = self.level_shape(level)
-        return buf[:, 3:3 + ny, 3:3 + nx]
+        v = buf[:, 3:3 + ny, 3:3 + nx]
+        if self.dtype == torch.float32:
+            return v.double() + torch.as_tensor(self.offsets, device="cuda")[:, None, None]
+        return v
 
 
 class _DeviceMemory:
     """__cuda_array_interface__ wrapper of library-owned device memory."""
 
-    def __init__(self, ptr, n):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3,
+    def __init__(self, ptr, n, typestr="<f8"):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 3,
                                          "strides": None}
 
 
@@ -252,6 +322,8 @@ class Hierarchy:
         self.min_size, self.max_size = min_size, max_size
         self.tag_buffer, self.efficiency = tag_buffer, efficiency
         self.block, self.nest_blocks = block, nest_blocks
+        # host seconds spent per regrid phase (tag map, clustering, tables, new fine data)
+        self.timing = {"tag": 0.0, "cluster": 0.0, "tables": 0.0, "refine": 0.0}
 
     def base_patches(self, size=256):
         nx, ny = self.E.level_shape(0)
@@ -263,6 +335,8 @@ class Hierarchy:
         return boxes
 
     def _nesting_blocks(self, level, nbx, nby):
+        """Blocks fully inside the patches of `level` (before the erosion by
+        nest_blocks that _nest_erode gives for fine levels)."""
         B = self.block
         m = np.zeros((nby, nbx), bool)
         for b in self.E.patches[level]:
@@ -270,25 +344,30 @@ class Hierarchy:
             by0, by1 = -(-b[2] // B), (b[3] + 1) // B - 1
             if bx1 >= bx0 and by1 >= by0:
                 m[by0:by1 + 1, bx0:bx1 + 1] = True
-        if self.nest_blocks > 0 and level > 0:
-            from scipy.ndimage import binary_erosion
-            m = binary_erosion(m, structure=np.ones((3, 3), bool), iterations=self.nest_blocks, border_value=1)
         return m
+
+    def _nest_erode(self, level):
+        return self.nest_blocks if (self.nest_blocks > 0 and level > 0) else 0
 
     def propose(self, level):
         """Fine boxes (level+1 index space) from the current tags of `level`."""
         E, B, r = self.E, self.block, self.E.ratio
+        t0 = time.perf_counter()
         bmap = E.tag_blocks(level, B, self.tag_buffer)
+        t1 = time.perf_counter()
+        self.timing["tag"] += t1 - t0
         nest = self._nesting_blocks(level, bmap.shape[1], bmap.shape[0])
         cell = B * r  # level+1 cells per block side
-        cboxes = cluster_tags(bmap, efficiency=self.efficiency, min_size=max(1, self.min_size // cell),
-                              max_size=max(1, self.max_size // cell), allowed=nest)
+        cboxes = cluster_tags_native(bmap, efficiency=self.efficiency, min_size=max(1, self.min_size // cell),
+                                     max_size=max(1, self.max_size // cell), allowed=nest,
+                                     nest_erode=self._nest_erode(level))
         nxf, nyf = E.level_shape(level + 1)
         fine = []
         for b in cboxes:
             fb = (b[0] * cell, min(nxf, (b[1] + 1) * cell) - 1, b[2] * cell, min(nyf, (b[3] + 1) * cell) - 1)
             if fb[1] >= fb[0] and fb[3] >= fb[2]:
                 fine.append(fb)
+        self.timing["cluster"] += time.perf_counter() - t1
         return fine
 
     def regrid_level(self, level):
@@ -298,9 +377,14 @@ class Hierarchy:
             return []
         fine = self.propose(level)
         old = list(E.patches[level + 1])
+        t0 = time.perf_counter()
         new_regions = box_difference(fine, old)
         E.set_patches(level + 1, fine)
+        t1 = time.perf_counter()
         E.refine_init(level + 1, new_regions)
+        t2 = time.perf_counter()
+        self.timing["tables"] += t1 - t0
+        self.timing["refine"] += t2 - t1
         return fine
 
     def regrid(self):

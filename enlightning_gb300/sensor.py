@@ -9,6 +9,9 @@ stencil features, whether WENO actually changes the right-hand side there:
   label y = 1  iff  the plain switch says WENO  and
                     err = max_k dt |KK_drp,k - KK_weno,k| / scale_k > tau
 
+The network only reviews cells the plain switch puts on WENO (it can send
+them back to DRP), so the harvest keeps those cells.
+
 where KK_drp and KK_weno are the two right-hand sides of the same cell in
 FP64 (harvested by enl_engine_harvest from trajectories of the batched
 engine).  Training runs entirely on the GPU with the library's BF16
@@ -149,7 +152,7 @@ def logits(X, params):
     return out
 
 
-def harvest_line_source(H, seeds, steps=30, every=10, keep0=0.05, prm=None, log=None, **kw):
+def harvest_line_source(H, seeds, steps=30, every=10, keep0=0.0, prm=None, log=None, **kw):
     from . import workloads
     from .engine import PREC_FP32
     prm = prm or default_params()
@@ -167,7 +170,7 @@ def harvest_line_source(H, seeds, steps=30, every=10, keep0=0.05, prm=None, log=
         E.close()
 
 
-def harvest_shock(H, seeds, steps=40, every=10, keep0=0.05, prm=None, log=None, **kw):
+def harvest_shock(H, seeds, steps=40, every=10, keep0=0.0, prm=None, log=None, **kw):
     from . import workloads
     prm = prm or default_params()
     for sd in seeds:

@@ -224,17 +224,13 @@ def pulse_batch(prm, seed=7, n=64, side_range=(128, 1024), precision=1, learned=
                learned=learned, independent=True)
     boxes = [(x, x + s - 1, y, y + s - 1) for (x, y), s in zip(pos, sides)]
     E.set_patches(0, boxes)
-    buf = E.buffer(0, 0)
     k = (prm["gamma1"] - 1.0) / (2.0 * prm["rho0"])
-    import torch
     for (x, y), s, a, sg in zip(pos, sides, amps, sigmas):
         dp = gaussian_dp(s, s, a * prm["p0"], sg)
         w = state_from_dp(dp, prm)
         drho = w[0] - prm["rho0"]
         p = prm["c"] ** 2 * (drho + k * drho ** 2) + prm["p0"]
         T = w[4] / w[0]
-        buf[0:5, 3 + y:3 + y + s, 3 + x:3 + x + s].copy_(torch.from_numpy(w))
-        buf[5, 3 + y:3 + y + s, 3 + x:3 + x + s].copy_(torch.from_numpy(p))
-        buf[6, 3 + y:3 + y + s, 3 + x:3 + x + s].copy_(torch.from_numpy(T))
+        E.set_box_state(0, x, y, w, p, T)
     dt = pulse_dt(prm, (dx, dx))
     return E, boxes, dict(sides=sides, amps=amps, sigmas=sigmas, dt=dt)

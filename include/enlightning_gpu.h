@@ -176,6 +176,10 @@ int enl_absorb(int ifirst0, int ilast0, int ifirst1, int ilast1, int gcw0,
 #define ENL_MAX_LEVELS 4
 #define ENL_PREC_FP64 0   /* RHS in FP64: same results as the plain path   */
 #define ENL_PREC_FP32 1   /* RHS in FP32 perturbation form, FP64 state     */
+#define ENL_PREC_FP32_STATE 2 /* FP32 throughout: canvases hold FP32
+                             perturbations about the ambient state (rho -
+                             rho0, rho u, rho v, rho s, rho T_n - rho0 T0,
+                             p - p0, T - T0); no plain path            */
 
 typedef struct {
   int nlevels;            /* 1..ENL_MAX_LEVELS                              */
@@ -185,8 +189,8 @@ typedef struct {
   double dx0[2];          /* level-0 cell size (m)                           */
   int bc[4];              /* L, R, B, T: 10 = REFLECT, 20 = ABSORB           */
   int variant;            /* ENL_* scheme id                                 */
-  int precision;          /* ENL_PREC_FP64 or ENL_PREC_FP32                  */
-  int learned;            /* 1: learned switch on level 0 (FP32 only)        */
+  int precision;          /* ENL_PREC_FP64, ENL_PREC_FP32, ENL_PREC_FP32_STATE */
+  int learned;            /* 1: learned switch on level 0 (FP32 modes only)  */
   double weno_alpha, kappa, mu, muB, R, T_star_n, tau_n, c, c_lr;
   double tol[3];
   double rho0, gamma1, c_p, p0, T0, c_v;
@@ -203,12 +207,19 @@ int enl_engine_create(const enl_engine_config* cfg, void** engine);
 int enl_engine_destroy(void* engine);
 /* Device canvas of one level: which = 0 current, 1 stage A, 2 stage B,
  * 3 source H0.  Cell (i, j) of the level (i, j >= -3) is element
- * base[k*fstride + (j+3)*pitch + (i+3)] of field k. */
-int enl_engine_buffer(void* engine, int level, int which, double** base,
+ * base[k*fstride + (j+3)*pitch + (i+3)] of field k, in the storage type of
+ * the engine (enl_engine_storage). */
+int enl_engine_buffer(void* engine, int level, int which, void** base,
                       long* pitch, long* fstride, int* nx, int* ny);
+/* Storage of the canvases and of the packed state: element size (8 = double,
+ * 4 = float) and, per field, the ambient value held out of the storage
+ * (absolute value = offsets[k] + stored value; all 0 for FP64 storage).
+ * offsets may be NULL. */
+int enl_engine_storage(void* engine, int* elem_bytes, double* offsets);
 /* Patch boxes of one level, (ilo, ihi, jlo, jhi) per patch in that level's
  * index space, host array of 4*npatch ints.  Level l > 0 boxes must be
- * properly nested in level l-1 (after coarsening) and start at even x. */
+ * properly nested in level l-1 (after coarsening).  ilo must be even (a
+ * multiple of 4 with FP32 storage): tile rows are TMA copies. */
 int enl_engine_set_patches(void* engine, int level, int npatch, const int* boxes);
 /* Fill the cells of the given boxes of `level` (current buffer) by bilinear
  * interpolation from level-1 (new fine data after a regrid). */
@@ -219,11 +230,17 @@ int enl_engine_fill(void* engine, int which);
 int enl_engine_step(void* engine, double dt);
 /* One RK3 step of the plain path: per patch, unfused FP64 rhs, runge_kutta
  * and update_state launches (what enlightning.C issues through the F77
- * entry points), same storage and ghost fill. */
+ * entry points), same storage and ghost fill.  FP64 storage only
+ * (ENL_ERR_STATE otherwise). */
 int enl_engine_step_plain(void* engine, double dt);
-/* Capture one fused step as a CUDA graph, then replay it nsteps times. */
+/* Capture one fused step as a CUDA graph, then replay it nsteps times.
+ * Kernels read tile, halo and patch tables from device memory, so a regrid
+ * (enl_engine_set_patches) keeps the graph valid unless a table outgrows its
+ * capacity; enl_engine_graph_valid (1/0) tells whether a new capture is
+ * needed. */
 int enl_engine_graph_capture(void* engine, double dt);
 int enl_engine_graph_replay(void* engine, int nsteps);
+int enl_engine_graph_valid(void* engine);
 /* tag_cells over the patches of `level` (fortran/tag_cells.m4), into a
  * device int array of nx*ny (level index space, row pitch nx); cells outside
  * the patches are 0.  Fills ghosts of the current buffer and H0 first. */
@@ -253,10 +270,11 @@ int enl_engine_time(void* engine, double* dt_last, double* sim_time);
 /* State exchange with host memory: the current buffer's patch interiors of
  * every level, packed (7 fields, tile order: level by level, patch by patch,
  * 32x8 tiles row-major).  Asynchronous on the stream; host memory should be
- * pinned.  enl_engine_packed_size gives the number of doubles. */
-int enl_engine_packed_size(void* engine, long long* ndoubles);
-int enl_engine_download(void* engine, double* host);
-int enl_engine_upload(void* engine, const double* host);
+ * pinned.  Elements are of the storage type (enl_engine_storage: doubles,
+ * or FP32 perturbations); enl_engine_packed_size gives their number. */
+int enl_engine_packed_size(void* engine, long long* nelems);
+int enl_engine_download(void* engine, void* host);
+int enl_engine_upload(void* engine, const void* host);
 
 /* Stage-kernel timing: with on = 1 every direct (not graph) enl_engine_step
  * brackets its three stage-kernel launches with CUDA events on the stream.
@@ -286,7 +304,7 @@ int enl_mlp_adam(float* params, const float* grad, float* m, float* v,
                  float lr, float beta1, float beta2, float eps, float inv_n,
                  int step);
 /* Install the network (host FP32 vector) in an engine created with
- * precision ENL_PREC_FP32 and learned = 1. */
+ * precision ENL_PREC_FP32 or ENL_PREC_FP32_STATE and learned = 1. */
 int enl_engine_set_mlp(void* engine, const float* params_host, float margin);
 /* Harvest training rows from a level of the engine (plain FP64 arithmetic):
  * features (device BF16 [capacity][40]), labels (device float [capacity][2]
@@ -317,6 +335,41 @@ int enl_engine_state_from_overpressure(void* engine, int level);
  * cell within `buffer` cells.  With map_host == NULL only nbx, nby are set. */
 int enl_engine_tag_blocks(void* engine, int level, int block, int buffer,
                           unsigned char* map_host, int* nbx, int* nby);
+/* Virtual microphones, enlightning::recordAudio (enlightning.C:2392-2506):
+ * with nmics > 0, every enl_engine_step (and graph replay) ends by sampling
+ * the pressure for each microphone (xy: host, x0, y0, x1, y1, ... in metres)
+ * in every patch of every level whose closed extent contains it, at
+ * i = int((x - patch xlo)/dx), j = int((y - patch ylo)/dy), read as element
+ * j*nx + i of the patch interior as the reference indexes it (NaN where
+ * that falls past the patch).  Records go to a device buffer of `capacity`
+ * entries; `iteration` is the number of the last completed step (the next
+ * step records iteration + 1).  nmics = 0 turns sampling off.  Setting or
+ * clearing microphones invalidates a captured graph. */
+typedef struct {
+  int iteration, mic, level, patch; /* patch: index over all levels, level-major */
+  double p;
+} enl_mic_record;
+int enl_engine_set_mics(void* engine, int nmics, const double* xy,
+                        long long capacity, int iteration);
+/* Copy up to max records (in device arrival order) to host memory and empty
+ * the buffer; dropped = records lost to a full buffer. */
+int enl_engine_mic_records(void* engine, void* host, long long max,
+                           long long* n, long long* dropped);
+
+/* Host-side clustering of a tag map (nx*ny bytes, row-major, e.g. the block
+ * map of enl_engine_tag_blocks) into boxes (ilo, ihi, jlo, jhi) in map
+ * coordinates, as SAMRAI's BergerRigoutsos does for the reference
+ * (main.C:261-265, input.txt:123-127): boxes cover every tag inside
+ * `allowed` (NULL: everywhere; proper nesting), after nest_erode erosions
+ * of `allowed` by the 3x3 square (cells outside the map count as allowed),
+ * never cover a disallowed cell, reach `efficiency` tagged fraction or
+ * cannot be cut further, and have no side longer than max_size.  Writes at
+ * most max_boxes boxes and the count needed to nboxes (ENL_ERR_ARG when
+ * that exceeds max_boxes).  No GPU involved. */
+int enl_cluster_tags(const unsigned char* tags, const unsigned char* allowed,
+                     int nx, int ny, int nest_erode, double efficiency,
+                     int min_size, int max_size, int* boxes, int max_boxes,
+                     int* nboxes);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free stable time step of one patch.  No counterpart in the

@@ -51,3 +51,60 @@ def test_chop_and_box_difference():
     m = _cover(d, (12, 12))
     ref = _cover([(0, 9, 0, 9)], (12, 12)) & ~_cover([(3, 5, 2, 20)], (12, 12))
     assert (m == ref).all()
+
+
+def _random_tag_map(rng, ny, nx, kind):
+    tags = np.zeros((ny, nx), bool)
+    if kind == "blobs":
+        Y, X = np.mgrid[0:ny, 0:nx]
+        for _ in range(rng.integers(1, 8)):
+            x, y, r = rng.integers(0, nx), rng.integers(0, ny), rng.integers(1, 12)
+            tags |= (X - x) ** 2 + (Y - y) ** 2 < r * r
+    elif kind == "walk":  # a thin random-walk channel like the line source's
+        x, y = nx / 2, ny - 2.0
+        for _ in range(6 * (nx + ny)):
+            a = -np.pi / 2 + rng.normal(0, 0.7)
+            x, y = x + np.cos(a) * 0.7, y + np.sin(a) * 0.7
+            if 0 <= int(y) < ny and 0 <= int(x) < nx:
+                tags[int(y), max(0, int(x) - 1):int(x) + 2] = True
+    else:  # sparse noise
+        tags = rng.random((ny, nx)) < 0.03
+    return tags
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_native_clustering_equals_specification(seed):
+    """enl_cluster_tags (C++, summed-area tables) returns exactly the boxes,
+    in the same order, of the array-based cluster_tags."""
+    from enlightning_gb300.cluster import cluster_tags_native
+    rng = np.random.default_rng(1000 + seed)
+    ny, nx = int(rng.integers(8, 120)), int(rng.integers(8, 160))
+    tags = _random_tag_map(rng, ny, nx, ["blobs", "walk", "noise"][seed % 3])
+    allowed = None
+    if seed % 2:
+        allowed = np.ones((ny, nx), bool)
+        for _ in range(3):
+            x0, y0 = rng.integers(0, nx), rng.integers(0, ny)
+            allowed[y0:y0 + rng.integers(1, 20), x0:x0 + rng.integers(1, 30)] = False
+    kw = dict(efficiency=float(rng.choice([0.5, 0.7, 0.9])), min_size=int(rng.integers(1, 5)),
+              max_size=int(rng.integers(4, 40)), allowed=allowed)
+    ref = cluster_tags(tags, **kw)
+    got = cluster_tags_native(tags, **kw)
+    assert got == ref
+    if allowed is not None:  # the nesting erosion done inside the native call
+        from enlightning_gb300.cluster import erode_allowed
+        for passes in (1, 2):
+            kw2 = dict(kw, allowed=erode_allowed(allowed, passes))
+            assert cluster_tags_native(tags, **dict(kw, nest_erode=passes)) == cluster_tags(tags, **kw2)
+
+
+def test_native_clustering_edge_cases():
+    from enlightning_gb300.cluster import cluster_tags_native
+    assert cluster_tags_native(np.zeros((5, 7), bool)) == []
+    one = np.zeros((5, 7), bool)
+    one[2, 3] = True
+    assert cluster_tags_native(one, min_size=1) == cluster_tags(one, min_size=1) == [(3, 3, 2, 2)]
+    full = np.ones((40, 300), bool)
+    assert cluster_tags_native(full, max_size=64) == cluster_tags(full, max_size=64)
+    nothing_allowed = np.zeros((5, 7), bool)
+    assert cluster_tags_native(one, allowed=nothing_allowed) == []

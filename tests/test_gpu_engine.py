@@ -4,7 +4,8 @@
   after several RK3 steps, on a single patch (the reference's own
   single-patch semantics) and on a two-level hierarchy (oracle/amr.py);
 * graph replay is bit-identical to direct launches;
-* the FP32 perturbation-form path stays within 1e-3 relative L2 of FP64,
+* the FP32 perturbation-form paths (FP32 right-hand side on FP64 state, and
+  FP32 perturbation state throughout) stay within 1e-3 relative L2 of FP64,
   also on the perturbation fields;
 * tag_cells over the level canvas is bit-exact.
 """
@@ -16,7 +17,9 @@ pytestmark = pytest.mark.gpu
 
 from enlightning_gb300 import workloads  # noqa: E402
 from enlightning_gb300.constants import ABSORB, REFLECT, default_params  # noqa: E402
-from enlightning_gb300.engine import PREC_FP32, PREC_FP64, Engine  # noqa: E402
+from enlightning_gb300 import _lib  # noqa: E402
+from enlightning_gb300._lib import EnlightningError  # noqa: E402
+from enlightning_gb300.engine import PREC_FP32, PREC_FP32_STATE, PREC_FP64, Engine  # noqa: E402
 
 G = 3
 
@@ -136,7 +139,7 @@ def test_fp32_fast_path_within_budget(ora):
     nx, ny = 96, 64
     boxes = [[(0, 47, 0, 63), (48, 95, 0, 63)], [(48, 143, 32, 95)]]
     out = {}
-    for prec in (PREC_FP64, PREC_FP32):
+    for prec in (PREC_FP64, PREC_FP32, PREC_FP32_STATE):
         E, O = make_pair(prm, nx, ny, (0.1, 0.1), 2, boxes, (REFLECT,) * 4, "hybrid_high_llf", precision=prec)
         dt = workloads.pulse_dt(prm, (0.05, 0.05))
         for _ in range(20):
@@ -144,15 +147,17 @@ def test_fp32_fast_path_within_budget(ora):
         torch.cuda.synchronize()
         assert E.health() == 0
         out[prec] = [E.level_state(l).cpu().numpy().copy() for l in range(2)]
-    for l in range(2):
-        a, b = out[PREC_FP32][l], out[PREC_FP64][l]
-        m = np.zeros(a.shape[1:], bool)
-        for bx in boxes[l]:
-            m[bx[2]:bx[3] + 1, bx[0]:bx[1] + 1] = True
-        for k in (0, 1, 2, 4):
-            assert relL2(a[k][m], b[k][m]) <= 1e-3
-        assert relL2(a[0][m] - prm["rho0"], b[0][m] - prm["rho0"]) <= 1e-3
-        assert relL2(a[5][m] - prm["p0"], b[5][m] - prm["p0"]) <= 1e-3
+    for prec in (PREC_FP32, PREC_FP32_STATE):
+        for l in range(2):
+            a, b = out[prec][l], out[PREC_FP64][l]
+            m = np.zeros(a.shape[1:], bool)
+            for bx in boxes[l]:
+                m[bx[2]:bx[3] + 1, bx[0]:bx[1] + 1] = True
+            for k in (0, 1, 2, 4):
+                assert relL2(a[k][m], b[k][m]) <= 1e-3, (prec, l, k)
+            assert relL2(a[0][m] - prm["rho0"], b[0][m] - prm["rho0"]) <= 1e-3, (prec, l)
+            assert relL2(a[5][m] - prm["p0"], b[5][m] - prm["p0"]) <= 1e-3, (prec, l)
+            assert relL2(a[6][m] - prm["T0"], b[6][m] - prm["T0"]) <= 1e-3, (prec, l)
 
 
 def test_engine_tag_bit_exact(ora):
@@ -240,7 +245,7 @@ def test_line_source_hierarchy_small():
     levels, regrids, FP32 batched vs FP64 plain within 1e-3."""
     prm = default_params()
     out = {}
-    for prec, plain in ((PREC_FP32, False), (PREC_FP64, True)):
+    for prec, plain in ((PREC_FP32, False), (PREC_FP32_STATE, False), (PREC_FP64, True)):
         E, H, segs = workloads.line_source(prm, nx0=256, ny0=128, dx0=0.5, nlevels=3, nseg=20, precision=prec,
                                            base_patch=64)
         assert len(E.patches[1]) > 0 and len(E.patches[2]) > 0
@@ -251,10 +256,12 @@ def test_line_source_hierarchy_small():
         torch.cuda.synchronize()
         assert E.health() == 0
         out[prec] = E.level_state(0).cpu().numpy().copy()
-    a, b = out[PREC_FP32], out[PREC_FP64]
-    for k in (0, 1, 2, 4, 5):
-        assert relL2(a[k], b[k]) <= 1e-3
-    assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) <= 1e-3
+    for prec in (PREC_FP32, PREC_FP32_STATE):
+        a, b = out[prec], out[PREC_FP64]
+        for k in (0, 1, 2, 4, 5):
+            assert relL2(a[k], b[k]) <= 1e-3, (prec, k)
+        assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) <= 1e-3, prec
+        assert relL2(a[5] - prm["p0"], b[5] - prm["p0"]) <= 1e-3, prec
 
 
 def test_independent_problems_match_single_patch_oracle(ora):
@@ -279,3 +286,147 @@ def test_independent_problems_match_single_patch_oracle(ora):
         ora.advance(P, prm, "hybrid_high_llf", info["dt"], 6, domain=((0, 0), (s * 0.1, s * 0.1)))
         for k in range(5):
             assert relL2(got[k, b[2]:b[3] + 1, b[0]:b[1] + 1], P.w_cur[k]) <= 1e-12
+
+
+def test_fp32_state_storage_roundtrip_and_graph(ora):
+    """FP32 perturbation storage: the canvases hold float32 values about the
+    ambient state, state I/O converts exactly, the packed exchange moves
+    float32, and graph replay equals direct launches bit for bit."""
+    prm = default_params()
+    nx, ny = 64, 48
+    res = []
+    for use_graph in (False, True):
+        E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 63, 0, 47)], [(32, 95, 24, 71)]], (REFLECT,) * 4,
+                         "hybrid_high_llf", precision=PREC_FP32_STATE)
+        assert E.dtype == torch.float32
+        assert E.offsets[0] == prm["rho0"] and E.offsets[5] == prm["p0"] and E.offsets[6] == prm["T0"]
+        raw = E.buffer(0, 0)
+        st = E.level_state(0)
+        assert raw.dtype == torch.float32 and st.dtype == torch.float64
+        assert torch.equal(st[0], raw[0, 3:3 + ny, 3:3 + nx].double() + prm["rho0"])
+        dt = workloads.pulse_dt(prm, (0.05, 0.05))
+        s = torch.cuda.Stream()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            E.L.enl_set_stream(__import__("ctypes").c_void_p(s.cuda_stream))
+            if use_graph:
+                E.capture(dt)
+                E.replay(5)
+            else:
+                for _ in range(5):
+                    E.step(dt)
+        torch.cuda.synchronize()
+        E.L.enl_set_stream(__import__("ctypes").c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert E.health() == 0
+        res.append([E.buffer(l, 0).cpu().numpy().copy() for l in range(2)])
+        # packed exchange in float32
+        host = E.packed_host(pin=True)
+        assert host.dtype == torch.float32 and host.numel() == E.packed_size()
+        E.download(host)
+        torch.cuda.synchronize()
+        before = [E.level_state(l).cpu().numpy().copy() for l in range(2)]
+        E.buffer(0, 0).zero_()
+        E.buffer(1, 0).zero_()
+        E.upload(host)
+        torch.cuda.synchronize()
+        for l in range(2):
+            after = E.level_state(l).cpu().numpy()
+            for b in E.patches[l]:
+                sl = (slice(None), slice(b[2], b[3] + 1), slice(b[0], b[1] + 1))
+                assert np.array_equal(after[sl], before[l][sl])
+        with pytest.raises(EnlightningError):
+            E.step(dt, plain=True)  # the plain path needs FP64 storage
+        assert _lib.lib().enl_get_last_error() == 5  # ENL_ERR_STATE, consumed here
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b)
+
+
+def test_fp32_state_refuses_unaligned_patches():
+    prm = default_params()
+    E = Engine(prm, 64, 32, (0.1, 0.1), nlevels=1, precision=PREC_FP32_STATE)
+    with pytest.raises(EnlightningError):
+        E.set_patches(0, [(2, 33, 0, 31)])  # x origin not a multiple of 4
+    assert _lib.lib().enl_get_last_error() == 1  # ENL_ERR_ARG, consumed here
+    E.set_patches(0, [(4, 35, 0, 31)])
+    E.close()
+
+
+def _expected_mics(E, mics, it):
+    """The reference's recordAudio rule (enlightning.C:2392-2506) on the
+    engine's current state: (iteration, mic, level, patch, p) rows."""
+    rows, base = [], 0
+    for l in range(E.nlevels):
+        st = E.level_state(l).cpu().numpy()
+        dx, dy = E.dx(l)
+        for q, b in enumerate(E.patches[l]):
+            xl, xh = E.xlo[0] + dx * b[0], E.xlo[0] + dx * (b[1] + 1)
+            yl, yh = E.xlo[1] + dy * b[2], E.xlo[1] + dy * (b[3] + 1)
+            nx, ny = b[1] - b[0] + 1, b[3] - b[2] + 1
+            for k, (x, y) in enumerate(mics):
+                if x >= xl and x <= xh and y >= yl and y <= yh:
+                    i, j = int((x - xl) / dx), int((y - yl) / dy)
+                    idx = j * nx + i
+                    p = st[5, b[2] + idx // nx, b[0] + idx % nx] if idx < nx * ny else np.nan
+                    rows.append((it, k, l, base + q, p))
+        base += len(E.patches[l])
+    return sorted(rows, key=lambda r: (r[0], r[1], r[2], r[3]))
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_microphones_follow_record_audio(ora, precision):
+    prm = default_params()
+    nx, ny = 64, 48
+    E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 31, 0, 47), (32, 63, 0, 47)], [(32, 95, 24, 71)]],
+                     (REFLECT,) * 4, "hybrid_high_llf", precision=precision)
+    mics = [(1.234, 2.71),   # level 0 only
+            (2.5, 3.05),     # inside the fine patch: recorded on both levels
+            (3.2, 1.0),      # on the boundary shared by the two level-0 patches
+            (6.4, 4.8),      # upper corner of the domain: reads past the patch (NaN)
+            (9.0, 9.0)]      # outside every patch
+    E.set_mics(mics, capacity=4096, iteration=0)
+    dt = workloads.pulse_dt(prm, (0.05, 0.05))
+    want = []
+    for it in range(1, 4):
+        E.step(dt)
+        torch.cuda.synchronize()
+        want += _expected_mics(E, mics, it)
+    got, dropped = E.mic_records()
+    assert dropped == 0
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert (int(g["iteration"]), int(g["mic"]), int(g["level"]), int(g["patch"])) == w[:4]
+        if np.isnan(w[4]):
+            assert np.isnan(g["p"])
+        else:
+            assert g["p"] == w[4]
+    assert sum(1 for w in want if w[1] == 1) == 2 * 3   # the fine-patch microphone, two levels per step
+    assert sum(1 for w in want if w[1] == 2) == 2 * 3   # the shared boundary, two patches per step
+    assert not any(w[1] == 4 for w in want)
+    # the same sampling inside a captured graph; iterations continue at 4
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        E.L.enl_set_stream(__import__("ctypes").c_void_p(s.cuda_stream))
+        E.capture(dt)
+        E.replay(2)
+    torch.cuda.synchronize()
+    E.L.enl_set_stream(__import__("ctypes").c_void_p(torch.cuda.current_stream().cuda_stream))
+    got, _ = E.mic_records()
+    assert sorted(set(int(v) for v in got["iteration"])) == [4, 5]  # capture records, replay runs two steps
+    E.set_mics([])
+    assert E.health() == 0
+
+
+def test_mic_files_in_reference_format(tmp_path):
+    from enlightning_gb300.engine import Engine as _E
+    from enlightning_gb300.record import write_mic_files
+    rec = np.zeros(3, _E.MIC_DTYPE)
+    rec["iteration"] = [1, 1, 2]
+    rec["mic"] = [0, 0, 0]
+    rec["level"] = [0, 1, 0]
+    rec["p"] = [101325.0, 101330.5, np.nan]
+    write_mic_files(rec, str(tmp_path), [(0.7, 0.1)], 101325.0, 44100, first_pulse_time=2)
+    assert (tmp_path / "mic-1.txt").read_text() == "1 0 1.013250e+05\n1 1 1.013305e+05\n2 0 nan\n"
+    assert (tmp_path / "mic-1-info.txt").read_text() == (
+        "1\n44100\n(0.7,0.1)\n1 0 1.013250e+05 1.013250e+05\n"
+        "1\n44100\n(0.7,0.1)\n1 1 1.013250e+05 1.013305e+05\n")
