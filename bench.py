@@ -815,7 +815,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="linesource", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--learned", type=int, default=-1,
+                    help="learned switch: 1 on, 0 off, -1 on when the trained network is present (default)")
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--compare-steps", type=int, default=20)
     ap.add_argument("--scale", type=int, default=1, help="shrink the line-source base grid (profiling)")
@@ -823,6 +824,8 @@ def main():
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="engine mode: 0 FP64, 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
     args = ap.parse_args()
+    if args.learned < 0:  # the metric's configuration: batched + learned switch
+        args.learned = int(os.path.exists(os.path.join(ROOT, "enlightning_gb300", "learned_sensor.npz")))
     if args.impl == "reference":
         run_reference(args)
     elif args.workload in ("linesource", "pulses64"):

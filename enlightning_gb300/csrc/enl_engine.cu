@@ -69,6 +69,7 @@ constexpr int kOffMlp = kOffPlanes + kPlanesBytes;
 constexpr int kOffPlanesS = 2 * kBufS;
 constexpr int kOffMlpS = kOffPlanesS + kPlanesBytes;
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
+constexpr int kFeatRows = 32;                    // learned switch: cells per network chunk
 
 // Absorbing envelope (enlightning.C:634-786) as per-level tables: for each
 // side, env[i] = 1 - exp(-ln2 d^2 / w^2) at the distance d of cell centre i
@@ -123,6 +124,8 @@ struct StageArgs {
   float gm1_over_2rho0_f, inv_c_p_f, inv_c_v_f, R_f, inv_rho0_f;  // FP32-storage epilogue
   double a1, a2, bdt, beta;
   const double* dt_dev;  // adaptive time step in device memory (or null)
+  float a1f, a2f, bdtf, betaf;
+  const float* dtf_dev;  // the same time step rounded to float (FP32 storage)
   const int4* tiles;
   const int* ntiles;
   int* counter;
@@ -131,7 +134,7 @@ struct StageArgs {
   AbsorbTables absorb;        // absorbing envelope, applied to each finished cell
   bool any_absorb;
   const int4* patchtab;       // patch boxes of all levels (tile .w = index)
-  const float* mlp;           // learned-sensor parameters (FP32 vector) or null
+  const MlpSmem* mlp;         // learned-sensor network image (global memory) or null
   float margin;               // |p - 0.5| <= margin -> plain sensor decides
   float feat_eps, feat_eps_p, feat_inv_sqrt_eps;
 };
@@ -202,10 +205,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
   unsigned char* dst[2] = {smem_raw, smem_raw + (kF32S ? kBufS : kStageBufBytes)};
   float* tile32_conv = reinterpret_cast<float*>(smem_raw + kOffTile32);  // FP64 storage, FAST
   float* planes = reinterpret_cast<float*>(smem_raw + (kF32S ? kOffPlanesS : kOffPlanes));  // FAST
-  // learned sensor (FAST + hybrid only): network image and feature tile
+  // learned sensor (FAST + hybrid only): features of up to kFeatRows cells
+  // at a time; the network image stays in global memory
   constexpr int kMlpOff = kF32S ? kOffMlpS : kOffMlp;
-  MlpSmem* mlp_s = reinterpret_cast<MlpSmem*>(smem_raw + kMlpOff);
-  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpOff + align128((int)sizeof(MlpSmem)));
+  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpOff);
   __shared__ unsigned char s_flag[256];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
@@ -244,7 +247,6 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
     return;
   }
   const bool learned = FAST && SCHEME == kHybrid && A.mlp != nullptr;
-  if (learned) mlp_stage_params(*mlp_s, A.mlp, tid, 256);
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -276,7 +278,8 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
       break;
     }
     phase[b] ^= 1u;
-    const double bdt = A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt;
+    // beta*dt of this stage (dt from the device CFL reduction when adaptive)
+    const double bdt = kF32S ? 0.0 : (A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt);
     if (FAST && !kF32S) {
       // FP64 box (rows of kBW) -> FP32 perturbations (rows of kBW32)
       for (int e = tid; e < kTileElems; e += 256) {
@@ -320,6 +323,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
     const int cc32 = (ty + 3) * kBW32 + (tx + 3);
     int flag = 0;
     int fallback = 0;
+    bool reviewed = false;  // the learned switch looked at this tile (block-uniform)
     if (learned && lvl == 0) {
       // learned switch: it refines the plain one and can only send cells the
       // plain switch puts on WENO back to DRP.  Those cells are compacted,
@@ -331,41 +335,48 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         SAcc32R acc{acc32(tile32, planes, tx, ty)};
         plain = sensor_fast(acc, A.F[lvl]);
       }
-      const unsigned bf = __ballot_sync(0xffffffffu, plain);
-      if (lane == 0) s_cnt[0][warp] = __popc(bf);
-      __syncthreads();
-      int nflag = 0, slot = 0;
+      const int nflag = __syncthreads_count(plain);
+      reviewed = nflag > 0;
+      int slot = 0;
+      if (reviewed) {  // slots of the flagged cells in tile order
+        const unsigned bf = __ballot_sync(0xffffffffu, plain);
+        if (lane == 0) s_cnt[0][warp] = __popc(bf);
+        __syncthreads();
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (q < warp) slot += s_cnt[0][q];
-        nflag += s_cnt[0][q];
+        for (int q = 0; q < 8; ++q)
+          if (q < warp) slot += s_cnt[0][q];
+        slot += __popc(bf & ((1u << lane) - 1u));
       }
-      slot += __popc(bf & ((1u << lane) - 1u));
-      if (nflag > 0) {
-        if (plain) {
+      // chunks of kFeatRows cells: features by the owning threads, then one
+      // warp per 16 cells through the network
+      for (int c0 = 0; c0 < nflag; c0 += kFeatRows) {
+        if (plain && slot >= c0 && slot < c0 + kFeatRows) {
           float fv[kFeat];
           SAcc32R acc{acc32(tile32, planes, tx, ty)};
           cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
 #pragma unroll
           for (int q = 0; q < kFeat; q += 2)
-            *reinterpret_cast<uint32_t*>(feat + slot * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
-          s_list[slot] = tid;
+            *reinterpret_cast<uint32_t*>(feat + (slot - c0) * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
+          s_list[slot - c0] = tid;
         }
         __syncthreads();
-        for (int g0 = warp * 16; g0 < nflag; g0 += 8 * 16) {
+        const int g0 = warp * 16;
+        if (g0 < kFeatRows && c0 + g0 < nflag) {
           MlpFwd16 F;
-          mlp_forward16(*mlp_s, feat + g0 * kFeat, kFeat, lane, F);
+          mlp_forward16(*A.mlp, feat + g0 * kFeat, kFeat, lane, F);
           if ((lane & 3) == 0) {
 #pragma unroll
             for (int hh = 0; hh < 2; ++hh) {
               const int sl = g0 + (lane >> 2) + 8 * hh;
-              if (sl < nflag)
+              if (c0 + sl < nflag)
                 s_flag[s_list[sl]] =
                     (unsigned char)(F.logit[hh] > 0.f ? 2 : 1) | (fabsf(F.logit[hh]) <= A.margin ? 4 : 0);
             }
           }
         }
         __syncthreads();
+      }
+      if (nflag > 0) {
         if (plain) {
           const unsigned char d = s_flag[tid];
           if (d & 4) {
@@ -385,7 +396,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         flag = rhs_switch<SCHEME, ORDER, LLF>(acc, A.P[lvl]);
       }
     }
-    const int nfb = learned ? __syncthreads_count(fallback) : 0;
+    const int nfb = reviewed ? __syncthreads_count(fallback) : 0;
     // compaction: DRP cells first, then WENO cells, each in tile order
     unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
     unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
@@ -404,7 +415,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
       nd += s_cnt[0][q];
       nw += s_cnt[1][q];
     }
-    if (valid) {
+    // a tile without WENO cells keeps its natural order (no list, no barrier)
+    const bool direct = nw == 0;
+    if (valid && !direct) {
       unsigned lt = (1u << lane) - 1u;
       int pos = flag ? (nd + ow + __popc(bw & lt)) : (od + __popc(bd & lt));
       s_list[pos] = (ty << 5) | tx | (flag << 16);
@@ -414,9 +427,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
       atomicAdd(&A.stats[3 * lvl + 1], (unsigned long long)(nd + nw));
       if (nfb) atomicAdd(&A.stats[3 * lvl + 2], (unsigned long long)nfb);
     }
-    __syncthreads();
-    if (tid < nd + nw) {
-      const int e = s_list[tid];
+    if (!direct) __syncthreads();
+    if (direct ? valid : (tid < nd + nw)) {
+      const int e = direct ? ((ty << 5) | tx) : s_list[tid];
       const int cx = e & 31, cy = (e >> 5) & 0xff, f = (e >> 16) & 1;
       const int c2 = (cy + 3) * kBW + (cx + 3);
       const int c32 = (cy + 3) * kBW32 + (cx + 3);
@@ -435,7 +448,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         H[0] = h0b[ci];
         sources_fast(acc, A.F[lvl], H);
         fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
-        const float a1 = (float)A.a1, a2 = (float)A.a2, bdtf = (float)bdt;
+        const float a1 = A.a1f, a2 = A.a2f, bdtf = A.dtf_dev ? A.betaf * (*A.dtf_dev) : A.bdtf;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
           const float w = tile32[k * kPlane32 + c32];
@@ -670,28 +683,32 @@ __device__ __forceinline__ void refine_weights(int I, int r, int& ic, S& f) {
   f = xc - fl;
 }
 
+// One thread per halo cell: segment q of the level covers cells
+// [segs[q].w, segs[q].w + length) of the level's halo, found by binary
+// search, so short segments (the 3-cell rows beside a patch) keep every lane
+// busy and each thread has its 4 x nfields loads in flight together.
 template <typename S>
 __global__ void interp_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4* segs, const int* meta, int moff,
-                              int mcnt, int nfields) {
-  const int off = meta[moff], cnt = meta[mcnt];
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  for (int s = gw; s < cnt; s += warps) {
-    int4 sg = segs[off + s];
-    int J = sg.x;
-    int jc;
-    S fy;
+                              int mcnt, int mncell, int nfields) {
+  const int off = meta[moff], cnt = meta[mcnt], ncell = meta[mncell];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += gridDim.x * blockDim.x) {
+    int lo = 0, hi = cnt - 1;  // last segment with .w <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[off + mid].w <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const int4 sg = segs[off + lo];
+    const int J = sg.x, I = sg.y + (t - sg.w);
+    int jc, ic;
+    S fy, fx;
     refine_weights(J, ratio, jc, fy);
-    for (int I = sg.y + lane; I <= sg.z; I += 32) {
-      int ic;
-      S fx;
-      refine_weights(I, ratio, ic, fx);
-      for (int k = 0; k < nfields; ++k) {
-        S c00 = C.at(k, ic, jc), c10 = C.at(k, ic + 1, jc), c01 = C.at(k, ic, jc + 1), c11 = C.at(k, ic + 1, jc + 1);
-        S lo = ((S)1 - fx) * c00 + fx * c10;
-        S hi = ((S)1 - fx) * c01 + fx * c11;
-        F.at(k, I, J) = ((S)1 - fy) * lo + fy * hi;
-      }
+    refine_weights(I, ratio, ic, fx);
+    for (int k = 0; k < nfields; ++k) {
+      S c00 = C.at(k, ic, jc), c10 = C.at(k, ic + 1, jc), c01 = C.at(k, ic, jc + 1), c11 = C.at(k, ic + 1, jc + 1);
+      S lo_ = ((S)1 - fx) * c00 + fx * c10;
+      S hi_ = ((S)1 - fx) * c01 + fx * c11;
+      F.at(k, I, J) = ((S)1 - fy) * lo_ + fy * hi_;
     }
   }
 }
@@ -1026,11 +1043,12 @@ __global__ void speed_kernel(SpeedArgs<S> A) {
   }
 }
 
-__global__ void dt_kernel(unsigned long long* smax_bits, double* dt, double* time, double cfl_dxmin,
+__global__ void dt_kernel(unsigned long long* smax_bits, double* dt, double* time, float* dt_f, double cfl_dxmin,
                           double dt_max) {
   double smax = __longlong_as_double((long long)*smax_bits);
   double d = smax > 0.0 ? cfl_dxmin / smax : dt_max;
   *dt = fmin(d, dt_max);
+  *dt_f = (float)*dt;  // for the FP32 stage epilogue
   *time += *dt;
   *smax_bits = 0ull;
 }
@@ -1257,7 +1275,8 @@ enum {
   M_CT_OFF = 1 + 2 * kL,
   M_CT_CNT = 1 + 3 * kL,
   M_PATCH_OFF = 1 + 4 * kL,  // kL + 1 entries: first patch-table index of each level, then the total
-  M_SIZE = 2 + 5 * kL
+  M_HALO_NCELL = 2 + 5 * kL,  // +level: halo cells to interpolate
+  M_SIZE = 2 + 6 * kL
 };
 
 template <typename T>
@@ -1299,7 +1318,7 @@ struct Engine {
   size_t bmap_cap = 0;
   double* d_segs = nullptr;
   size_t segs_cap = 0;
-  float* d_mlp = nullptr;    // learned-sensor parameters
+  MlpSmem* d_mlp = nullptr;  // learned-sensor network image (BF16 transposed weights)
   float margin = 0.f;
   int adaptive = 0;          // device-computed dt
   double cfl = 0.5;
@@ -1434,6 +1453,12 @@ static int rebuild_tables(Engine* E) {
     E->h_meta[M_HALO_OFF + l] = (int)E->h_halo.size();
     if (l > 0) halo_segments(E->lev[l].patches, E->lev[l].nx, E->lev[l].ny, E->h_halo);
     E->h_meta[M_HALO_CNT + l] = (int)E->h_halo.size() - E->h_meta[M_HALO_OFF + l];
+    int ncell = 0;  // .w = halo cells of the level before this segment
+    for (size_t q = E->h_meta[M_HALO_OFF + l]; q < E->h_halo.size(); ++q) {
+      E->h_halo[q].w = ncell;
+      ncell += E->h_halo[q].z - E->h_halo[q].y + 1;
+    }
+    E->h_meta[M_HALO_NCELL + l] = ncell;
     E->h_meta[M_CT_OFF + l] = (int)E->h_ctiles.size();
     if (l > 0) {
       int r = E->cfg.ratio;
@@ -1553,6 +1578,11 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.R_f = (float)c.R;
   A.inv_rho0_f = (float)(1.0 / c.rho0);
   A.dt_dev = E->adaptive ? E->d_dt : nullptr;
+  A.dtf_dev = E->adaptive ? reinterpret_cast<const float*>(E->d_dt + 2) : nullptr;
+  A.a1f = (float)A.a1;
+  A.a2f = (float)A.a2;
+  A.betaf = (float)A.beta;
+  A.bdtf = (float)A.bdt;
   A.absorb = absorb_tables(E);
   A.any_absorb = any_absorb(E);
   A.patchtab = E->d_patchtab.p;
@@ -1561,7 +1591,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.counter = E->d_counters + stage;
   A.health = E->d_health;
   A.stats = E->d_stats;
-  A.mlp = (E->cfg.learned && E->cfg.precision != ENL_PREC_FP64) ? E->d_mlp : nullptr;
+  A.mlp = (E->cfg.learned && E->cfg.precision != ENL_PREC_FP64) ? E->d_mlp : nullptr;  // null until set_mlp
   A.margin = E->margin;
   A.feat_eps = (float)A.P[0].sensor_eps;
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
@@ -1599,7 +1629,8 @@ static int fill_level(Engine* E, int l, int which) {
   Level& L = E->lev[l];
   if (l > 0) {
     interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(which), c.ratio,
-                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l, kNF);
+                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l,
+                                                M_HALO_NCELL + l, kNF);
   }
   if (c.independent) {
     if (E->patch_cnt[l])
@@ -1725,7 +1756,7 @@ static void adaptive_dt(Engine* E, double dt_max) {
   if (!E->adaptive) return;
   if (E->f32s) speed_t<float>(E);
   else speed_t<double>(E);
-  dt_kernel<<<1, 1, 0, stream()>>>(E->d_smax, E->d_dt, E->d_dt + 1, E->cfl * finest_dx(E), dt_max);
+  dt_kernel<<<1, 1, 0, stream()>>>(E->d_smax, E->d_dt, E->d_dt + 1, reinterpret_cast<float*>(E->d_dt + 2), E->cfl * finest_dx(E), dt_max);
 }
 
 template <typename S>
@@ -1958,14 +1989,14 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMemset(E->d_health, 0, sizeof(int));
   cudaMalloc(&E->d_stats, 3 * kL * sizeof(unsigned long long));
   cudaMemset(E->d_stats, 0, 3 * kL * sizeof(unsigned long long));
-  cudaMalloc(&E->d_dt, 2 * sizeof(double));
-  cudaMemset(E->d_dt, 0, 2 * sizeof(double));
+  cudaMalloc(&E->d_dt, 3 * sizeof(double));  // dt, simulated time, dt as float
+  cudaMemset(E->d_dt, 0, 3 * sizeof(double));
   cudaMalloc(&E->d_smax, sizeof(unsigned long long));
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
   if (E->f32s) E->smem_bytes = kOffMlpS;
   else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kOffMlp : 2 * kStageBufBytes;
   if (cfg->precision != ENL_PREC_FP64 && cfg->learned)
-    E->smem_bytes += align128((int)sizeof(MlpSmem)) + 256 * kFeat * sizeof(__nv_bfloat16);
+    E->smem_bytes += align128(kFeatRows * kFeat * (int)sizeof(__nv_bfloat16));
   StageFn fn = pick_stage(cfg->precision, cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
   int per_sm = 0;
@@ -2572,12 +2603,14 @@ int enl_engine_set_mlp(void* e, const float* params_host, float margin) {
     set_error(ENL_ERR_STATE);
     return ENL_ERR_STATE;
   }
-  if (!E->d_mlp && cudaMalloc(&E->d_mlp, kNParams * sizeof(float)) != cudaSuccess) {
+  if (!E->d_mlp && cudaMalloc(&E->d_mlp, sizeof(MlpSmem)) != cudaSuccess) {
     E->d_mlp = nullptr;
     set_error(ENL_ERR_CUDA);
     return ENL_ERR_CUDA;
   }
-  cudaMemcpyAsync(E->d_mlp, params_host, kNParams * sizeof(float), cudaMemcpyHostToDevice, stream());
+  MlpSmem img;
+  mlp_build_image(params_host, img);
+  cudaMemcpyAsync(E->d_mlp, &img, sizeof(MlpSmem), cudaMemcpyHostToDevice, stream());
   cudaStreamSynchronize(stream());
   if (E->margin != margin) E->graph_valid = false;  // the margin is a kernel argument
   E->margin = margin;

@@ -33,6 +33,22 @@ struct MlpSmem {
   float b3;
 };
 
+// The same image built on the host (the stage kernel reads it from global
+// memory through L1: the network runs on few cells, and keeping it out of
+// shared memory keeps three stage blocks per SM).
+inline void mlp_build_image(const float* P, MlpSmem& S) {
+  for (int n = 0; n < kHid; ++n)
+    for (int k = 0; k < kFeatPad; ++k) S.w1t[n][k] = __float2bfloat16_rn(k < kFeat ? P[kOffW1 + k * kHid + n] : 0.0f);
+  for (int n = 0; n < kHid; ++n)
+    for (int k = 0; k < kHid; ++k) S.w2t[n][k] = __float2bfloat16_rn(P[kOffW2 + k * kHid + n]);
+  for (int e = 0; e < kHid; ++e) {
+    S.b1[e] = P[kOffB1 + e];
+    S.b2[e] = P[kOffB2 + e];
+    S.w3[e] = __bfloat162float(__float2bfloat16_rn(P[kOffW3 + e]));
+  }
+  S.b3 = P[kOffB3];
+}
+
 __device__ __forceinline__ void mlp_stage_params(MlpSmem& S, const float* __restrict__ P, int tid, int nthr) {
   for (int e = tid; e < kHid * kFeatPad; e += nthr) {
     int n = e / kFeatPad, k = e % kFeatPad;

@@ -154,10 +154,10 @@ def logits(X, params):
 
 def harvest_line_source(H, seeds, steps=30, every=10, keep0=0.0, prm=None, log=None, **kw):
     from . import workloads
-    from .engine import PREC_FP32
+    from .engine import PREC_FP32_STATE
     prm = prm or default_params()
     for sd in seeds:
-        E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32, **kw)
+        E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32_STATE, **kw)
         for s in range(steps):
             if s and s % 10 == 0:
                 Hy.regrid()
@@ -174,7 +174,8 @@ def harvest_shock(H, seeds, steps=40, every=10, keep0=0.0, prm=None, log=None, *
     from . import workloads
     prm = prm or default_params()
     for sd in seeds:
-        E, Hy = workloads.mach_shock(prm, seed=sd, **kw)
+        from .engine import PREC_FP32_STATE
+        E, Hy = workloads.mach_shock(prm, seed=sd, precision=PREC_FP32_STATE, **kw)
         for s in range(steps):
             if s and s % 10 == 0:
                 Hy.regrid()
@@ -192,13 +193,13 @@ def evaluate(params, margin, seeds=(100, 101, 102, 103, 104), steps=40, prm=None
     WENO fractions (level 0 and all levels), fallback fraction, and the
     relative L2 difference of the final level-0 states."""
     from . import workloads
-    from .engine import PREC_FP32
+    from .engine import PREC_FP32_STATE
     prm = prm or default_params()
     rows = []
     for sd in seeds:
         res = {}
         for learned in (False, True):
-            E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32, learned=learned, **kw)
+            E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32_STATE, learned=learned, **kw)
             if learned:
                 E.set_mlp(params, margin)
             E.stats()
