@@ -88,19 +88,46 @@ struct AbsorbTables {
 // (i, j) of patch b is reached follows from its neighbour towards the side:
 // the walk is evaluated per cell.  The sides that reach the cell are returned
 // (0..3 = L, R, B, T) in the reference's order.
+// `mask` (bit s = side s) limits the walk to the sides that can reach the
+// cell's tile (absorb_tile_mask).
 __device__ __forceinline__ int absorb_walk(const AbsorbTables& T, int lvl, int i, int j, const int4& b,
-                                           int q[4]) {
+                                           int q[4], int mask = 15) {
   int n = 0;
   const unsigned char* c = T.cont[lvl][0];
-  if (c && (j != b.z || c[b.x]) && (i == b.x || c[i - 1])) q[n++] = 0;
+  if ((mask & 1) && c && (j != b.z || c[b.x]) && (i == b.x || c[i - 1])) q[n++] = 0;
   c = T.cont[lvl][1];
-  if (c && (j != b.z || c[b.y]) && (i == b.y || c[i + 1])) q[n++] = 1;
+  if ((mask & 2) && c && (j != b.z || c[b.y]) && (i == b.y || c[i + 1])) q[n++] = 1;
   c = T.cont[lvl][2];
-  if (c && c[b.z] && (j == b.z || c[j - 1])) q[n++] = 2;
+  if ((mask & 4) && c && c[b.z] && (j == b.z || c[j - 1])) q[n++] = 2;
   c = T.cont[lvl][3];
-  if (c && c[b.w] && (j == b.w || c[j + 1])) q[n++] = 3;
+  if ((mask & 8) && c && c[b.w] && (j == b.w || c[j + 1])) q[n++] = 3;
   return n;
 }
+
+// Sides whose walk can reach some cell of the w x h tile at (i0, j0) of patch
+// b: the continuation tests are monotone, so the tile's cell nearest to each
+// side decides.
+__device__ __forceinline__ int absorb_tile_mask(const AbsorbTables& T, int lvl, int i0, int j0, int w, int h,
+                                                const int4& b) {
+  int m = 0;
+  const unsigned char* c = T.cont[lvl][0];
+  if (c && (i0 == b.x || c[i0 - 1])) m |= 1;
+  c = T.cont[lvl][1];
+  if (c && (i0 + w - 1 == b.y || c[i0 + w])) m |= 2;
+  c = T.cont[lvl][2];
+  if (c && c[b.z] && (j0 == b.z || c[j0 - 1])) m |= 4;
+  c = T.cont[lvl][3];
+  if (c && c[b.w] && (j0 + h - 1 == b.w || c[j0 + h])) m |= 8;
+  return m;
+}
+
+// Per-tile values computed once by thread 0 and read by every thread after
+// the next barrier.
+struct TileInfo {
+  int4 box;       // the tile's patch
+  int absorb;     // absorb_tile_mask
+  float bdtf;     // beta * dt in single precision
+};
 
 // (q - ambient) * tmp + ambient, rounding like the reference's statement
 __device__ __forceinline__ double relax_(double q, double amb, double tmp) {
@@ -214,6 +241,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
   __shared__ int s_t[2];
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
+  __shared__ TileInfo s_tile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ntiles = *A.ntiles;
   auto issue = [&](int t, int b) {
@@ -280,6 +308,12 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
     phase[b] ^= 1u;
     // beta*dt of this stage (dt from the device CFL reduction when adaptive)
     const double bdt = kF32S ? 0.0 : (A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt);
+    if (tid == 0) {
+      const int4 pb = A.patchtab[td.w];
+      s_tile.box = pb;
+      s_tile.absorb = A.any_absorb ? absorb_tile_mask(A.absorb, lvl, i0, j0, w, h, pb) : 0;
+      s_tile.bdtf = A.dtf_dev ? A.betaf * (*A.dtf_dev) : A.bdtf;
+    }
     if (FAST && !kF32S) {
       // FP64 box (rows of kBW) -> FP32 perturbations (rows of kBW32)
       for (int e = tid; e < kTileElems; e += 256) {
@@ -322,72 +356,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
     const int cc = (ty + 3) * kBW + (tx + 3);
     const int cc32 = (ty + 3) * kBW32 + (tx + 3);
     int flag = 0;
-    int fallback = 0;
-    bool reviewed = false;  // the learned switch looked at this tile (block-uniform)
-    if (learned && lvl == 0) {
-      // learned switch: it refines the plain one and can only send cells the
-      // plain switch puts on WENO back to DRP.  Those cells are compacted,
-      // their features go through the BF16 MLP on the tensor cores (one warp
-      // per 16 cells), and cells with |logit| <= margin keep the plain
-      // decision.  Tiles without such cells skip the network.
-      int plain = 0;
-      if (valid) {
-        SAcc32R acc{acc32(tile32, planes, tx, ty)};
-        plain = sensor_fast(acc, A.F[lvl]);
-      }
-      const int nflag = __syncthreads_count(plain);
-      reviewed = nflag > 0;
-      int slot = 0;
-      if (reviewed) {  // slots of the flagged cells in tile order
-        const unsigned bf = __ballot_sync(0xffffffffu, plain);
-        if (lane == 0) s_cnt[0][warp] = __popc(bf);
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if (q < warp) slot += s_cnt[0][q];
-        slot += __popc(bf & ((1u << lane) - 1u));
-      }
-      // chunks of kFeatRows cells: features by the owning threads, then one
-      // warp per 16 cells through the network
-      for (int c0 = 0; c0 < nflag; c0 += kFeatRows) {
-        if (plain && slot >= c0 && slot < c0 + kFeatRows) {
-          float fv[kFeat];
-          SAcc32R acc{acc32(tile32, planes, tx, ty)};
-          cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
-#pragma unroll
-          for (int q = 0; q < kFeat; q += 2)
-            *reinterpret_cast<uint32_t*>(feat + (slot - c0) * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
-          s_list[slot - c0] = tid;
-        }
-        __syncthreads();
-        const int g0 = warp * 16;
-        if (g0 < kFeatRows && c0 + g0 < nflag) {
-          MlpFwd16 F;
-          mlp_forward16(*A.mlp, feat + g0 * kFeat, kFeat, lane, F);
-          if ((lane & 3) == 0) {
-#pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-              const int sl = g0 + (lane >> 2) + 8 * hh;
-              if (c0 + sl < nflag)
-                s_flag[s_list[sl]] =
-                    (unsigned char)(F.logit[hh] > 0.f ? 2 : 1) | (fabsf(F.logit[hh]) <= A.margin ? 4 : 0);
-            }
-          }
-        }
-        __syncthreads();
-      }
-      if (nflag > 0) {
-        if (plain) {
-          const unsigned char d = s_flag[tid];
-          if (d & 4) {
-            flag = 1;
-            fallback = 1;
-          } else {
-            flag = (d & 2) ? 1 : 0;
-          }
-        }
-      }
-    } else if (valid) {
+    if (valid) {
       if (FAST) {
         SAcc32R acc{acc32(tile32, planes, tx, ty)};
         flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
@@ -396,8 +365,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         flag = rhs_switch<SCHEME, ORDER, LLF>(acc, A.P[lvl]);
       }
     }
-    const int nfb = reviewed ? __syncthreads_count(fallback) : 0;
-    // compaction: DRP cells first, then WENO cells, each in tile order
+    // compaction counts: DRP cells first, then WENO cells, each in tile order
     unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
     unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
     if (lane == 0) {
@@ -414,6 +382,67 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
       }
       nd += s_cnt[0][q];
       nw += s_cnt[1][q];
+    }
+    int nfb = 0;
+    if (learned && lvl == 0 && nw > 0) {
+      // learned switch: it refines the plain one and can only send cells the
+      // plain switch put on WENO back to DRP.  Those cells (numbered in tile
+      // order by the counts above) go through the BF16 MLP on the tensor
+      // cores in chunks of kFeatRows, one warp per 16 cells; cells with
+      // |logit| <= margin keep the plain decision.  Tiles without such cells
+      // (almost all) pay nothing: the counts above were needed anyway.
+      const int slot = ow + __popc(bw & ((1u << lane) - 1u));
+      for (int c0 = 0; c0 < nw; c0 += kFeatRows) {
+        if (valid && flag && slot >= c0 && slot < c0 + kFeatRows) {
+          float fv[kFeat];
+          SAcc32R acc{acc32(tile32, planes, tx, ty)};
+          cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
+#pragma unroll
+          for (int q = 0; q < kFeat; q += 2)
+            *reinterpret_cast<uint32_t*>(feat + (slot - c0) * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
+          s_list[slot - c0] = tid;
+        }
+        __syncthreads();
+        const int g0 = warp * 16;
+        if (g0 < kFeatRows && c0 + g0 < nw) {
+          float logit[2];
+          mlp_logits16(*A.mlp, feat + g0 * kFeat, kFeat, lane, logit);
+          if ((lane & 3) == 0) {
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const int sl = g0 + (lane >> 2) + 8 * hh;
+              if (c0 + sl < nw)
+                s_flag[s_list[sl]] =
+                    (unsigned char)(logit[hh] > 0.f ? 2 : 1) | (fabsf(logit[hh]) <= A.margin ? 4 : 0);
+            }
+          }
+        }
+        __syncthreads();
+      }
+      int fallback = 0;
+      if (valid && flag) {
+        const unsigned char d = s_flag[tid];
+        if (d & 4) fallback = 1;       // plain decision (WENO) kept
+        else flag = (d & 2) ? 1 : 0;
+      }
+      nfb = __syncthreads_count(fallback);  // also orders the counts' reuse below
+      bd = __ballot_sync(0xffffffffu, valid && !flag);
+      bw = __ballot_sync(0xffffffffu, valid && flag);
+      if (lane == 0) {
+        s_cnt[0][warp] = __popc(bd);
+        s_cnt[1][warp] = __popc(bw);
+      }
+      __syncthreads();
+      nd = nw = od = ow = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (q < warp) {
+          od += s_cnt[0][q];
+          ow += s_cnt[1][q];
+        }
+        nd += s_cnt[0][q];
+        nw += s_cnt[1][q];
+      }
     }
     // a tile without WENO cells keeps its natural order (no list, no barrier)
     const bool direct = nw == 0;
@@ -448,7 +477,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         H[0] = h0b[ci];
         sources_fast(acc, A.F[lvl], H);
         fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
-        const float a1 = A.a1f, a2 = A.a2f, bdtf = A.dtf_dev ? A.betaf * (*A.dtf_dev) : A.bdtf;
+        const float a1 = A.a1f, a2 = A.a2f, bdtf = s_tile.bdtf;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
           const float w = tile32[k * kPlane32 + c32];
@@ -466,9 +495,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         const float x = (s + A.R_f * log1pf(rp * A.inv_rho0_f)) * A.inv_c_v_f;
         float tp = F.T0 * expm1f(x);
         float pq = pp;
-        if (A.any_absorb) {  // perturbations relax towards 0
+        if (s_tile.absorb) {  // perturbations relax towards 0
           int side[4];
-          const int na = absorb_walk(A.absorb, lvl, gi, gj, A.patchtab[td.w], side);
+          const int na = absorb_walk(A.absorb, lvl, gi, gj, s_tile.box, side, s_tile.absorb);
           for (int q = 0; q < na; ++q) {
             const float t_ = A.absorb.envf[lvl][side[q]][side[q] < 2 ? gi : gj];
 #pragma unroll
@@ -529,10 +558,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
           pv = __dadd_rn(__dmul_rn(__dmul_rn(cc_, cc_), inner), A.p0);
           tv = A.T0 * exp((s - A.R * log(A.rho0 / wn[0])) / A.c_v);
         }
-        if (A.any_absorb) {  // absolute values relax towards the ambient state
+        if (s_tile.absorb) {  // absolute values relax towards the ambient state
           int side[4];
           double fa[4];
-          const int na = absorb_walk(A.absorb, lvl, gi, gj, A.patchtab[td.w], side);
+          const int na = absorb_walk(A.absorb, lvl, gi, gj, s_tile.box, side, s_tile.absorb);
           for (int q = 0; q < na; ++q) fa[q] = A.absorb.env[lvl][side[q]][side[q] < 2 ? gi : gj];
           const double rT = __dmul_rn(A.T0, A.rho0);
           for (int q = 0; q < na; ++q) {

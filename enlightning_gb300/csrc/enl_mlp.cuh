@@ -158,6 +158,68 @@ __device__ __forceinline__ void mlp_forward16(const MlpSmem& S, const __nv_bfloa
   F.logit[1] = s1 + S.b3;
 }
 
+// Inference only, with the same arithmetic as mlp_forward16 (the same
+// accumulation orders, so the same logits) and fewer live registers: the
+// hidden layer is packed into BF16 A fragments before the second layer, which
+// then runs one n-tile at a time into the logit sums.
+__device__ __forceinline__ void mlp_logits16(const MlpSmem& S, const __nv_bfloat16* X, int ldx, int lane,
+                                             float logit[2]) {
+  const int g = lane >> 2, t = lane & 3;
+  uint32_t h[4][4];  // gelu(layer 1) as A fragments, k-chunks of 16
+  {
+    float z1[8][4];
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) z1[n][q] = S.b1[n * 8 + 2 * t + (q & 1)];
+#pragma unroll
+    for (int kc = 0; kc < 3; ++kc) {
+      int c0 = kc * 16 + 2 * t, c1 = c0 + 8;
+      uint32_t a0 = c0 < kFeat ? ld_pair(X + g * ldx + c0) : 0u;
+      uint32_t a1 = c0 < kFeat ? ld_pair(X + (g + 8) * ldx + c0) : 0u;
+      uint32_t a2 = c1 < kFeat ? ld_pair(X + g * ldx + c1) : 0u;
+      uint32_t a3 = c1 < kFeat ? ld_pair(X + (g + 8) * ldx + c1) : 0u;
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        uint32_t b0 = ld_pair(&S.w1t[n * 8 + g][kc * 16 + 2 * t]);
+        uint32_t b1 = ld_pair(&S.w1t[n * 8 + g][kc * 16 + 2 * t + 8]);
+        mma_bf16(z1[n], a0, a1, a2, a3, b0, b1);
+      }
+    }
+#pragma unroll
+    for (int kc = 0; kc < 4; ++kc) {
+      h[kc][0] = pack_bf16(gelu(z1[2 * kc][0]), gelu(z1[2 * kc][1]));
+      h[kc][1] = pack_bf16(gelu(z1[2 * kc][2]), gelu(z1[2 * kc][3]));
+      h[kc][2] = pack_bf16(gelu(z1[2 * kc + 1][0]), gelu(z1[2 * kc + 1][1]));
+      h[kc][3] = pack_bf16(gelu(z1[2 * kc + 1][2]), gelu(z1[2 * kc + 1][3]));
+    }
+  }
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    float z2[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) z2[q] = S.b2[n * 8 + 2 * t + (q & 1)];
+#pragma unroll
+    for (int kc = 0; kc < 4; ++kc) {
+      uint32_t b0 = ld_pair(&S.w2t[n * 8 + g][kc * 16 + 2 * t]);
+      uint32_t b1 = ld_pair(&S.w2t[n * 8 + g][kc * 16 + 2 * t + 8]);
+      mma_bf16(z2, h[kc][0], h[kc][1], h[kc][2], h[kc][3], b0, b1);
+    }
+    int col = n * 8 + 2 * t;
+    s0 += __bfloat162float(__float2bfloat16_rn(gelu(z2[0]))) * S.w3[col] +
+          __bfloat162float(__float2bfloat16_rn(gelu(z2[1]))) * S.w3[col + 1];
+    s1 += __bfloat162float(__float2bfloat16_rn(gelu(z2[2]))) * S.w3[col] +
+          __bfloat162float(__float2bfloat16_rn(gelu(z2[3]))) * S.w3[col + 1];
+  }
+  s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+  s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+  s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+  s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+  logit[0] = s0 + S.b3;
+  logit[1] = s1 + S.b3;
+}
+
 // ------------------------------------------------------------------------
 // Features of one cell (40 values) from an FP32 perturbation accessor:
 // for each direction (x, y) and each stencil offset m = -2..2:
