@@ -746,19 +746,21 @@ def run_linesource(args):
     # 320 B per RK3 cell-update with FP64 fields; FP32 storage moves half of it
     bytes_per_cell_launch = STEP_BYTES_PER_CELL / 3.0 * esize / 8.0
     achieved = cells_per_launch * bytes_per_cell_launch / (per_launch_ms * 1e-3) / 1e9
-    # e2e: hierarchy state through the public API from pinned host memory
-    n = wl.fast.packed_size()
-    host = wl.fast.packed_host(pin=True)
-    wl.fast.download(host)
+    # e2e: the conserved hierarchy state (5 fields of every patch interior)
+    # through the public API from pinned host memory; p and T are recomputed
+    # on the device after each upload
+    host = wl.fast.state_host(pin=True)
+    n = host.numel()
+    wl.fast.download_state(host)
     barrier()
     ke = max(1, min(args.steps, 10))
     q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     q0.record()
     cue = 0
     for _ in range(ke):
-        wl.fast.upload(host)
+        wl.fast.upload_state(host)
         cue += wl.advance("fast", 1, use_graph=True)
-        wl.fast.download(host)
+        wl.fast.download_state(host)
     q1.record()
     barrier()
     e2e_value = cue * ws / (q0.elapsed_time(q1) * 1e-3)

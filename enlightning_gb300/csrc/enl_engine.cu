@@ -134,6 +134,44 @@ __device__ __forceinline__ double relax_(double q, double amb, double tmp) {
   return __dadd_rn(__dmul_rn(__dsub_rn(q, amb), tmp), amb);
 }
 
+// update_state (update_state.m4:90-105) on absolute FP64 values, with the
+// reference's rounding; height = centre height of the cell row.
+struct EosConst64 {
+  double rho0, c, c_lr, gm1_over_2rho0, c_p, p0, T0, c_v, R;
+};
+__device__ __forceinline__ void eos_abs64(const EosConst64& E, double w0, double w3, double height, double& p,
+                                          double& T) {
+  const double cc = __dadd_rn(E.c, __dmul_rn(E.c_lr, height));
+  const double d = __dsub_rn(w0, E.rho0);
+  const double s = __ddiv_rn(w3, w0);
+  const double inner =
+      __dadd_rn(__dadd_rn(d, __dmul_rn(E.gm1_over_2rho0, __dmul_rn(d, d))), __dmul_rn(__ddiv_rn(w0, E.c_p), s));
+  p = __dadd_rn(__dmul_rn(__dmul_rn(cc, cc), inner), E.p0);
+  T = E.T0 * exp((s - E.R * log(E.rho0 / w0)) / E.c_v);
+}
+
+// The same in single-precision perturbation form: rp = rho - rho0, w3 = rho s;
+// returns p - p0 and T - T0 (log1p/expm1 keep small perturbations exact).
+struct EosConst32 {
+  float rho0, c, c_lr, gm1_over_2rho0, inv_c_p, T0, inv_c_v, R, inv_rho0;
+};
+// Every operation is explicitly rounded, so the result does not depend on
+// how the compiler contracts it at each call site (the stage epilogue and the
+// state upload must agree bit for bit).
+__device__ __forceinline__ void eos_pert32(const EosConst32& E, float rp, float w3, float height, float& pp,
+                                           float& tp) {
+  const float s = __fmul_rn(w3, rcp_approx(__fadd_rn(E.rho0, rp)));
+  const float ccl = __fmaf_rn(E.c_lr, height, E.c);
+  const float inner = __fadd_rn(__fmaf_rn(E.gm1_over_2rho0, __fmul_rn(rp, rp), rp), __fmul_rn(w3, E.inv_c_p));
+  pp = __fmul_rn(__fmul_rn(ccl, ccl), inner);
+  const float x = __fmul_rn(__fmaf_rn(E.R, log1pf(__fmul_rn(rp, E.inv_rho0)), s), E.inv_c_v);
+  tp = __fmul_rn(E.T0, expm1f(x));
+}
+// Centre height of cell row j in single precision.
+__device__ __forceinline__ float row_height32(float ylo, float dy, int j) {
+  return __fmaf_rn(dy, __fadd_rn((float)j, 0.5f), ylo);
+}
+
 struct StageArgs {
   CUtensorMap tmap[kL];     // input buffer, per level (halo box)
   CUtensorMap tmap_un[kL];  // FP32 storage: u^n interior box
@@ -148,7 +186,7 @@ struct StageArgs {
   RhsConst P[kL];
   FastConst F[kL];
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
-  float gm1_over_2rho0_f, inv_c_p_f, inv_c_v_f, R_f, inv_rho0_f;  // FP32-storage epilogue
+  EosConst32 E32;  // FP32-storage epilogue
   double a1, a2, bdt, beta;
   const double* dt_dev;  // adaptive time step in device memory (or null)
   float a1f, a2f, bdtf, betaf;
@@ -486,15 +524,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         }
         // update_state in perturbation form (update_state.m4:90-105)
         const FastConst& F = A.F[lvl];
-        const float rp = wn[0];
-        const float rho = F.rho0 + rp;
-        const float s = wn[3] * rcp_approx(rho);
-        const float hgt = F.ylo + F.dy * ((float)gj + 0.5f);
-        const float ccl = F.c + F.c_lr * hgt;
-        const float pp = (ccl * ccl) * ((rp + A.gm1_over_2rho0_f * (rp * rp)) + wn[3] * A.inv_c_p_f);
-        const float x = (s + A.R_f * log1pf(rp * A.inv_rho0_f)) * A.inv_c_v_f;
-        float tp = F.T0 * expm1f(x);
-        float pq = pp;
+        const float rho = F.rho0 + wn[0];
+        float pq, tp;
+        eos_pert32(A.E32, wn[0], wn[3], row_height32(F.ylo, F.dy, gj), pq, tp);
         if (s_tile.absorb) {  // perturbations relax towards 0
           int side[4];
           const int na = absorb_walk(A.absorb, lvl, gi, gj, s_tile.box, side, s_tile.absorb);
@@ -610,10 +642,12 @@ template <typename S>
 __global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int bcB, int bcT) {
   const int nx = V.nx, ny = V.ny;
   const long nedge_x = 3L * ny, nedge_y = 3L * nx;
-  const long total = (2 * nedge_x + 2 * nedge_y + 36) * nfields;
+  const long nband = 2 * nedge_x + 2 * nedge_y + 36;
+  const long total = nband * nfields;
+  // field-major: neighbouring threads fill neighbouring band cells of one field
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    int k = (int)(t % nfields);
-    long r = t / nfields;
+    int k = (int)(t / nband);
+    long r = t - (long)k * nband;
     int i, j, si, sj;
     bool negu = false, negv = false;
     if (r < 2 * nedge_x) {
@@ -880,16 +914,14 @@ __global__ void eos_plain_kernel(CanvasView S, int ilo, int jlo, int w, int h, E
   int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y * blockDim.y + threadIdx.y;
   if (ci >= w || cj >= h) return;
   int i = ilo + ci, j = jlo + cj;
-  double w0 = S.at(0, i, j), w3 = S.at(3, i, j);
   // update_state.m4:88 uses the patch's xlo and (j - ifirst1); with the level
   // origin that is the same centre height.
-  double height = __dadd_rn(E.ylo, __dmul_rn(E.dy, (double)j + 0.5));
-  double cc = __dadd_rn(E.c, __dmul_rn(E.c_lr, height));
-  double d = __dsub_rn(w0, E.rho0);
-  double s = __ddiv_rn(w3, w0);
-  double inner = __dadd_rn(__dadd_rn(d, __dmul_rn(E.gm1_over_2rho0, __dmul_rn(d, d))), __dmul_rn(__ddiv_rn(w0, E.c_p), s));
-  S.at(5, i, j) = __dadd_rn(__dmul_rn(__dmul_rn(cc, cc), inner), E.p0);
-  S.at(6, i, j) = E.T0 * exp((s - E.R * log(E.rho0 / w0)) / E.c_v);
+  const double height = __dadd_rn(E.ylo, __dmul_rn(E.dy, (double)j + 0.5));
+  const EosConst64 K{E.rho0, E.c, E.c_lr, E.gm1_over_2rho0, E.c_p, E.p0, E.T0, E.c_v, E.R};
+  double p, T;
+  eos_abs64(K, S.at(0, i, j), S.at(3, i, j), height, p, T);
+  S.at(5, i, j) = p;
+  S.at(6, i, j) = T;
 }
 
 // ---------------------------------------------------------------------------
@@ -1161,6 +1193,10 @@ struct PackArgs {
   long long total;
   S* packed;
   int unpack;
+  int nfields;          // 7: every stored field; 5: the conserved state only
+  double ylo, dy[kL];   // cell-row heights (update_state after a 5-field unpack)
+  EosConst64 E64;
+  EosConst32 E32;
 };
 
 template <typename S>
@@ -1172,11 +1208,26 @@ __global__ void pack_kernel(PackArgs<S> A) {
     if (tx >= w || ty >= h) continue;
     long long o = A.off[t] + ty * w + tx;
     const CanvasT<S>& V = A.lev[lvl];
-    for (int k = 0; k < kNF; ++k) {
-      S& c = V.at(k, td.x + tx, td.y + ty);
+    const int i = td.x + tx, j = td.y + ty;
+    for (int k = 0; k < A.nfields; ++k) {
+      S& c = V.at(k, i, j);
       S& p = A.packed[k * A.total + o];
       if (A.unpack) c = p;
       else p = c;
+    }
+    if (A.unpack && A.nfields == 5) {  // p and T follow from the state (update_state)
+      if constexpr (std::is_same<S, float>::value) {
+        float pp, tp;
+        eos_pert32(A.E32, V.at(0, i, j), V.at(3, i, j), row_height32((float)A.ylo, (float)A.dy[lvl], j), pp, tp);
+        V.at(5, i, j) = pp;
+        V.at(6, i, j) = tp;
+      } else {
+        double pv, tv;
+        eos_abs64(A.E64, V.at(0, i, j), V.at(3, i, j), __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)j + 0.5)), pv,
+                  tv);
+        V.at(5, i, j) = pv;
+        V.at(6, i, j) = tv;
+      }
     }
   }
 }
@@ -1538,6 +1589,24 @@ static int rebuild_tables(Engine* E) {
 static bool any_absorb(const Engine* E);
 static AbsorbTables absorb_tables(const Engine* E);
 
+static EosConst32 eos_const32(const enl_engine_config& c) {
+  EosConst32 e;
+  e.rho0 = (float)c.rho0;
+  e.c = (float)c.c;
+  e.c_lr = (float)c.c_lr;
+  e.gm1_over_2rho0 = (float)((c.gamma1 - 1.0) / (2.0 * c.rho0));
+  e.inv_c_p = (float)(1.0 / c.c_p);
+  e.T0 = (float)c.T0;
+  e.inv_c_v = (float)(1.0 / c.c_v);
+  e.R = (float)c.R;
+  e.inv_rho0 = (float)(1.0 / c.rho0);
+  return e;
+}
+
+static EosConst64 eos_const64(const enl_engine_config& c) {
+  return EosConst64{c.rho0, c.c, c.c_lr, (c.gamma1 - 1.0) / (2.0 * c.rho0), c.c_p, c.p0, c.T0, c.c_v, c.R};
+}
+
 static StageArgs stage_args(Engine* E, int stage, double dt) {
   StageArgs A;
   memset(&A, 0, sizeof(A));
@@ -1601,11 +1670,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.a2 = c.rk_alpha2[stage];
   A.bdt = c.rk_beta[stage] * dt;
   A.beta = c.rk_beta[stage];
-  A.gm1_over_2rho0_f = (float)A.gm1_over_2rho0;
-  A.inv_c_p_f = (float)(1.0 / c.c_p);
-  A.inv_c_v_f = (float)(1.0 / c.c_v);
-  A.R_f = (float)c.R;
-  A.inv_rho0_f = (float)(1.0 / c.rho0);
+  A.E32 = eos_const32(c);
   A.dt_dev = E->adaptive ? E->d_dt : nullptr;
   A.dtf_dev = E->adaptive ? reinterpret_cast<const float*>(E->d_dt + 2) : nullptr;
   A.a1f = (float)A.a1;
@@ -1666,7 +1731,7 @@ static int fill_level(Engine* E, int l, int which) {
       physbc_patches_kernel<S><<<E->patch_cnt[l], 256, 0, s>>>(L.view<S>(which), E->d_patchtab.p, E->patch_off[l],
                                                                E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
   } else {
-    physbc_kernel<S><<<E->nsm * 2, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+    physbc_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
   }
   return ENL_OK;
 }
@@ -1778,7 +1843,7 @@ static void speed_t(Engine* E) {
   A.c = E->cfg.c;
   A.rho_off = E->off[0];
   A.smax_bits = E->d_smax;
-  speed_kernel<S><<<E->nsm * 4, 256, 0, stream()>>>(A);
+  speed_kernel<S><<<E->nsm * 8, 256, 0, stream()>>>(A);
 }
 
 static void adaptive_dt(Engine* E, double dt_max) {
@@ -2558,10 +2623,17 @@ int enl_engine_storage(void* e, int* elem_bytes, double* offsets) {
 }  // extern "C"
 
 template <typename S>
-static void pack_t(Engine* E, long long cells, int unpack) {
+static void pack_t(Engine* E, long long cells, int unpack, int nfields) {
   PackArgs<S> A;
   memset(&A, 0, sizeof(A));
-  for (int l = 0; l < E->cfg.nlevels; ++l) A.lev[l] = E->lev[l].view<S>(0);
+  for (int l = 0; l < E->cfg.nlevels; ++l) {
+    A.lev[l] = E->lev[l].view<S>(0);
+    A.dy[l] = E->lev[l].dx[1];
+  }
+  A.nfields = nfields;
+  A.ylo = E->cfg.xlo[1];
+  A.E64 = eos_const64(E->cfg);
+  A.E32 = eos_const32(E->cfg);
   A.tiles = E->d_tiles.p;
   A.off = E->d_tileoff.p;
   A.ntiles = (int)E->h_tiles.size();
@@ -2573,10 +2645,10 @@ static void pack_t(Engine* E, long long cells, int unpack) {
 
 extern "C" {
 
-static int pack_common(Engine* E, void* host, int unpack) {
+static int pack_common(Engine* E, void* host, int unpack, int nfields) {
   long long cells = packed_cells(E);
   if (cells == 0) return ENL_OK;
-  const size_t bytes = (size_t)cells * kNF * E->esize;
+  const size_t bytes = (size_t)cells * nfields * E->esize;
   if (bytes > E->packed_cap) {
     if (E->d_packed) cudaFree(E->d_packed);
     if (cudaMalloc(&E->d_packed, bytes) != cudaSuccess) {
@@ -2589,8 +2661,8 @@ static int pack_common(Engine* E, void* host, int unpack) {
   }
   cudaStream_t s = stream();
   if (unpack) cudaMemcpyAsync(E->d_packed, host, bytes, cudaMemcpyHostToDevice, s);
-  if (E->f32s) pack_t<float>(E, cells, unpack);
-  else pack_t<double>(E, cells, unpack);
+  if (E->f32s) pack_t<float>(E, cells, unpack, nfields);
+  else pack_t<double>(E, cells, unpack, nfields);
   if (!unpack) cudaMemcpyAsync(host, E->d_packed, bytes, cudaMemcpyDeviceToHost, s);
   return check_launch(unpack ? "engine upload" : "engine download");
 }
@@ -2598,13 +2670,25 @@ static int pack_common(Engine* E, void* host, int unpack) {
 int enl_engine_download(void* e, void* host) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, host, 0);
+  return pack_common(E, host, 0, kNF);
 }
 
 int enl_engine_upload(void* e, const void* host) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, const_cast<void*>(host), 1);
+  return pack_common(E, const_cast<void*>(host), 1, kNF);
+}
+
+int enl_engine_download_state(void* e, void* host) {
+  Engine* E = (Engine*)e;
+  if (!E || !host) return ENL_ERR_ARG;
+  return pack_common(E, host, 0, 5);
+}
+
+int enl_engine_upload_state(void* e, const void* host) {
+  Engine* E = (Engine*)e;
+  if (!E || !host) return ENL_ERR_ARG;
+  return pack_common(E, const_cast<void*>(host), 1, 5);
 }
 
 int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, long long* cells) {

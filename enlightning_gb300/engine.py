@@ -196,6 +196,21 @@ class Engine:
         assert host.dtype == self.dtype
         _lib.check(self.L.enl_engine_upload(self.h, C.c_void_p(host.data_ptr())), "enl_engine_upload")
 
+    def state_host(self, pin=True):
+        """Host tensor sized for download_state/upload_state (5 fields)."""
+        t = torch.empty(self.packed_size() // 7 * 5, dtype=self.dtype)
+        return t.pin_memory() if pin else t
+
+    def download_state(self, host: torch.Tensor):
+        """Conserved state (5 fields) of every patch interior to host memory."""
+        assert host.dtype == self.dtype
+        _lib.check(self.L.enl_engine_download_state(self.h, C.c_void_p(host.data_ptr())), "enl_engine_download_state")
+
+    def upload_state(self, host: torch.Tensor):
+        """Conserved state from host memory; p and T follow on the device."""
+        assert host.dtype == self.dtype
+        _lib.check(self.L.enl_engine_upload_state(self.h, C.c_void_p(host.data_ptr())), "enl_engine_upload_state")
+
     def set_adaptive_dt(self, on=True, cfl=0.5):
         _lib.check(self.L.enl_engine_set_adaptive_dt(self.h, int(on), float(cfl)), "enl_engine_set_adaptive_dt")
 

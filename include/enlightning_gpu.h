@@ -275,6 +275,11 @@ int enl_engine_time(void* engine, double* dt_last, double* sim_time);
 int enl_engine_packed_size(void* engine, long long* nelems);
 int enl_engine_download(void* engine, void* host);
 int enl_engine_upload(void* engine, const void* host);
+/* The same with the conserved state only (rho, rho u, rho v, rho s,
+ * rho T_n: 5 of the 7 fields, nelems * 5/7 elements); the upload recomputes
+ * p and T on the device with update_state (update_state.m4:90-105). */
+int enl_engine_download_state(void* engine, void* host);
+int enl_engine_upload_state(void* engine, const void* host);
 
 /* Stage-kernel timing: with on = 1 every direct (not graph) enl_engine_step
  * brackets its three stage-kernel launches with CUDA events on the stream.

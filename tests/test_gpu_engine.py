@@ -430,3 +430,27 @@ def test_mic_files_in_reference_format(tmp_path):
     assert (tmp_path / "mic-1-info.txt").read_text() == (
         "1\n44100\n(0.7,0.1)\n1 0 1.013250e+05 1.013250e+05\n"
         "1\n44100\n(0.7,0.1)\n1 1 1.013250e+05 1.013305e+05\n")
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_state_exchange_recomputes_p_and_t(ora, precision):
+    """download_state/upload_state move the 5 conserved fields; p and T come
+    back from update_state on the device, equal bit for bit to what a stage
+    wrote (single level, reflecting walls: every p, T is update_state of w)."""
+    prm = default_params()
+    nx, ny = 64, 48
+    E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 1, [[(0, 31, 0, 47), (32, 63, 0, 47)]], (REFLECT,) * 4,
+                     "hybrid_high_llf", precision=precision)
+    for _ in range(2):
+        E.step(workloads.pulse_dt(prm, (0.1, 0.1)))
+    host = E.state_host()
+    assert host.numel() * 7 == E.packed_size() * 5
+    E.download_state(host)
+    torch.cuda.synchronize()
+    before = E.level_state(0).cpu().numpy().copy()
+    E.buffer(0, 0).zero_()
+    E.upload_state(host)
+    torch.cuda.synchronize()
+    after = E.level_state(0).cpu().numpy()
+    assert np.array_equal(after, before)
+    assert E.health() == 0
