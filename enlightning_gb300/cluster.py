@@ -147,9 +147,13 @@ def cluster_tags_native(tags, efficiency=0.7, min_size=8, max_size=128, allowed=
     import ctypes as C
 
     from . import _lib
-    t = np.ascontiguousarray(np.asarray(tags, dtype=np.uint8))
+    def as_bytes(m):  # bool maps are passed as their bytes, without a copy
+        m = np.ascontiguousarray(m)
+        return m.view(np.uint8) if m.dtype == np.bool_ else np.ascontiguousarray(m, dtype=np.uint8)
+
+    t = as_bytes(tags)
     ny, nx = t.shape
-    a = None if allowed is None else np.ascontiguousarray(np.asarray(allowed, dtype=np.uint8))
+    a = None if allowed is None else as_bytes(allowed)
     cap = 1024
     while True:
         out = np.zeros((cap, 4), np.int32)

@@ -17,7 +17,6 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <map>
 #include <type_traits>
 #include <vector>
 
@@ -1366,7 +1365,8 @@ struct DevArray {
   bool ensure(size_t n) {  // returns true if reallocated
     if (n <= cap) return false;
     if (p) cudaFree(p);
-    cap = std::max<size_t>(n, 2 * cap);
+    // headroom, so that regrids rarely outgrow a table (and a captured graph)
+    cap = std::max<size_t>(n + n / 2, 2 * cap);
     cudaMalloc(&p, cap * sizeof(T));
     return true;
   }
@@ -1427,6 +1427,9 @@ struct Engine {
   bool f32s = false;
   size_t esize = 8;
   double* d_env[kL][4] = {};  // absorbing-envelope tables (null: side not ABSORB)
+  void* stage_host = nullptr;  // pinned staging of the tables
+  size_t stage_cap = 0;
+  cudaEvent_t stage_ev = nullptr;
   float* d_envf[kL][4] = {};
   unsigned char* d_cont[kL][4] = {};
   double off[kNF] = {0, 0, 0, 0, 0, 0, 0};
@@ -1476,27 +1479,31 @@ static void tiles_of_box(int4 b, int level, int pid, std::vector<int4>& out) {
 // Row segments of the cells within distance 3 (Chebyshev) of the patch union,
 // inside [0,nx)x[0,ny), not covered by any patch.
 static void halo_segments(const std::vector<int4>& P, int nx, int ny, std::vector<int4>& out) {
-  std::map<int, std::vector<std::pair<int, int>>> grow, cover;
+  if (P.empty()) return;
+  // rows touched by the grown patches, each with its grown and covered intervals
+  int j0 = ny, j1 = -1;
+  for (auto& b : P) {
+    j0 = std::min(j0, std::max(0, b.z - 3));
+    j1 = std::max(j1, std::min(ny - 1, b.w + 3));
+  }
+  std::vector<std::vector<std::pair<int, int>>> grow(j1 - j0 + 1), cover(j1 - j0 + 1);
   for (auto& b : P) {
     for (int j = std::max(0, b.z - 3); j <= std::min(ny - 1, b.w + 3); ++j)
-      grow[j].push_back({std::max(0, b.x - 3), std::min(nx - 1, b.y + 3)});
-    for (int j = b.z; j <= b.w; ++j) cover[j].push_back({b.x, b.y});
+      grow[j - j0].push_back({std::max(0, b.x - 3), std::min(nx - 1, b.y + 3)});
+    for (int j = b.z; j <= b.w; ++j) cover[j - j0].push_back({b.x, b.y});
   }
-  for (auto& kv : grow) {
-    int j = kv.first;
-    auto g = kv.second;
+  std::vector<std::pair<int, int>> gm;
+  for (int j = j0; j <= j1; ++j) {
+    auto& g = grow[j - j0];
+    if (g.empty()) continue;
     std::sort(g.begin(), g.end());
-    std::vector<std::pair<int, int>> gm;  // merged grown intervals
+    gm.clear();  // merged grown intervals
     for (auto& iv : g) {
       if (!gm.empty() && iv.first <= gm.back().second + 1) gm.back().second = std::max(gm.back().second, iv.second);
       else gm.push_back(iv);
     }
-    std::vector<std::pair<int, int>> cv;
-    auto it = cover.find(j);
-    if (it != cover.end()) {
-      cv = it->second;
-      std::sort(cv.begin(), cv.end());
-    }
+    auto& cv = cover[j - j0];
+    std::sort(cv.begin(), cv.end());
     for (auto& iv : gm) {
       int a = iv.first;
       for (auto& c : cv) {
@@ -1559,30 +1566,46 @@ static int rebuild_tables(Engine* E) {
     int4 td = E->h_tiles[q];
     acc += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
   }
-  E->d_tileoff.ensure(std::max<size_t>(E->h_tileoff.size(), 1));
-  if (!E->h_tileoff.empty())
-    cudaMemcpyAsync(E->d_tileoff.p, E->h_tileoff.data(), E->h_tileoff.size() * sizeof(long long),
-                    cudaMemcpyHostToDevice, stream());
   bool grew = false;
+  E->d_tileoff.ensure(std::max<size_t>(E->h_tileoff.size(), 1));
   grew |= E->d_tiles.ensure(std::max<size_t>(E->h_tiles.size(), 1));
   grew |= E->d_halo.ensure(std::max<size_t>(E->h_halo.size(), 1));
   grew |= E->d_ctiles.ensure(std::max<size_t>(E->h_ctiles.size(), 1));
   grew |= E->d_patchtab.ensure(std::max<size_t>(E->h_patchtab.size(), 1));
   if (grew) E->graph_valid = false;
+  // one pinned staging buffer for all tables, copied asynchronously; the
+  // previous rebuild's copies must have left it before it is rewritten
+  const size_t b_off = E->h_tileoff.size() * sizeof(long long), b_tiles = E->h_tiles.size() * sizeof(int4),
+               b_halo = E->h_halo.size() * sizeof(int4), b_ct = E->h_ctiles.size() * sizeof(int4),
+               b_pt = E->h_patchtab.size() * sizeof(int4), b_meta = sizeof(E->h_meta);
+  const size_t need = b_off + b_tiles + b_halo + b_ct + b_pt + b_meta;
+  if (E->stage_ev) cudaEventSynchronize(E->stage_ev);
+  if (need > E->stage_cap) {
+    if (E->stage_host) cudaFreeHost(E->stage_host);
+    E->stage_cap = need + need / 2;
+    if (cudaHostAlloc(&E->stage_host, E->stage_cap, cudaHostAllocDefault) != cudaSuccess) {
+      E->stage_host = nullptr;
+      E->stage_cap = 0;
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+  }
+  if (!E->stage_ev) cudaEventCreateWithFlags(&E->stage_ev, cudaEventDisableTiming);
   cudaStream_t s = stream();
-  if (!E->h_tiles.empty())
-    cudaMemcpyAsync(E->d_tiles.p, E->h_tiles.data(), E->h_tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
-  if (!E->h_halo.empty())
-    cudaMemcpyAsync(E->d_halo.p, E->h_halo.data(), E->h_halo.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
-  if (!E->h_ctiles.empty())
-    cudaMemcpyAsync(E->d_ctiles.p, E->h_ctiles.data(), E->h_ctiles.size() * sizeof(int4), cudaMemcpyHostToDevice,
-                    s);
-  if (!E->h_patchtab.empty())
-    cudaMemcpyAsync(E->d_patchtab.p, E->h_patchtab.data(), E->h_patchtab.size() * sizeof(int4),
-                    cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(E->d_meta, E->h_meta, sizeof(E->h_meta), cudaMemcpyHostToDevice, s);
-  // the host vectors are reused; wait so they are not modified under the copy
-  cudaStreamSynchronize(s);
+  unsigned char* h = static_cast<unsigned char*>(E->stage_host);
+  auto put = [&](void* dst, const void* src, size_t n) {
+    if (!n) return;
+    memcpy(h, src, n);
+    cudaMemcpyAsync(dst, h, n, cudaMemcpyHostToDevice, s);
+    h += n;
+  };
+  put(E->d_tileoff.p, E->h_tileoff.data(), b_off);
+  put(E->d_tiles.p, E->h_tiles.data(), b_tiles);
+  put(E->d_halo.p, E->h_halo.data(), b_halo);
+  put(E->d_ctiles.p, E->h_ctiles.data(), b_ct);
+  put(E->d_patchtab.p, E->h_patchtab.data(), b_pt);
+  put(E->d_meta, E->h_meta, b_meta);
+  cudaEventRecord(E->stage_ev, s);
   return check_launch("engine tables");
 }
 
@@ -2137,6 +2160,11 @@ int enl_engine_destroy(void* e) {
   for (int q = 0; q < 6; ++q)
     if (E->pev[q]) cudaEventDestroy(E->pev[q]);
   if (E->d_smax) cudaFree(E->d_smax);
+  if (E->stage_ev) {
+    cudaEventSynchronize(E->stage_ev);
+    cudaEventDestroy(E->stage_ev);
+  }
+  if (E->stage_host) cudaFreeHost(E->stage_host);
   if (E->d_mics) cudaFree(E->d_mics);
   if (E->d_mic_it) cudaFree(E->d_mic_it);
   if (E->d_mic_rec) cudaFree(E->d_mic_rec);
