@@ -469,6 +469,25 @@ WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource, "pulses64": Pu
 # ---------------------------------------------------------------------------
 
 
+def max_over_ranks(ms, ws, device=None):
+    """The slowest rank's time: replicas run the same work, and the job is
+    done when the last one is."""
+    if ws <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    if device is None:
+        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank, ws, ms):
+    """Whole-job throughput: every rank processed units_per_rank in ms (the max over ranks)."""
+    return units_per_rank * ws / (ms * 1e-3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -619,12 +638,8 @@ def run_ours(args):
             wl.step(timed_rhs=True)
             ev[k][1].record()
         barrier()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = wl.cells * args.steps * ws / (ms * 1e-3)
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), ws)
+    value = aggregate_rate(wl.cells * args.steps, ws, ms)
     rhs_ms = float(np.mean([a.elapsed_time(b) for a, b in wl.rhs_events]))
     achieved = wl.cells * RHS_BYTES_PER_CELL / (rhs_ms * 1e-3) / 1e9
 
@@ -647,7 +662,8 @@ def run_ours(args):
     tf = os.path.join(ROOT, "profiles", "rhs_traffic.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get(args.workload)
+            with open(tf) as f:
+                traffic = json.load(f).get(args.workload)
         except Exception:
             traffic = None
     line = {
@@ -711,12 +727,8 @@ def run_linesource(args):
         cu = wl.advance("fast", args.steps, use_graph=True)
         e1.record()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cu * ws / (ms * 1e-3)
+    ms = max_over_ranks(e0.elapsed_time(e1), ws)
+    value = aggregate_rate(cu, ws, ms)
     regrid_info = {"regrids": wl.regrids["fast"] - rn0, "host_ms": 1e3 * (wl.regrid_s["fast"] - rg0),
                    "graph_captures": wl.captures - cap0}
     if wl.fast_h is not None:
@@ -775,7 +787,8 @@ def run_linesource(args):
     tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
     if os.path.exists(tf):
         try:
-            rec = json.load(open(tf)).get(PREC_NAMES[args.precision])
+            with open(tf) as f:
+                rec = json.load(f).get(PREC_NAMES[args.precision])
             if rec:
                 traffic = rec["dram_bytes_per_cell_launch"] * cells_per_launch
         except Exception:

@@ -87,20 +87,21 @@ struct AbsorbTables {
 // (i, j) of patch b is reached follows from its neighbour towards the side:
 // the walk is evaluated per cell.  The sides that reach the cell are returned
 // (0..3 = L, R, B, T) in the reference's order.
-// `mask` (bit s = side s) limits the walk to the sides that can reach the
-// cell's tile (absorb_tile_mask).
-__device__ __forceinline__ int absorb_walk(const AbsorbTables& T, int lvl, int i, int j, const int4& b,
-                                           int q[4], int mask = 15) {
-  int n = 0;
+// Bit s set when the walk from side s (0..3 = L, R, B, T) reaches the cell;
+// `mask` limits the test to the sides that can reach the cell's tile
+// (absorb_tile_mask).  Callers apply the sides in the reference's order.
+__device__ __forceinline__ int absorb_reach(const AbsorbTables& T, int lvl, int i, int j, const int4& b,
+                                            int mask = 15) {
+  int r = 0;
   const unsigned char* c = T.cont[lvl][0];
-  if ((mask & 1) && c && (j != b.z || c[b.x]) && (i == b.x || c[i - 1])) q[n++] = 0;
+  if ((mask & 1) && c && (j != b.z || c[b.x]) && (i == b.x || c[i - 1])) r |= 1;
   c = T.cont[lvl][1];
-  if ((mask & 2) && c && (j != b.z || c[b.y]) && (i == b.y || c[i + 1])) q[n++] = 1;
+  if ((mask & 2) && c && (j != b.z || c[b.y]) && (i == b.y || c[i + 1])) r |= 2;
   c = T.cont[lvl][2];
-  if ((mask & 4) && c && c[b.z] && (j == b.z || c[j - 1])) q[n++] = 2;
+  if ((mask & 4) && c && c[b.z] && (j == b.z || c[j - 1])) r |= 4;
   c = T.cont[lvl][3];
-  if ((mask & 8) && c && c[b.w] && (j == b.w || c[j + 1])) q[n++] = 3;
-  return n;
+  if ((mask & 8) && c && c[b.w] && (j == b.w || c[j + 1])) r |= 8;
+  return r;
 }
 
 // Sides whose walk can reach some cell of the w x h tile at (i0, j0) of patch
@@ -527,10 +528,11 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
         float pq, tp;
         eos_pert32(A.E32, wn[0], wn[3], row_height32(F.ylo, F.dy, gj), pq, tp);
         if (s_tile.absorb) {  // perturbations relax towards 0
-          int side[4];
-          const int na = absorb_walk(A.absorb, lvl, gi, gj, s_tile.box, side, s_tile.absorb);
-          for (int q = 0; q < na; ++q) {
-            const float t_ = A.absorb.envf[lvl][side[q]][side[q] < 2 ? gi : gj];
+          const int reach = absorb_reach(A.absorb, lvl, gi, gj, s_tile.box, s_tile.absorb);
+#pragma unroll
+          for (int sd = 0; sd < 4; ++sd) {
+            if (!(reach & (1 << sd))) continue;
+            const float t_ = A.absorb.envf[lvl][sd][sd < 2 ? gi : gj];
 #pragma unroll
             for (int k = 0; k < 5; ++k) wn[k] *= t_;
             pq *= t_;
@@ -590,19 +592,19 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) st
           tv = A.T0 * exp((s - A.R * log(A.rho0 / wn[0])) / A.c_v);
         }
         if (s_tile.absorb) {  // absolute values relax towards the ambient state
-          int side[4];
-          double fa[4];
-          const int na = absorb_walk(A.absorb, lvl, gi, gj, s_tile.box, side, s_tile.absorb);
-          for (int q = 0; q < na; ++q) fa[q] = A.absorb.env[lvl][side[q]][side[q] < 2 ? gi : gj];
+          const int reach = absorb_reach(A.absorb, lvl, gi, gj, s_tile.box, s_tile.absorb);
           const double rT = __dmul_rn(A.T0, A.rho0);
-          for (int q = 0; q < na; ++q) {
-            pv = relax_(pv, A.p0, fa[q]);
-            tv = relax_(tv, A.T0, fa[q]);
-            wn[0] = relax_(wn[0], A.rho0, fa[q]);
-            wn[1] = __dmul_rn(wn[1], fa[q]);
-            wn[2] = __dmul_rn(wn[2], fa[q]);
-            wn[3] = __dmul_rn(wn[3], fa[q]);
-            wn[4] = relax_(wn[4], rT, fa[q]);
+#pragma unroll
+          for (int sd = 0; sd < 4; ++sd) {
+            if (!(reach & (1 << sd))) continue;
+            const double fa = A.absorb.env[lvl][sd][sd < 2 ? gi : gj];
+            pv = relax_(pv, A.p0, fa);
+            tv = relax_(tv, A.T0, fa);
+            wn[0] = relax_(wn[0], A.rho0, fa);
+            wn[1] = __dmul_rn(wn[1], fa);
+            wn[2] = __dmul_rn(wn[2], fa);
+            wn[3] = __dmul_rn(wn[3], fa);
+            wn[4] = relax_(wn[4], rT, fa);
           }
         }
         out[5 * fs + g] = pv;
@@ -874,20 +876,20 @@ __global__ void absorb_tiles_kernel(AbsorbTileArgs A) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx >= w || ty >= h) continue;
     const int i = td.x + tx, j = td.y + ty;
-    int side[4];
-    double fa[4];
-    const int na = absorb_walk(A.T, lvl, i, j, A.patchtab[td.w], side);
-    for (int q = 0; q < na; ++q) fa[q] = A.T.env[lvl][side[q]][side[q] < 2 ? i : j];
+    const int reach = absorb_reach(A.T, lvl, i, j, A.patchtab[td.w]);
     const CanvasView& V = A.lev[lvl];
     const double rT = __dmul_rn(A.T0, A.rho0);
-    for (int q = 0; q < na; ++q) {
-      V.at(5, i, j) = relax_(V.at(5, i, j), A.p0, fa[q]);
-      V.at(6, i, j) = relax_(V.at(6, i, j), A.T0, fa[q]);
-      V.at(0, i, j) = relax_(V.at(0, i, j), A.rho0, fa[q]);
-      V.at(1, i, j) = __dmul_rn(V.at(1, i, j), fa[q]);
-      V.at(2, i, j) = __dmul_rn(V.at(2, i, j), fa[q]);
-      V.at(3, i, j) = __dmul_rn(V.at(3, i, j), fa[q]);
-      V.at(4, i, j) = relax_(V.at(4, i, j), rT, fa[q]);
+#pragma unroll
+    for (int sd = 0; sd < 4; ++sd) {
+      if (!(reach & (1 << sd))) continue;
+      const double fa = A.T.env[lvl][sd][sd < 2 ? i : j];
+      V.at(5, i, j) = relax_(V.at(5, i, j), A.p0, fa);
+      V.at(6, i, j) = relax_(V.at(6, i, j), A.T0, fa);
+      V.at(0, i, j) = relax_(V.at(0, i, j), A.rho0, fa);
+      V.at(1, i, j) = __dmul_rn(V.at(1, i, j), fa);
+      V.at(2, i, j) = __dmul_rn(V.at(2, i, j), fa);
+      V.at(3, i, j) = __dmul_rn(V.at(3, i, j), fa);
+      V.at(4, i, j) = relax_(V.at(4, i, j), rT, fa);
     }
   }
 }

@@ -115,6 +115,39 @@ __device__ __forceinline__ void sources_fast(const ACC& A, const FastConst& P, f
   H[4] = (rho * P.inv_tau_n) * dT;
 }
 
+// LLF-split WENO derivative of field k at the cell, plus its source term hk:
+// KK_k = hk - (dF/dx + dG/dy), from the staged fluxes and the cell's speeds.
+template <int ORDER, class ACC>
+__device__ __noinline__ float weno_field(const ACC A, const FastConst& P, int k, float af, float ag, float hk) {
+  float fp[7], fm[7], gp[7], gm[7];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    float wx = A.w(k, q - 3, 0), wy = A.w(k, 0, q - 3);
+    float F = A.fx(k, q - 3), G = A.gy(k, q - 3);
+    fp[q] = 0.5f * fmaf(af, wx, F);
+    fm[q] = 0.5f * fmaf(-af, wx, F);
+    gp[q] = 0.5f * fmaf(ag, wy, G);
+    gm[q] = 0.5f * fmaf(-ag, wy, G);
+  }
+  float dfx, dgy;
+  if (ORDER == 5) {
+    dfx = ((weno5f<true>(fp[0], fp[1], fp[2], fp[3], fp[4]) + weno5f<false>(fm[1], fm[2], fm[3], fm[4], fm[5])) -
+           weno5f<true>(fp[1], fp[2], fp[3], fp[4], fp[5])) -
+          weno5f<false>(fm[2], fm[3], fm[4], fm[5], fm[6]);
+    dgy = ((weno5f<true>(gp[0], gp[1], gp[2], gp[3], gp[4]) + weno5f<false>(gm[1], gm[2], gm[3], gm[4], gm[5])) -
+           weno5f<true>(gp[1], gp[2], gp[3], gp[4], gp[5])) -
+          weno5f<false>(gm[2], gm[3], gm[4], gm[5], gm[6]);
+  } else {
+    dfx = ((weno3f<true>(fp[1], fp[2], fp[3]) + weno3f<false>(fm[2], fm[3], fm[4])) -
+           weno3f<true>(fp[2], fp[3], fp[4])) -
+          weno3f<false>(fm[3], fm[4], fm[5]);
+    dgy = ((weno3f<true>(gp[1], gp[2], gp[3]) + weno3f<false>(gm[2], gm[3], gm[4])) -
+           weno3f<true>(gp[2], gp[3], gp[4])) -
+          weno3f<false>(gm[3], gm[4], gm[5]);
+  }
+  return fmaf(dfx, P.inv_dx0, fmaf(dgy, P.inv_dx1, hk));
+}
+
 template <int ORDER, bool LLF, class ACC>
 __device__ __forceinline__ void fluxes_fast(const ACC& A, const FastConst& P, int row, int tag, float H[5],
                                             float KK[5]) {
@@ -156,36 +189,13 @@ __device__ __forceinline__ void fluxes_fast(const ACC& A, const FastConst& P, in
     af = P.alpha;
     ag = P.alpha;
   }
-#pragma unroll 1
-  for (int k = 0; k < 5; ++k) {
-    float fp[7], fm[7], gp[7], gm[7];
-#pragma unroll
-    for (int q = 0; q < 7; ++q) {
-      float wx = A.w(k, q - 3, 0), wy = A.w(k, 0, q - 3);
-      float F = A.fx(k, q - 3), G = A.gy(k, q - 3);
-      fp[q] = 0.5f * fmaf(af, wx, F);
-      fm[q] = 0.5f * fmaf(-af, wx, F);
-      gp[q] = 0.5f * fmaf(ag, wy, G);
-      gm[q] = 0.5f * fmaf(-ag, wy, G);
-    }
-    float dfx, dgy;
-    if (ORDER == 5) {
-      dfx = ((weno5f<true>(fp[0], fp[1], fp[2], fp[3], fp[4]) + weno5f<false>(fm[1], fm[2], fm[3], fm[4], fm[5])) -
-             weno5f<true>(fp[1], fp[2], fp[3], fp[4], fp[5])) -
-            weno5f<false>(fm[2], fm[3], fm[4], fm[5], fm[6]);
-      dgy = ((weno5f<true>(gp[0], gp[1], gp[2], gp[3], gp[4]) + weno5f<false>(gm[1], gm[2], gm[3], gm[4], gm[5])) -
-             weno5f<true>(gp[1], gp[2], gp[3], gp[4], gp[5])) -
-            weno5f<false>(gm[2], gm[3], gm[4], gm[5], gm[6]);
-    } else {
-      dfx = ((weno3f<true>(fp[1], fp[2], fp[3]) + weno3f<false>(fm[2], fm[3], fm[4])) -
-             weno3f<true>(fp[2], fp[3], fp[4])) -
-            weno3f<false>(fm[3], fm[4], fm[5]);
-      dgy = ((weno3f<true>(gp[1], gp[2], gp[3]) + weno3f<false>(gm[2], gm[3], gm[4])) -
-             weno3f<true>(gp[2], gp[3], gp[4])) -
-            weno3f<false>(gm[3], gm[4], gm[5]);
-    }
-    KK[k] = fmaf(dfx, P.inv_dx0, fmaf(dgy, P.inv_dx1, H[k]));
-  }
+  // one out-of-line call per field keeps this function's H and KK indexed by
+  // constants (registers) and the code of the five fields shared
+  KK[0] = weno_field<ORDER>(A, P, 0, af, ag, H[0]);
+  KK[1] = weno_field<ORDER>(A, P, 1, af, ag, H[1]);
+  KK[2] = weno_field<ORDER>(A, P, 2, af, ag, H[2]);
+  KK[3] = weno_field<ORDER>(A, P, 3, af, ag, H[3]);
+  KK[4] = weno_field<ORDER>(A, P, 4, af, ag, H[4]);
 }
 
 }  // namespace enl

@@ -286,11 +286,12 @@ def main(out_dir="gpurun_out", quick=False):
     best = max(good, key=lambda r: r["gain"])
     np.savez(os.path.join(out_dir, "learned_sensor.npz"), params=best["P"], margin=np.float32(best["margin"]),
              tau=np.float64(best["tau"]), loss=np.array(best["loss"]))
-    json.dump(dict(chosen_tau=best["tau"], err_budget=ERR_BUDGET, rows=int(n),
-                   sweep=[{k: v for k, v in r.items() if k != "P"} for r in results]),
-              open(os.path.join(out_dir, "sensor_report.json"), "w"), indent=1)
+    with open(os.path.join(out_dir, "sensor_report.json"), "w") as f:
+        json.dump(dict(chosen_tau=best["tau"], err_budget=ERR_BUDGET, rows=int(n),
+                       sweep=[{k: v for k, v in r.items() if k != "P"} for r in results]), f, indent=1)
     log(f"chosen tau {best['tau']}")
     log("done")
+    logf.close()
 
 
 if __name__ == "__main__":

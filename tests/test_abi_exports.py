@@ -17,7 +17,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_symbols():
     names = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
-        text = open(h).read()
+        with open(h) as f:
+            text = f.read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(", text, re.M):
             name = m.group(1)

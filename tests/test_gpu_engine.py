@@ -454,3 +454,32 @@ def test_state_exchange_recomputes_p_and_t(ora, precision):
     after = E.level_state(0).cpu().numpy()
     assert np.array_equal(after, before)
     assert E.health() == 0
+
+
+@pytest.mark.parametrize("variant", ["hybrid_high_llf", "hybrid_high", "hybrid_low_llf", "hybrid_low",
+                                     "weno_high_llf", "weno_high", "weno_low_llf", "weno_low", "drp"])
+def test_fp32_state_every_variant_within_budget(ora, variant):
+    """The FP32 perturbation-storage stage kernel of every scheme against the
+    FP64 engine (itself held to the oracle at 1e-12), two levels, 6 steps."""
+    prm = default_params()
+    nx, ny = 96, 64
+    boxes = [[(0, 47, 0, 63), (48, 95, 0, 63)], [(48, 143, 32, 95)]]
+    out = {}
+    for prec in (PREC_FP64, PREC_FP32_STATE):
+        E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, boxes, (REFLECT,) * 4, variant, precision=prec)
+        dt = workloads.pulse_dt(prm, (0.05, 0.05))
+        for _ in range(6):
+            E.step(dt)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        out[prec] = [E.level_state(l).cpu().numpy().copy() for l in range(2)]
+        E.close()
+    for l in range(2):
+        a, b = out[PREC_FP32_STATE][l], out[PREC_FP64][l]
+        m = np.zeros(a.shape[1:], bool)
+        for bx in boxes[l]:
+            m[bx[2]:bx[3] + 1, bx[0]:bx[1] + 1] = True
+        assert relL2(a[0][m] - prm["rho0"], b[0][m] - prm["rho0"]) <= 1e-3, (variant, l)
+        assert relL2(a[5][m] - prm["p0"], b[5][m] - prm["p0"]) <= 1e-3, (variant, l)
+        for k in (1, 2):
+            assert relL2(a[k][m], b[k][m]) <= 1e-3, (variant, l, k)
