@@ -112,7 +112,7 @@ class ClockSampler:
 
 
 class Pulse512Plain:
-    """Config 1: one 512x512 patch, Gaussian overpressure 0.1 p0, sigma 8 cells,
+    """Single pulse: one 512x512 patch, Gaussian overpressure 0.1 p0, sigma 8 cells,
     dx = 0.1 m, reflective walls, CFL 0.5, hybrid WENO5/DRP with LLF splitting,
     advanced through the drop-in F77 entry points (plain FP64 path)."""
 
@@ -252,7 +252,7 @@ class Pulse512Plain:
 
 
 class LineSource:
-    """Config 3: thunder-like line source on a 3-level hierarchy.
+    """Thunder-like line source on a 3-level hierarchy.
 
     4096x2048 base cells, dx = 0.5 m, refinement ratio 2 (finest dx 0.125 m),
     200-segment seeded random-walk channel depositing 10 p0 with sigma 2 base
@@ -381,7 +381,7 @@ class LineSource:
 
 
 class PulseBatch(LineSource):
-    """Config 5: 64 independent Gaussian-pulse problems (square sides uniform
+    """64 independent Gaussian-pulse problems (square sides uniform
     in 128..1024, multiples of 32; amplitude U(0.01, 0.5) p0; sigma U(4, 16)
     cells; dx 0.1 m; reflective walls; dt = cfl dx / c) advanced together: one
     persistent launch per RK stage covers every tile of every problem."""
@@ -698,6 +698,8 @@ def run_linesource(args):
     t_build = time.perf_counter()
     wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=not args.no_plain,
                                   precision=args.precision)
+    if args.regrid_every is not None and wl.REGRID:
+        wl.REGRID = args.regrid_every
     esize = 4 if args.precision == 2 else 8
     t_build = time.perf_counter() - t_build
 
@@ -836,6 +838,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=20)
     ap.add_argument("--scale", type=int, default=1, help="shrink the line-source base grid (profiling)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm (profiling)")
+    ap.add_argument("--regrid-every", type=int, default=None,
+                    help="regrid interval of the multi-level workloads (default: the workload's, 10)")
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="engine mode: 0 FP64, 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
     args = ap.parse_args()

@@ -838,6 +838,16 @@ __device__ __forceinline__ bool ratio_below_e(double fm, double f0, double fp, d
   return __ddiv_rn(num, den) < Lit::c0_9999;
 }
 
+// The same test in single precision for FP32 storage (FP64 division is slow
+// on this part and the fast engine's tags need no bit-exactness); 0.9999f is
+// the reference's REAL*4 literal itself.
+__device__ __forceinline__ bool ratio_below_f(float fm, float f0, float fp, float ep) {
+  const float t1 = f0 - fm, t2 = fp - f0;
+  const float num = fmaf(2.0f, fabsf(t1 * t2), ep);
+  const float den = fmaf(t1, t1, fmaf(t2, t2, ep));
+  return __fdiv_rn(num, den) < 0.9999f;
+}
+
 // The ratio test depends on differences only, so it reads perturbation
 // storage as it is.
 template <typename S>
@@ -849,10 +859,19 @@ __global__ void tag_tiles_kernel(int* tags, CanvasT<S> W, CanvasT<S> H, const in
     int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx >= w || ty >= h) continue;
     int i = td.x + tx, j = td.y + ty;
-    bool tg = ratio_below_e(H.at(0, i - 1, j), H.at(0, i, j), H.at(0, i + 1, j), ep0) ||
-              ratio_below_e(H.at(0, i, j - 1), H.at(0, i, j), H.at(0, i, j + 1), ep0) ||
-              ratio_below_e(W.at(0, i - 1, j), W.at(0, i, j), W.at(0, i + 1, j), ep1) ||
-              ratio_below_e(W.at(0, i, j - 1), W.at(0, i, j), W.at(0, i, j + 1), ep1);
+    bool tg;
+    if constexpr (std::is_same<S, float>::value) {
+      const float e0 = (float)ep0, e1 = (float)ep1;
+      tg = ratio_below_f(H.at(0, i - 1, j), H.at(0, i, j), H.at(0, i + 1, j), e0) ||
+           ratio_below_f(H.at(0, i, j - 1), H.at(0, i, j), H.at(0, i, j + 1), e0) ||
+           ratio_below_f(W.at(0, i - 1, j), W.at(0, i, j), W.at(0, i + 1, j), e1) ||
+           ratio_below_f(W.at(0, i, j - 1), W.at(0, i, j), W.at(0, i, j + 1), e1);
+    } else {
+      tg = ratio_below_e(H.at(0, i - 1, j), H.at(0, i, j), H.at(0, i + 1, j), ep0) ||
+           ratio_below_e(H.at(0, i, j - 1), H.at(0, i, j), H.at(0, i, j + 1), ep0) ||
+           ratio_below_e(W.at(0, i - 1, j), W.at(0, i, j), W.at(0, i + 1, j), ep1) ||
+           ratio_below_e(W.at(0, i, j - 1), W.at(0, i, j), W.at(0, i, j + 1), ep1);
+    }
     tags[(long)j * W.nx + i] = tg ? 1 : 0;
   }
 }
@@ -2623,6 +2642,17 @@ int enl_engine_time(void* e, double* dt_last, double* sim_time) {
   if (dt_last) *dt_last = h[0];
   if (sim_time) *sim_time = h[1];
   return check_launch("engine time");
+}
+
+int enl_engine_set_time(void* e, double dt_last, double sim_time) {
+  Engine* E = (Engine*)e;
+  if (!E) return ENL_ERR_ARG;
+  const double h[2] = {dt_last, sim_time};
+  const float hf = (float)dt_last;
+  cudaMemcpyAsync(E->d_dt, h, sizeof(h), cudaMemcpyHostToDevice, stream());
+  cudaMemcpyAsync(E->d_dt + 2, &hf, sizeof(float), cudaMemcpyHostToDevice, stream());
+  cudaStreamSynchronize(stream());
+  return check_launch("engine set_time");
 }
 
 static long long packed_cells(Engine* E) {

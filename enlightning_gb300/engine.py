@@ -63,6 +63,9 @@ class Engine:
         cfg.independent = int(bool(independent))
         self.cfg = cfg
         self.params = dict(p)
+        self._init_args = dict(nx0=nx0, ny0=ny0, dx0=tuple(dx0), nlevels=nlevels, ratio=ratio, xlo=tuple(xlo),
+                               bc=tuple(bc), variant=variant, precision=int(precision), learned=bool(learned),
+                               independent=bool(independent))
         self.nlevels, self.ratio = nlevels, ratio
         self.dx0 = tuple(dx0)
         self.xlo = tuple(xlo)
@@ -218,6 +221,41 @@ class Engine:
         dt, t = C.c_double(), C.c_double()
         _lib.check(self.L.enl_engine_time(self.h, C.byref(dt), C.byref(t)), "enl_engine_time")
         return dt.value, t.value
+
+    # -- restart (the role of enlightning.C:1859-2060 for this engine) ------------
+    def save(self, path, iteration=0):
+        """Restart file (.npz): construction arguments, parameters, patch boxes
+        of every level, the packed state of every patch interior (7 fields,
+        storage type), the CFL state and the iteration number."""
+        host = self.packed_host(pin=False)
+        self.download(host)
+        torch.cuda.synchronize()
+        dt, t = self.time()
+        boxes = np.full((self.nlevels, max(1, max(len(b) for b in self.patches)), 4), -1, np.int64)
+        for l, bl in enumerate(self.patches):
+            if bl:
+                boxes[l, :len(bl)] = np.asarray(bl, np.int64)
+        np.savez(path, state=host.numpy(), boxes=boxes, npatch=np.array([len(b) for b in self.patches]),
+                 dt=dt, time=t, iteration=int(iteration),
+                 init=np.array(repr(self._init_args)), params=np.array(repr(self.params)))
+
+    @classmethod
+    def load(cls, path):
+        """Engine, iteration from a restart file written by save()."""
+        import ast
+        d = np.load(path)
+        params = ast.literal_eval(str(d["params"]))
+        init = ast.literal_eval(str(d["init"]))
+        E = cls(params, init.pop("nx0"), init.pop("ny0"), init.pop("dx0"), **init)
+        for l in range(E.nlevels):
+            n = int(d["npatch"][l])
+            E.set_patches(l, [tuple(int(v) for v in b) for b in d["boxes"][l, :n]])
+        host = torch.from_numpy(np.ascontiguousarray(d["state"]))
+        assert host.numel() == E.packed_size() and host.dtype == E.dtype
+        E.upload(host)
+        _lib.check(E.L.enl_engine_set_time(E.h, float(d["dt"]), float(d["time"])), "enl_engine_set_time")
+        torch.cuda.synchronize()
+        return E, int(d["iteration"])
 
     def paint_source(self, level, src_type, mode=10, amp=1.0, spread=1.0, pos=(0.0, 0.0), sine_amp=0.0,
                      sine_freq=0.0, segs=None, drive=1.0):

@@ -231,7 +231,7 @@ def evaluate(params, margin, seeds=(100, 101, 102, 103, 104), steps=40, prm=None
     return rows
 
 
-def main(out_dir="gpurun_out", quick=False):
+def main(out_dir="sensor_out", quick=False):
     torch.cuda.set_device(0)
     torch.cuda.set_stream(torch.cuda.Stream())
     prm = default_params()
@@ -295,5 +295,10 @@ def main(out_dir="gpurun_out", quick=False):
 
 
 if __name__ == "__main__":
-    import sys
-    main(quick="--quick" in sys.argv)
+    import argparse
+    ap = argparse.ArgumentParser(description="harvest, train and evaluate the learned switch on the GPU")
+    ap.add_argument("--out", default="sensor_out", help="directory for the network, log and report")
+    ap.add_argument("--quick", action="store_true")
+    a = ap.parse_args()
+    os.makedirs(a.out, exist_ok=True)
+    main(out_dir=a.out, quick=a.quick)

@@ -40,7 +40,7 @@ def gaussian_dp(nx, ny, amp, sigma_cells, cx=None, cy=None):
 
 
 def pulse_patch_state(nx, ny, p, amp_frac=0.1, sigma_cells=8.0, g=3):
-    """Config-1 style patch: ghosted (5, ny+2g, nx+2g) array, interior set."""
+    """Single-pulse patch: ghosted (5, ny+2g, nx+2g) array, interior set."""
     w = np.zeros((5, ny + 2 * g, nx + 2 * g))
     dp = gaussian_dp(nx, ny, amp_frac * p["p0"], sigma_cells)
     w[:, g:g + ny, g:g + nx] = state_from_dp(dp, p)

@@ -266,6 +266,8 @@ int enl_engine_launches_per_step(void* engine, int plain);
 int enl_engine_set_adaptive_dt(void* engine, int on, double cfl);
 /* Last device dt and accumulated simulated time (adaptive mode). */
 int enl_engine_time(void* engine, double* dt_last, double* sim_time);
+/* Restore them (restart). */
+int enl_engine_set_time(void* engine, double dt_last, double sim_time);
 
 /* State exchange with host memory: the current buffer's patch interiors of
  * every level, packed (7 fields, tile order: level by level, patch by patch,

@@ -483,3 +483,31 @@ def test_fp32_state_every_variant_within_budget(ora, variant):
         assert relL2(a[5][m] - prm["p0"], b[5][m] - prm["p0"]) <= 1e-3, (variant, l)
         for k in (1, 2):
             assert relL2(a[k][m], b[k][m]) <= 1e-3, (variant, l, k)
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_restart_roundtrip(ora, tmp_path, precision):
+    """save() / load(): a restarted engine continues exactly like the original."""
+    prm = default_params()
+    nx, ny = 64, 48
+    E, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 31, 0, 47), (32, 63, 0, 47)], [(32, 95, 24, 71)]],
+                     (REFLECT,) * 4, "hybrid_high_llf", precision=precision)
+    E.set_adaptive_dt(True, 0.5)
+    for _ in range(2):
+        E.step(1.0)
+    path = str(tmp_path / "restart.npz")
+    E.save(path, iteration=2)
+    F, it = Engine.load(path)
+    assert it == 2 and F.patches == E.patches and F.dtype == E.dtype
+    F.set_adaptive_dt(True, 0.5)
+    for X in (E, F):
+        for _ in range(2):
+            X.step(1.0)
+    torch.cuda.synchronize()
+    for l in range(2):
+        a, b = E.level_state(l).cpu().numpy(), F.level_state(l).cpu().numpy()
+        for bx in E.patches[l]:
+            sl = (slice(None), slice(bx[2], bx[3] + 1), slice(bx[0], bx[1] + 1))
+            assert np.array_equal(a[sl], b[sl])
+    assert E.time() == F.time()
+    F.close()

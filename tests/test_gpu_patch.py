@@ -224,7 +224,7 @@ def oracle_pulse(ora, prm, variant, nsteps, n=64, perturb=False):
 
 @pytest.mark.parametrize("variant", ["hybrid_high_llf", "weno_low", "drp", "hybrid_low"])
 def test_pulse_multistep_parity(L, ora, variant):
-    """Config-1 physics on a 64x64 patch, reflective walls, SSP-RK3, 60 steps.
+    """Single-pulse physics on a 64x64 patch, reflective walls, SSP-RK3, 60 steps.
 
     The bound is 1e-12, or ten times the reference's own sensitivity when
     that is larger: the oracle rerun from an initial state moved by one ulp
