@@ -2566,6 +2566,112 @@ int enl_engine_tag_blocks(void* e, int level, int block, int buffer, unsigned ch
   return check_launch("tag_blocks");
 }
 
+}  // extern "C"
+
+// Rectangles covering box a minus box r (inclusive boxes as int4 ilo, ihi,
+// jlo, jhi): bottom and top slabs, then the left and right pieces between.
+static void box_subtract(const int4& a, const int4& r, std::vector<int4>& out) {
+  if (r.y < a.x || r.x > a.y || r.w < a.z || r.z > a.w) {
+    out.push_back(a);
+    return;
+  }
+  if (a.z < r.z) out.push_back(make_int4(a.x, a.y, a.z, r.z - 1));
+  if (a.w > r.w) out.push_back(make_int4(a.x, a.y, r.w + 1, a.w));
+  const int j0 = std::max(a.z, r.z), j1 = std::min(a.w, r.w);
+  if (a.x < r.x) out.push_back(make_int4(a.x, r.x - 1, j0, j1));
+  if (a.y > r.y) out.push_back(make_int4(r.y + 1, a.y, j0, j1));
+}
+
+extern "C" {
+
+int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_blocks, double efficiency,
+                      int min_size, int max_size) {
+  Engine* E = (Engine*)e;
+  if (!E || level < 0 || level + 1 >= E->cfg.nlevels || block < 1 || tag_buffer < 0 || nest_blocks < 0 ||
+      min_size < 1 || max_size < 1) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  // tags of `level` folded into blocks (device), then to the host
+  int nbx = 0, nby = 0;
+  enl_engine_tag_blocks(e, level, block, tag_buffer, nullptr, &nbx, &nby);
+  std::vector<unsigned char> bmap((size_t)nbx * nby), allowed((size_t)nbx * nby, 0);
+  int st = enl_engine_tag_blocks(e, level, block, tag_buffer, bmap.data(), &nbx, &nby);
+  if (st != ENL_OK) return st;
+  // blocks lying wholly inside a patch of `level`
+  for (const int4& b : E->lev[level].patches) {
+    const int bx0 = (b.x + block - 1) / block, bx1 = (b.y + 1) / block - 1;
+    const int by0 = (b.z + block - 1) / block, by1 = (b.w + 1) / block - 1;
+    for (int j = by0; j <= by1; ++j)
+      for (int i = bx0; i <= bx1; ++i) allowed[(size_t)j * nbx + i] = 1;
+  }
+  const int cell = block * E->cfg.ratio;  // level+1 cells per block side
+  std::vector<int> cb(4 * 1024);
+  int nb = 0;
+  for (;;) {
+    st = enl_cluster_tags(bmap.data(), allowed.data(), nbx, nby, level > 0 ? nest_blocks : 0, efficiency,
+                          std::max(1, min_size / cell), std::max(1, max_size / cell), cb.data(),
+                          (int)(cb.size() / 4), &nb);
+    if (st == ENL_OK) break;
+    if (nb * 4 <= (int)cb.size()) {
+      set_error(st);
+      return st;
+    }
+    cb.resize((size_t)nb * 4);
+  }
+  const Level& F = E->lev[level + 1];
+  std::vector<int4> fine;
+  for (int q = 0; q < nb; ++q) {
+    const int4 fb = make_int4(cb[4 * q] * cell, std::min(F.nx, (cb[4 * q + 1] + 1) * cell) - 1, cb[4 * q + 2] * cell,
+                              std::min(F.ny, (cb[4 * q + 3] + 1) * cell) - 1);
+    if (fb.y >= fb.x && fb.w >= fb.z) fine.push_back(fb);
+  }
+  // new fine cells (not covered by the old fine patches) are interpolated
+  std::vector<int4> fresh;
+  for (const int4& b : fine) {
+    std::vector<int4> pieces{b}, next;
+    for (const int4& r : F.patches) {
+      next.clear();
+      for (const int4& p : pieces) box_subtract(p, r, next);
+      pieces.swap(next);
+    }
+    fresh.insert(fresh.end(), pieces.begin(), pieces.end());
+  }
+  std::vector<int> flat(4 * fine.size()), flat2(4 * fresh.size());
+  for (size_t q = 0; q < fine.size(); ++q) {
+    flat[4 * q] = fine[q].x;
+    flat[4 * q + 1] = fine[q].y;
+    flat[4 * q + 2] = fine[q].z;
+    flat[4 * q + 3] = fine[q].w;
+  }
+  for (size_t q = 0; q < fresh.size(); ++q) {
+    flat2[4 * q] = fresh[q].x;
+    flat2[4 * q + 1] = fresh[q].y;
+    flat2[4 * q + 2] = fresh[q].z;
+    flat2[4 * q + 3] = fresh[q].w;
+  }
+  st = enl_engine_set_patches(e, level + 1, (int)fine.size(), flat.data());
+  if (st != ENL_OK) return st;
+  return enl_engine_refine_init(e, level + 1, (int)fresh.size(), flat2.data());
+}
+
+int enl_engine_get_patches(void* e, int level, int* boxes, int max_boxes, int* npatch) {
+  Engine* E = (Engine*)e;
+  if (!E || level < 0 || level >= E->cfg.nlevels || !npatch || max_boxes < 0 || (max_boxes > 0 && !boxes)) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  const auto& P = E->lev[level].patches;
+  *npatch = (int)P.size();
+  for (int q = 0; q < (int)P.size() && q < max_boxes; ++q) {
+    boxes[4 * q] = P[q].x;
+    boxes[4 * q + 1] = P[q].y;
+    boxes[4 * q + 2] = P[q].z;
+    boxes[4 * q + 3] = P[q].w;
+  }
+  return (int)P.size() <= max_boxes ? ENL_OK : ENL_ERR_ARG;
+}
+
 int enl_engine_set_mics(void* e, int nmics, const double* xy, long long capacity, int iteration) {
   Engine* E = (Engine*)e;
   if (!E || nmics < 0 || (nmics > 0 && (!xy || capacity < 1))) {

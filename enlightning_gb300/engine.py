@@ -370,8 +370,9 @@ class Hierarchy:
     """
 
     def __init__(self, engine: Engine, min_size=16, max_size=256, tag_buffer=2, efficiency=0.7, block=4,
-                 nest_blocks=1):
+                 nest_blocks=1, native=True):
         self.E = engine
+        self.native = native  # one library call per level (enl_engine_regrid) instead of the steps below
         self.min_size, self.max_size = min_size, max_size
         self.tag_buffer, self.efficiency = tag_buffer, efficiency
         self.block, self.nest_blocks = block, nest_blocks
@@ -428,6 +429,8 @@ class Hierarchy:
         E = self.E
         if level + 1 >= E.nlevels:
             return []
+        if self.native:
+            return self._regrid_native(level)
         fine = self.propose(level)
         old = list(E.patches[level + 1])
         t0 = time.perf_counter()
@@ -439,6 +442,21 @@ class Hierarchy:
         self.timing["tables"] += t1 - t0
         self.timing["refine"] += t2 - t1
         return fine
+
+    def _regrid_native(self, level):
+        """The same regrid in one library call (enl_engine_regrid)."""
+        E = self.E
+        t0 = time.perf_counter()
+        _lib.check(E.L.enl_engine_regrid(E.h, level, self.block, self.tag_buffer, self.nest_blocks,
+                                         float(self.efficiency), self.min_size, self.max_size), "enl_engine_regrid")
+        n = C.c_int()
+        E.L.enl_engine_get_patches(E.h, level + 1, None, 0, C.byref(n))
+        out = np.zeros((max(1, n.value), 4), np.int32)
+        _lib.check(E.L.enl_engine_get_patches(E.h, level + 1, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)),
+                   "enl_engine_get_patches")
+        E.patches[level + 1] = [tuple(int(v) for v in b) for b in out[: n.value]]
+        self.timing["native"] = self.timing.get("native", 0.0) + time.perf_counter() - t0
+        return E.patches[level + 1]
 
     def regrid(self):
         """Regrid every finer level, coarse to fine (regridAllFinerLevels)."""

@@ -100,7 +100,7 @@ def gaussian_spread(sigma):
 
 def line_source(prm, nx0=4096, ny0=2048, dx0=0.5, nlevels=3, seed=100, nseg=200, precision=1,
                 variant="hybrid_high_llf", learned=False, base_patch=256, cfl=0.5, amp_frac=10.0,
-                sigma_cells=2.0, min_size=16, max_size=256):
+                sigma_cells=2.0, min_size=16, max_size=256, native_regrid=True):
     """Thunder-like line source on a multi-level hierarchy (synthetic).
 
     A seeded random-walk channel of `nseg` segments (lengths U(1, 3) m, turns
@@ -123,7 +123,7 @@ def line_source(prm, nx0=4096, ny0=2048, dx0=0.5, nlevels=3, seed=100, nseg=200,
     E = Engine(prm, nx0, ny0, (dx0, dx0), nlevels=nlevels, ratio=2, bc=(ABSORB, ABSORB, REFLECT, ABSORB),
                variant=variant, precision=precision, learned=learned)
     E.set_adaptive_dt(True, cfl)
-    Hy = Hierarchy(E, min_size=min_size, max_size=max_size, tag_buffer=2)
+    Hy = Hierarchy(E, min_size=min_size, max_size=max_size, tag_buffer=2, native=native_regrid)
     Hy.base_patches(base_patch)
     amp = amp_frac * prm["p0"]
     spread = gaussian_spread(sigma_cells * dx0)

@@ -342,6 +342,19 @@ int enl_engine_state_from_overpressure(void* engine, int level);
  * cell within `buffer` cells.  With map_host == NULL only nbx, nby are set. */
 int enl_engine_tag_blocks(void* engine, int level, int block, int buffer,
                           unsigned char* map_host, int* nbx, int* nby);
+/* One regrid of level+1 from the tags of `level` (SAMRAI's gridding step
+ * for the reference, main.C:489-502) in one call: enl_engine_tag_blocks,
+ * proper nesting inside the patches of `level` (eroded by nest_blocks blocks
+ * for level > 0), enl_cluster_tags, fine boxes (block * ratio cells per block
+ * side, sizes min_size..max_size fine cells), enl_engine_set_patches and
+ * enl_engine_refine_init of the cells the old fine patches did not cover. */
+int enl_engine_regrid(void* engine, int level, int block, int tag_buffer,
+                      int nest_blocks, double efficiency, int min_size,
+                      int max_size);
+/* Patch boxes of a level (host array of 4*max_boxes ints); npatch = count. */
+int enl_engine_get_patches(void* engine, int level, int* boxes, int max_boxes,
+                           int* npatch);
+
 /* Virtual microphones, enlightning::recordAudio (enlightning.C:2392-2506):
  * with nmics > 0, every enl_engine_step (and graph replay) ends by sampling
  * the pressure for each microphone (xy: host, x0, y0, x1, y1, ... in metres)

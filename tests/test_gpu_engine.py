@@ -511,3 +511,27 @@ def test_restart_roundtrip(ora, tmp_path, precision):
             assert np.array_equal(a[sl], b[sl])
     assert E.time() == F.time()
     F.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_native_regrid_equals_host_regrid(precision):
+    """enl_engine_regrid (one library call per level) builds the same
+    hierarchy, and the same new fine data, as the host-side steps of
+    Hierarchy (tag map, nesting, clustering, box difference, refine)."""
+    prm = default_params()
+    res = []
+    for native in (False, True):
+        E, H, _ = workloads.line_source(prm, nx0=256, ny0=128, dx0=0.5, nlevels=3, nseg=20, precision=precision,
+                                        base_patch=64, native_regrid=native)
+        for s in range(8):
+            if s and s % 3 == 0:
+                H.regrid()
+            E.step(1.0)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        res.append(([list(b) for b in E.patches], [E.level_state(l).cpu().numpy().copy() for l in range(3)]))
+        E.close()
+    assert res[0][0] == res[1][0]
+    assert len(res[0][0][2]) > 0
+    for a, b in zip(res[0][1], res[1][1]):
+        assert np.array_equal(a, b)
