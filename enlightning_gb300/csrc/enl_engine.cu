@@ -69,6 +69,12 @@ constexpr int kOffPlanesS = 2 * kBufS;
 constexpr int kOffMlpS = kOffPlanesS + kPlanesBytes;
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
 constexpr int kFeatRows = 32;                    // learned switch: cells per network chunk
+// Resident stage blocks per SM with FP32 storage (bounds the registers per
+// thread: 3 blocks of 256 threads leave 80).
+#ifndef ENL_STAGE_BLOCKS_F32
+#define ENL_STAGE_BLOCKS_F32 3
+#endif
+constexpr int kStageBlocksF32 = ENL_STAGE_BLOCKS_F32;
 
 // Absorbing envelope (enlightning.C:634-786) as per-level tables: for each
 // side, env[i] = 1 - exp(-ln2 d^2 / w^2) at the distance d of cell centre i
@@ -261,7 +267,8 @@ __device__ __forceinline__ void raise_health(int* h, int code) { atomicCAS(h, 0,
 // straight into the FP32 tile and the whole cell update is single precision.
 // ---------------------------------------------------------------------------
 template <int SCHEME, int ORDER, bool LLF, bool FAST, typename S>
-__global__ void __launch_bounds__(256, std::is_same<S, float>::value ? 3 : 2) stage_kernel(const __grid_constant__ StageArgs A) {
+__global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlocksF32 : 2)
+    stage_kernel(const __grid_constant__ StageArgs A) {
   constexpr bool kF32S = std::is_same<S, float>::value;
   static_assert(!kF32S || FAST, "single-precision storage runs the FP32 right-hand side");
   extern __shared__ __align__(128) unsigned char smem_raw[];
