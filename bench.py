@@ -820,6 +820,8 @@ def run_linesource(args):
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "clocks": clk.summary(), "gpu_launches": launches,
+        "gpu_launches_counted": "kernels of the timed steps (graph replays); the regrids inside the timed "
+                                "region launch more (tagging, tag blocks, refine) and are not counted",
     }
     print(json.dumps(line), flush=True)
 
