@@ -535,3 +535,44 @@ def test_native_regrid_equals_host_regrid(precision):
     assert len(res[0][0][2]) > 0
     for a, b in zip(res[0][1], res[1][1]):
         assert np.array_equal(a, b)
+
+
+def test_four_levels_fp32_state_within_budget(ora):
+    """The deepest hierarchy the engine takes (ENL_MAX_LEVELS = 4) in FP32
+    storage against FP64, with a regrid between steps."""
+    prm = default_params()
+    out = {}
+    for prec in (PREC_FP64, PREC_FP32_STATE):
+        E, H, _ = workloads.line_source(prm, nx0=128, ny0=64, dx0=1.0, nlevels=4, nseg=12, precision=prec,
+                                        base_patch=64)
+        assert all(len(E.patches[l]) > 0 for l in range(4))
+        for s in range(6):
+            if s == 3:
+                H.regrid()
+            E.step(1.0)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        out[prec] = E.level_state(0).cpu().numpy().copy()
+        E.close()
+    a, b = out[PREC_FP32_STATE], out[PREC_FP64]
+    assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) <= 1e-3
+    assert relL2(a[5] - prm["p0"], b[5] - prm["p0"]) <= 1e-3
+
+
+def test_independent_problems_fp32_state_within_budget(ora):
+    """Batched independent pulses in FP32 storage against the FP64 engine."""
+    prm = default_params()
+    out = {}
+    for prec in (PREC_FP64, PREC_FP32_STATE):
+        E, boxes, info = workloads.pulse_batch(prm, seed=5, n=4, side_range=(32, 128), precision=prec, width=640)
+        for _ in range(8):
+            E.step(info["dt"])
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        out[prec] = E.level_state(0).cpu().numpy().copy()
+        E.close()
+    a, b = out[PREC_FP32_STATE], out[PREC_FP64]
+    for bx in boxes:
+        sl = (slice(bx[2], bx[3] + 1), slice(bx[0], bx[1] + 1))
+        assert relL2(a[0][sl] - prm["rho0"], b[0][sl] - prm["rho0"]) <= 1e-3
+        assert relL2(a[1][sl], b[1][sl]) <= 1e-3
