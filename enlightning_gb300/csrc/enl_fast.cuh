@@ -117,8 +117,15 @@ __device__ __forceinline__ void sources_fast(const ACC& A, const FastConst& P, f
 
 // LLF-split WENO derivative of field k at the cell, plus its source term hk:
 // KK_k = hk - (dF/dx + dG/dy), from the staged fluxes and the cell's speeds.
+// Out of line by default: one copy of the code for the five fields keeps the
+// caller's registers and code size small (ENL_WENO_INLINE inlines it).
+#ifdef ENL_WENO_INLINE
+#define ENL_WENO_FN __device__ __forceinline__
+#else
+#define ENL_WENO_FN __device__ __noinline__
+#endif
 template <int ORDER, class ACC>
-__device__ __noinline__ float weno_field(const ACC A, const FastConst& P, int k, float af, float ag, float hk) {
+ENL_WENO_FN float weno_field(const ACC A, const FastConst& P, int k, float af, float ag, float hk) {
   float fp[7], fm[7], gp[7], gm[7];
 #pragma unroll
   for (int q = 0; q < 7; ++q) {
