@@ -78,6 +78,7 @@ ENGINE_SIGNATURES = {
     "enl_engine_graph_valid": (C.c_int, [C.c_void_p]),
     "enl_engine_regrid": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]),
     "enl_engine_get_patches": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "enl_engine_regrid_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "enl_engine_set_time": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
     "enl_engine_set_mics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.c_int]),
     "enl_engine_mic_records": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),

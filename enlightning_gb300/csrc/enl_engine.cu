@@ -15,6 +15,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -1455,6 +1456,7 @@ struct Engine {
   bool f32s = false;
   size_t esize = 8;
   double* d_env[kL][4] = {};  // absorbing-envelope tables (null: side not ABSORB)
+  double regrid_ms[5] = {0, 0, 0, 0, 0};  // host wall time of enl_engine_regrid phases
   void* stage_host = nullptr;  // pinned staging of the tables
   size_t stage_cap = 0;
   cudaEvent_t stage_ev = nullptr;
@@ -2599,12 +2601,18 @@ int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_bl
     set_error(ENL_ERR_ARG);
     return ENL_ERR_ARG;
   }
+  using clk = std::chrono::steady_clock;
+  auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+  const auto t0 = clk::now();
+  cudaStreamSynchronize(stream());  // the steps already queued (timed apart from the regrid's own work)
+  const auto t1 = clk::now();
   // tags of `level` folded into blocks (device), then to the host
   int nbx = 0, nby = 0;
   enl_engine_tag_blocks(e, level, block, tag_buffer, nullptr, &nbx, &nby);
   std::vector<unsigned char> bmap((size_t)nbx * nby), allowed((size_t)nbx * nby, 0);
   int st = enl_engine_tag_blocks(e, level, block, tag_buffer, bmap.data(), &nbx, &nby);
   if (st != ENL_OK) return st;
+  const auto t2 = clk::now();
   // blocks lying wholly inside a patch of `level`
   for (const int4& b : E->lev[level].patches) {
     const int bx0 = (b.x + block - 1) / block, bx1 = (b.y + 1) / block - 1;
@@ -2627,6 +2635,7 @@ int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_bl
     cb.resize((size_t)nb * 4);
   }
   const Level& F = E->lev[level + 1];
+  const auto t3 = clk::now();
   std::vector<int4> fine;
   for (int q = 0; q < nb; ++q) {
     const int4 fb = make_int4(cb[4 * q] * cell, std::min(F.nx, (cb[4 * q + 1] + 1) * cell) - 1, cb[4 * q + 2] * cell,
@@ -2659,7 +2668,25 @@ int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_bl
   }
   st = enl_engine_set_patches(e, level + 1, (int)fine.size(), flat.data());
   if (st != ENL_OK) return st;
-  return enl_engine_refine_init(e, level + 1, (int)fresh.size(), flat2.data());
+  const auto t4 = clk::now();
+  st = enl_engine_refine_init(e, level + 1, (int)fresh.size(), flat2.data());
+  const auto t5 = clk::now();
+  const double ph[5] = {ms(t0, t1), ms(t1, t2), ms(t2, t3), ms(t3, t4), ms(t4, t5)};
+  for (int q = 0; q < 5; ++q) E->regrid_ms[q] += ph[q];
+  return st;
+}
+
+int enl_engine_regrid_timing(void* e, double* ms5) {
+  Engine* E = (Engine*)e;
+  if (!E || !ms5) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  for (int q = 0; q < 5; ++q) {
+    ms5[q] = E->regrid_ms[q];
+    E->regrid_ms[q] = 0.0;
+  }
+  return ENL_OK;
 }
 
 int enl_engine_get_patches(void* e, int level, int* boxes, int max_boxes, int* npatch) {

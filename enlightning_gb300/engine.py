@@ -456,6 +456,10 @@ class Hierarchy:
                    "enl_engine_get_patches")
         E.patches[level + 1] = [tuple(int(v) for v in b) for b in out[: n.value]]
         self.timing["native"] = self.timing.get("native", 0.0) + time.perf_counter() - t0
+        ph = (C.c_double * 5)()
+        E.L.enl_engine_regrid_timing(E.h, ph)
+        for k, v in zip(("queue_wait", "tag", "cluster", "tables", "refine"), ph):
+            self.timing["native_" + k] = self.timing.get("native_" + k, 0.0) + v * 1e-3
         return E.patches[level + 1]
 
     def regrid(self):

@@ -351,6 +351,10 @@ int enl_engine_tag_blocks(void* engine, int level, int block, int buffer,
 int enl_engine_regrid(void* engine, int level, int block, int tag_buffer,
                       int nest_blocks, double efficiency, int min_size,
                       int max_size);
+/* Host wall time (ms) spent in enl_engine_regrid since the last call, by
+ * phase: waiting for the steps already queued, device tagging with the block
+ * map read back, clustering, tables, refine launches; then reset. */
+int enl_engine_regrid_timing(void* engine, double* ms5);
 /* Patch boxes of a level (host array of 4*max_boxes ints); npatch = count. */
 int enl_engine_get_patches(void* engine, int level, int* boxes, int max_boxes,
                            int* npatch);
