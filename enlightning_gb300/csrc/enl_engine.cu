@@ -1059,21 +1059,41 @@ __global__ void overpressure_state_kernel(CanvasT<S> V, CanvasT<S> H, const int4
 
 // Block map of tags for regridding: map[by][bx] = 1 if any tagged cell lies
 // within `buf` cells of the block (tag buffering folded into the reduction).
+// bbox (device, 4 ints: min bx, max bx, min by, max by; preset to an empty
+// box) receives the bounding box of the tagged blocks, one atomic per warp.
 __global__ void tag_block_kernel(const int* tags, int nx, int ny, int B, int buf, unsigned char* map, int nbx,
-                                 int nby) {
-  long n = (long)nbx * nby;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    int bx = (int)(t % nbx), by = (int)(t / nbx);
-    int i0 = max(0, bx * B - buf), i1 = min(nx - 1, (bx + 1) * B - 1 + buf);
-    int j0 = max(0, by * B - buf), j1 = min(ny - 1, (by + 1) * B - 1 + buf);
+                                 int nby, int* bbox) {
+  const long n = (long)nbx * nby;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long t0 = blockIdx.x * (long)blockDim.x; t0 < n; t0 += stride) {  // trip count uniform per warp
+    const long t = t0 + threadIdx.x;
     unsigned char any = 0;
-    for (int j = j0; j <= j1 && !any; ++j)
-      for (int i = i0; i <= i1; ++i)
-        if (tags[(long)j * nx + i]) {
-          any = 1;
-          break;
-        }
-    map[t] = any;
+    int bx = 0, by = 0;
+    if (t < n) {
+      bx = (int)(t % nbx);
+      by = (int)(t / nbx);
+      const int i0 = max(0, bx * B - buf), i1 = min(nx - 1, (bx + 1) * B - 1 + buf);
+      const int j0 = max(0, by * B - buf), j1 = min(ny - 1, (by + 1) * B - 1 + buf);
+      for (int j = j0; j <= j1 && !any; ++j)
+        for (int i = i0; i <= i1; ++i)
+          if (tags[(long)j * nx + i]) {
+            any = 1;
+            break;
+          }
+      map[t] = any;
+    }
+    if (__ballot_sync(0xffffffffu, any)) {
+      const int x0 = __reduce_min_sync(0xffffffffu, any ? bx : 0x7fffffff);
+      const int x1 = __reduce_max_sync(0xffffffffu, any ? bx : -1);
+      const int y0 = __reduce_min_sync(0xffffffffu, any ? by : 0x7fffffff);
+      const int y1 = __reduce_max_sync(0xffffffffu, any ? by : -1);
+      if ((threadIdx.x & 31) == 0) {
+        atomicMin(&bbox[0], x0);
+        atomicMax(&bbox[1], x1);
+        atomicMin(&bbox[2], y0);
+        atomicMax(&bbox[3], y1);
+      }
+    }
   }
 }
 
@@ -1415,6 +1435,8 @@ struct Engine {
   std::vector<int4> h_patchtab;              // patch boxes, all levels
   std::vector<int> patch_off, patch_cnt;
   int h_meta[M_SIZE];
+  int tables_from = 0;            // first level whose tables are out of date
+  bool tables_on_device = false;  // the device tables hold the kept levels
   DevArray<int4> d_tiles, d_halo, d_ctiles, d_patchtab;
   int* d_meta = nullptr;
   int* d_counters = nullptr;   // 3 stage counters
@@ -1424,6 +1446,7 @@ struct Engine {
   bool graph_valid = false;
   int* d_tags[kL] = {nullptr, nullptr, nullptr, nullptr};  // tag scratch per level
   unsigned char* d_bmap = nullptr;
+  int* d_bbox = nullptr;  // bounding box of the tagged blocks of the last block map
   size_t bmap_cap = 0;
   double* d_segs = nullptr;
   size_t segs_cap = 0;
@@ -1507,24 +1530,44 @@ static void tiles_of_box(int4 b, int level, int pid, std::vector<int4>& out) {
 }
 
 // Row segments of the cells within distance 3 (Chebyshev) of the patch union,
-// inside [0,nx)x[0,ny), not covered by any patch.
+// inside [0,nx)x[0,ny), not covered by any patch, in row order and, within a
+// row, left to right.  Rows where no patch starts or ends (grown or not) have
+// the same segments, so they are computed once per band of such rows, from
+// the patches whose grown rows hold the band (a sweep over the patches in
+// order of their first grown row): O(bands x active patches), not
+// O(rows x patches).
 static void halo_segments(const std::vector<int4>& P, int nx, int ny, std::vector<int4>& out) {
   if (P.empty()) return;
-  // rows touched by the grown patches, each with its grown and covered intervals
-  int j0 = ny, j1 = -1;
+  std::vector<int> cuts;  // first rows of the bands
+  cuts.reserve(4 * P.size());
   for (auto& b : P) {
-    j0 = std::min(j0, std::max(0, b.z - 3));
-    j1 = std::max(j1, std::min(ny - 1, b.w + 3));
+    cuts.push_back(std::max(0, b.z - 3));
+    cuts.push_back(b.z);
+    cuts.push_back(b.w + 1);
+    cuts.push_back(std::min(ny, b.w + 4));
   }
-  std::vector<std::vector<std::pair<int, int>>> grow(j1 - j0 + 1), cover(j1 - j0 + 1);
-  for (auto& b : P) {
-    for (int j = std::max(0, b.z - 3); j <= std::min(ny - 1, b.w + 3); ++j)
-      grow[j - j0].push_back({std::max(0, b.x - 3), std::min(nx - 1, b.y + 3)});
-    for (int j = b.z; j <= b.w; ++j) cover[j - j0].push_back({b.x, b.y});
-  }
-  std::vector<std::pair<int, int>> gm;
-  for (int j = j0; j <= j1; ++j) {
-    auto& g = grow[j - j0];
+  std::sort(cuts.begin(), cuts.end());
+  cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+  std::vector<int> order(P.size()), active;
+  for (size_t q = 0; q < P.size(); ++q) order[q] = (int)q;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return P[a].z < P[b].z; });
+  size_t next = 0;
+  std::vector<std::pair<int, int>> g, gm, cv;
+  std::vector<int4> seg;  // one row's segments (.x = row, filled per row)
+  for (size_t k = 0; k + 1 < cuts.size(); ++k) {
+    const int r0 = cuts[k], r1 = std::min(cuts[k + 1], ny);  // rows [r0, r1)
+    if (r0 >= r1) continue;
+    while (next < order.size() && std::max(0, P[order[next]].z - 3) <= r0) active.push_back(order[next++]);
+    active.erase(std::remove_if(active.begin(), active.end(),
+                                [&](int q) { return std::min(ny - 1, P[q].w + 3) < r0; }),
+                 active.end());
+    g.clear();
+    cv.clear();
+    for (int q : active) {
+      const int4& b = P[q];
+      g.push_back({std::max(0, b.x - 3), std::min(nx - 1, b.y + 3)});
+      if (r0 >= b.z && r0 <= b.w) cv.push_back({b.x, b.y});
+    }
     if (g.empty()) continue;
     std::sort(g.begin(), g.end());
     gm.clear();  // merged grown intervals
@@ -1532,32 +1575,47 @@ static void halo_segments(const std::vector<int4>& P, int nx, int ny, std::vecto
       if (!gm.empty() && iv.first <= gm.back().second + 1) gm.back().second = std::max(gm.back().second, iv.second);
       else gm.push_back(iv);
     }
-    auto& cv = cover[j - j0];
     std::sort(cv.begin(), cv.end());
+    seg.clear();
     for (auto& iv : gm) {
       int a = iv.first;
       for (auto& c : cv) {
         if (c.second < a || c.first > iv.second) continue;
-        if (c.first > a) out.push_back(make_int4(j, a, c.first - 1, 0));
+        if (c.first > a) seg.push_back(make_int4(0, a, c.first - 1, 0));
         a = std::max(a, c.second + 1);
       }
-      if (a <= iv.second) out.push_back(make_int4(j, a, iv.second, 0));
+      if (a <= iv.second) seg.push_back(make_int4(0, a, iv.second, 0));
     }
+    for (int j = r0; j < r1; ++j)
+      for (const int4& q : seg) out.push_back(make_int4(j, q.y, q.z, 0));
   }
 }
 
+// Host and device patch, tile, halo and coarsen tables.  Levels below
+// E->tables_from are unchanged since the last rebuild: their entries (at the
+// front of every table) are kept on the host and, unless a device table was
+// reallocated, on the device; only the rest is rebuilt and copied.
 static int rebuild_tables(Engine* E) {
   const int nl = E->cfg.nlevels;
-  E->h_tiles.clear();
-  E->h_halo.clear();
-  E->h_ctiles.clear();
-  E->h_patchtab.clear();
-  E->tile_off.assign(nl, 0);
-  E->tile_cnt.assign(nl, 0);
-  E->patch_off.assign(nl, 0);
-  E->patch_cnt.assign(nl, 0);
-  memset(E->h_meta, 0, sizeof(E->h_meta));
-  for (int l = 0; l < nl; ++l) {
+  const int l0 = std::min(E->tables_from, nl);
+  if (l0 == 0) {
+    E->tile_off.assign(nl, 0);
+    E->tile_cnt.assign(nl, 0);
+    E->patch_off.assign(nl, 0);
+    E->patch_cnt.assign(nl, 0);
+    memset(E->h_meta, 0, sizeof(E->h_meta));
+  }
+  // truncate every table to the kept levels
+  const size_t keep_tiles = l0 < nl ? (size_t)E->tile_off[l0] : E->h_tiles.size();
+  const size_t keep_pt = l0 < nl ? (size_t)E->patch_off[l0] : E->h_patchtab.size();
+  const size_t keep_halo = l0 < nl ? (size_t)E->h_meta[M_HALO_OFF + l0] : E->h_halo.size();
+  const size_t keep_ct = l0 < nl ? (size_t)E->h_meta[M_CT_OFF + l0] : E->h_ctiles.size();
+  E->h_tiles.resize(keep_tiles);
+  E->h_tileoff.resize(keep_tiles);
+  E->h_patchtab.resize(keep_pt);
+  E->h_halo.resize(keep_halo);
+  E->h_ctiles.resize(keep_ct);
+  for (int l = l0; l < nl; ++l) {
     E->tile_off[l] = (int)E->h_tiles.size();
     E->patch_off[l] = (int)E->h_patchtab.size();
     for (auto& b : E->lev[l].patches) {
@@ -1591,23 +1649,34 @@ static int rebuild_tables(Engine* E) {
   E->h_meta[M_PATCH_OFF + kL] = (int)E->h_patchtab.size();
   E->h_tileoff.resize(E->h_tiles.size());
   long long acc = 0;
-  for (size_t q = 0; q < E->h_tiles.size(); ++q) {
+  if (keep_tiles > 0) {
+    const int4 td = E->h_tiles[keep_tiles - 1];
+    acc = E->h_tileoff[keep_tiles - 1] + (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
+  }
+  for (size_t q = keep_tiles; q < E->h_tiles.size(); ++q) {
     E->h_tileoff[q] = acc;
     int4 td = E->h_tiles[q];
     acc += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
   }
+  E->tables_from = nl;
   bool grew = false;
-  E->d_tileoff.ensure(std::max<size_t>(E->h_tileoff.size(), 1));
+  const bool off_grew = E->d_tileoff.ensure(std::max<size_t>(E->h_tileoff.size(), 1));
   grew |= E->d_tiles.ensure(std::max<size_t>(E->h_tiles.size(), 1));
   grew |= E->d_halo.ensure(std::max<size_t>(E->h_halo.size(), 1));
   grew |= E->d_ctiles.ensure(std::max<size_t>(E->h_ctiles.size(), 1));
   grew |= E->d_patchtab.ensure(std::max<size_t>(E->h_patchtab.size(), 1));
   if (grew) E->graph_valid = false;
+  // entries kept on the device: none when a table was reallocated (its old
+  // contents are gone) or when the tables were never copied
+  const bool keep_dev = !grew && !off_grew && E->tables_on_device;
+  const size_t k_tiles = keep_dev ? keep_tiles : 0, k_halo = keep_dev ? keep_halo : 0,
+               k_ct = keep_dev ? keep_ct : 0, k_pt = keep_dev ? keep_pt : 0;
   // one pinned staging buffer for all tables, copied asynchronously; the
   // previous rebuild's copies must have left it before it is rewritten
-  const size_t b_off = E->h_tileoff.size() * sizeof(long long), b_tiles = E->h_tiles.size() * sizeof(int4),
-               b_halo = E->h_halo.size() * sizeof(int4), b_ct = E->h_ctiles.size() * sizeof(int4),
-               b_pt = E->h_patchtab.size() * sizeof(int4), b_meta = sizeof(E->h_meta);
+  const size_t b_off = (E->h_tileoff.size() - k_tiles) * sizeof(long long),
+               b_tiles = (E->h_tiles.size() - k_tiles) * sizeof(int4),
+               b_halo = (E->h_halo.size() - k_halo) * sizeof(int4), b_ct = (E->h_ctiles.size() - k_ct) * sizeof(int4),
+               b_pt = (E->h_patchtab.size() - k_pt) * sizeof(int4), b_meta = sizeof(E->h_meta);
   const size_t need = b_off + b_tiles + b_halo + b_ct + b_pt + b_meta;
   if (E->stage_ev) cudaEventSynchronize(E->stage_ev);
   if (need > E->stage_cap) {
@@ -1629,13 +1698,14 @@ static int rebuild_tables(Engine* E) {
     cudaMemcpyAsync(dst, h, n, cudaMemcpyHostToDevice, s);
     h += n;
   };
-  put(E->d_tileoff.p, E->h_tileoff.data(), b_off);
-  put(E->d_tiles.p, E->h_tiles.data(), b_tiles);
-  put(E->d_halo.p, E->h_halo.data(), b_halo);
-  put(E->d_ctiles.p, E->h_ctiles.data(), b_ct);
-  put(E->d_patchtab.p, E->h_patchtab.data(), b_pt);
+  put(E->d_tileoff.p + k_tiles, E->h_tileoff.data() + k_tiles, b_off);
+  put(E->d_tiles.p + k_tiles, E->h_tiles.data() + k_tiles, b_tiles);
+  put(E->d_halo.p + k_halo, E->h_halo.data() + k_halo, b_halo);
+  put(E->d_ctiles.p + k_ct, E->h_ctiles.data() + k_ct, b_ct);
+  put(E->d_patchtab.p + k_pt, E->h_patchtab.data() + k_pt, b_pt);
   put(E->d_meta, E->h_meta, b_meta);
   cudaEventRecord(E->stage_ev, s);
+  E->tables_on_device = true;
   return check_launch("engine tables");
 }
 
@@ -2184,6 +2254,7 @@ int enl_engine_destroy(void* e) {
   for (int l = 0; l < kL; ++l)
     if (E->d_tags[l]) cudaFree(E->d_tags[l]);
   if (E->d_bmap) cudaFree(E->d_bmap);
+  if (E->d_bbox) cudaFree(E->d_bbox);
   if (E->d_dt) cudaFree(E->d_dt);
   if (E->d_mlp) cudaFree(E->d_mlp);
   if (E->d_packed) cudaFree(E->d_packed);
@@ -2239,6 +2310,7 @@ int enl_engine_set_patches(void* e, int level, int npatch, const int* boxes) {
     P.push_back(b);
   }
   L.patches = P;
+  E->tables_from = std::min(E->tables_from, level);
   return rebuild_tables(E);
 }
 
@@ -2536,6 +2608,45 @@ int enl_engine_state_from_overpressure(void* e, int level) {
   return check_launch("state_from_overpressure");
 }
 
+// tag_cells on `level` and its block map (tags buffered by `buffer` cells)
+// into E->d_bmap, with the tagged blocks' bounding box in E->d_bbox; no copy
+// to the host and no synchronisation.
+static int tag_blocks_device(Engine* E, int level, int block, int buffer) {
+  Level& L = E->lev[level];
+  const int nbx = (L.nx + block - 1) / block, nby = (L.ny + block - 1) / block;
+  cudaStream_t s = stream();
+  if (!E->d_tags[level]) {
+    if (cudaMalloc(&E->d_tags[level], (size_t)L.nx * L.ny * sizeof(int)) != cudaSuccess) {
+      E->d_tags[level] = nullptr;
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+  }
+  const size_t nb = (size_t)nbx * nby;
+  if (nb > E->bmap_cap) {
+    if (E->d_bmap) cudaFree(E->d_bmap);
+    if (cudaMalloc(&E->d_bmap, nb) != cudaSuccess) {
+      E->d_bmap = nullptr;
+      E->bmap_cap = 0;
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+    E->bmap_cap = nb;
+  }
+  if (!E->d_bbox && cudaMalloc(&E->d_bbox, 4 * sizeof(int)) != cudaSuccess) {
+    E->d_bbox = nullptr;
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  int st = enl_engine_tag(E, level, E->d_tags[level]);
+  if (st != ENL_OK) return st;
+  static const int empty[4] = {0x7fffffff, -1, 0x7fffffff, -1};
+  cudaMemcpyAsync(E->d_bbox, empty, sizeof(empty), cudaMemcpyHostToDevice, s);
+  tag_block_kernel<<<E->nsm * 4, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, buffer, E->d_bmap, nbx, nby,
+                                              E->d_bbox);
+  return check_launch("tag_blocks");
+}
+
 int enl_engine_tag_blocks(void* e, int level, int block, int buffer, unsigned char* map_host, int* nbx_out,
                           int* nby_out) {
   Engine* E = (Engine*)e;
@@ -2548,30 +2659,10 @@ int enl_engine_tag_blocks(void* e, int level, int block, int buffer, unsigned ch
   if (nbx_out) *nbx_out = nbx;
   if (nby_out) *nby_out = nby;
   if (!map_host) return ENL_OK;  // size query
-  cudaStream_t s = stream();
-  if (!E->d_tags[level]) {
-    if (cudaMalloc(&E->d_tags[level], (size_t)L.nx * L.ny * sizeof(int)) != cudaSuccess) {
-      E->d_tags[level] = nullptr;
-      set_error(ENL_ERR_CUDA);
-      return ENL_ERR_CUDA;
-    }
-  }
-  size_t nb = (size_t)nbx * nby;
-  if (nb > E->bmap_cap) {
-    if (E->d_bmap) cudaFree(E->d_bmap);
-    if (cudaMalloc(&E->d_bmap, nb) != cudaSuccess) {
-      E->d_bmap = nullptr;
-      E->bmap_cap = 0;
-      set_error(ENL_ERR_CUDA);
-      return ENL_ERR_CUDA;
-    }
-    E->bmap_cap = nb;
-  }
-  int st = enl_engine_tag(e, level, E->d_tags[level]);
+  int st = tag_blocks_device(E, level, block, buffer);
   if (st != ENL_OK) return st;
-  tag_block_kernel<<<E->nsm * 4, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, buffer, E->d_bmap, nbx, nby);
-  cudaMemcpyAsync(map_host, E->d_bmap, nb, cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
+  cudaMemcpyAsync(map_host, E->d_bmap, (size_t)nbx * nby, cudaMemcpyDeviceToHost, stream());
+  cudaStreamSynchronize(stream());
   return check_launch("tag_blocks");
 }
 
@@ -2606,40 +2697,59 @@ int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_bl
   const auto t0 = clk::now();
   cudaStreamSynchronize(stream());  // the steps already queued (timed apart from the regrid's own work)
   const auto t1 = clk::now();
-  // tags of `level` folded into blocks (device), then to the host
-  int nbx = 0, nby = 0;
-  enl_engine_tag_blocks(e, level, block, tag_buffer, nullptr, &nbx, &nby);
-  std::vector<unsigned char> bmap((size_t)nbx * nby), allowed((size_t)nbx * nby, 0);
-  int st = enl_engine_tag_blocks(e, level, block, tag_buffer, bmap.data(), &nbx, &nby);
+  // tags of `level` folded into blocks on the device; only the window of the
+  // tagged blocks' bounding box, grown by the nesting erosion, comes back
+  const Level& C = E->lev[level];
+  const int nbx = (C.nx + block - 1) / block, nby = (C.ny + block - 1) / block;
+  int st = tag_blocks_device(E, level, block, tag_buffer);
   if (st != ENL_OK) return st;
+  int bb[4];
+  cudaMemcpyAsync(bb, E->d_bbox, sizeof(bb), cudaMemcpyDeviceToHost, stream());
+  cudaStreamSynchronize(stream());
   const auto t2 = clk::now();
-  // blocks lying wholly inside a patch of `level`
-  for (const int4& b : E->lev[level].patches) {
-    const int bx0 = (b.x + block - 1) / block, bx1 = (b.y + 1) / block - 1;
-    const int by0 = (b.z + block - 1) / block, by1 = (b.w + 1) / block - 1;
-    for (int j = by0; j <= by1; ++j)
-      for (int i = bx0; i <= bx1; ++i) allowed[(size_t)j * nbx + i] = 1;
-  }
+  // The clusterer works inside the bounding box of the tags that survive the
+  // nesting mask, and eroding a block reads `passes` blocks around it: a
+  // window of the tags' bounding box grown by `passes` (clamped to the map,
+  // where the full map has its edge too) gives the boxes of the full map.
+  const int passes = level > 0 ? nest_blocks : 0;
   const int cell = block * E->cfg.ratio;  // level+1 cells per block side
   std::vector<int> cb(4 * 1024);
-  int nb = 0;
-  for (;;) {
-    st = enl_cluster_tags(bmap.data(), allowed.data(), nbx, nby, level > 0 ? nest_blocks : 0, efficiency,
-                          std::max(1, min_size / cell), std::max(1, max_size / cell), cb.data(),
-                          (int)(cb.size() / 4), &nb);
-    if (st == ENL_OK) break;
-    if (nb * 4 <= (int)cb.size()) {
-      set_error(st);
-      return st;
+  int nb = 0, wx0 = 0, wy0 = 0;
+  if (bb[1] >= bb[0] && bb[3] >= bb[2]) {
+    wx0 = std::max(0, bb[0] - passes);
+    wy0 = std::max(0, bb[2] - passes);
+    const int wx1 = std::min(nbx - 1, bb[1] + passes), wy1 = std::min(nby - 1, bb[3] + passes);
+    const int ww = wx1 - wx0 + 1, wh = wy1 - wy0 + 1;
+    std::vector<unsigned char> bmap((size_t)ww * wh), allowed((size_t)ww * wh, 0);
+    cudaMemcpy2DAsync(bmap.data(), ww, E->d_bmap + (size_t)wy0 * nbx + wx0, nbx, ww, wh, cudaMemcpyDeviceToHost,
+                      stream());
+    // blocks lying wholly inside a patch of `level`, in window coordinates
+    for (const int4& b : C.patches) {
+      const int bx0 = std::max((b.x + block - 1) / block, wx0), bx1 = std::min((b.y + 1) / block - 1, wx1);
+      const int by0 = std::max((b.z + block - 1) / block, wy0), by1 = std::min((b.w + 1) / block - 1, wy1);
+      for (int j = by0; j <= by1; ++j)
+        for (int i = bx0; i <= bx1; ++i) allowed[(size_t)(j - wy0) * ww + (i - wx0)] = 1;
     }
-    cb.resize((size_t)nb * 4);
+    cudaStreamSynchronize(stream());
+    st = check_launch("regrid tags");
+    if (st != ENL_OK) return st;
+    for (;;) {
+      st = enl_cluster_tags(bmap.data(), allowed.data(), ww, wh, passes, efficiency, std::max(1, min_size / cell),
+                            std::max(1, max_size / cell), cb.data(), (int)(cb.size() / 4), &nb);
+      if (st == ENL_OK) break;
+      if (nb * 4 <= (int)cb.size()) {
+        set_error(st);
+        return st;
+      }
+      cb.resize((size_t)nb * 4);
+    }
   }
   const Level& F = E->lev[level + 1];
   const auto t3 = clk::now();
   std::vector<int4> fine;
   for (int q = 0; q < nb; ++q) {
-    const int4 fb = make_int4(cb[4 * q] * cell, std::min(F.nx, (cb[4 * q + 1] + 1) * cell) - 1, cb[4 * q + 2] * cell,
-                              std::min(F.ny, (cb[4 * q + 3] + 1) * cell) - 1);
+    const int4 fb = make_int4((wx0 + cb[4 * q]) * cell, std::min(F.nx, (wx0 + cb[4 * q + 1] + 1) * cell) - 1,
+                              (wy0 + cb[4 * q + 2]) * cell, std::min(F.ny, (wy0 + cb[4 * q + 3] + 1) * cell) - 1);
     if (fb.y >= fb.x && fb.w >= fb.z) fine.push_back(fb);
   }
   // new fine cells (not covered by the old fine patches) are interpolated

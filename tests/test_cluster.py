@@ -108,3 +108,33 @@ def test_native_clustering_edge_cases():
     assert cluster_tags_native(full, max_size=64) == cluster_tags(full, max_size=64)
     nothing_allowed = np.zeros((5, 7), bool)
     assert cluster_tags_native(one, allowed=nothing_allowed) == []
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_native_clustering_of_the_tag_window(seed):
+    """The native regrid clusters only the window of the tagged blocks'
+    bounding box grown by the erosion passes (clamped to the map) and shifts
+    the boxes back: the same boxes as clustering the whole map."""
+    from enlightning_gb300.cluster import cluster_tags_native
+    rng = np.random.default_rng(2000 + seed)
+    ny, nx = int(rng.integers(30, 120)), int(rng.integers(30, 160))
+    tags = np.zeros((ny, nx), bool)
+    sub = _random_tag_map(rng, ny // 2, nx // 2, ["blobs", "walk", "noise"][seed % 3])
+    y0, x0 = int(rng.integers(0, ny - ny // 2 + 1)), int(rng.integers(0, nx - nx // 2 + 1))
+    tags[y0:y0 + ny // 2, x0:x0 + nx // 2] = sub
+    allowed = np.ones((ny, nx), bool)
+    for _ in range(4):
+        ax, ay = rng.integers(0, nx), rng.integers(0, ny)
+        allowed[ay:ay + rng.integers(1, 20), ax:ax + rng.integers(1, 30)] = False
+    kw = dict(efficiency=float(rng.choice([0.5, 0.7, 0.9])), min_size=int(rng.integers(1, 5)),
+              max_size=int(rng.integers(4, 40)))
+    if not tags.any():
+        return
+    jj, ii = np.nonzero(tags)
+    for passes in (0, 1, 2, 3):
+        full = cluster_tags_native(tags, allowed=allowed, nest_erode=passes, **kw)
+        wx0, wx1 = max(0, ii.min() - passes), min(nx - 1, ii.max() + passes)
+        wy0, wy1 = max(0, jj.min() - passes), min(ny - 1, jj.max() + passes)
+        win = cluster_tags_native(tags[wy0:wy1 + 1, wx0:wx1 + 1], allowed=allowed[wy0:wy1 + 1, wx0:wx1 + 1],
+                                  nest_erode=passes, **kw)
+        assert [(a + wx0, b + wx0, c + wy0, d + wy0) for a, b, c, d in win] == full
