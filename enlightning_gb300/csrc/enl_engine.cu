@@ -1059,8 +1059,81 @@ __global__ void overpressure_state_kernel(CanvasT<S> V, CanvasT<S> H, const int4
 
 // Block map of tags for regridding: map[by][bx] = 1 if any tagged cell lies
 // within `buf` cells of the block (tag buffering folded into the reduction).
-// bbox (device, 4 ints: min bx, max bx, min by, max by; preset to an empty
-// box) receives the bounding box of the tagged blocks, one atomic per warp.
+// Warp-wide bounding box of the blocks with any != 0, merged into bbox by
+// lane 0 (all 32 lanes call it).
+__device__ __forceinline__ void bbox_merge(int* bbox, unsigned char any, int bx, int by) {
+  if (__ballot_sync(0xffffffffu, any)) {
+    const int x0 = __reduce_min_sync(0xffffffffu, any ? bx : 0x7fffffff);
+    const int x1 = __reduce_max_sync(0xffffffffu, any ? bx : -1);
+    const int y0 = __reduce_min_sync(0xffffffffu, any ? by : 0x7fffffff);
+    const int y1 = __reduce_max_sync(0xffffffffu, any ? by : -1);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&bbox[0], x0);
+      atomicMax(&bbox[1], x1);
+      atomicMin(&bbox[2], y0);
+      atomicMax(&bbox[3], y1);
+    }
+  }
+}
+
+// Block map, first pass (B <= 8): one 64-bit word per block of B x B cells,
+// bit r*B + c set when cell (c, r) of the block is tagged.  One thread per
+// block; a warp reads 32 neighbouring blocks' rows, so every load instruction
+// is one contiguous run of the tag map.
+__global__ void tag_mask_kernel(const int* __restrict__ tags, int nx, int ny, int B, unsigned long long* mask,
+                                int nbx, int nby) {
+  const long n = (long)nbx * nby;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int bx = (int)(t % nbx), by = (int)(t / nbx);
+    const int i0 = bx * B, j0 = by * B;
+    const int w = min(B, nx - i0), h = min(B, ny - j0);
+    unsigned long long m = 0;
+    for (int r = 0; r < h; ++r) {
+      const int* row = tags + (long)(j0 + r) * nx + i0;
+#pragma unroll 8
+      for (int c = 0; c < w; ++c)
+        if (row[c]) m |= 1ull << (r * B + c);
+    }
+    mask[t] = m;
+  }
+}
+
+// Block map, second pass: a block is tagged when its own cells or the cells
+// of its 8 neighbours within `buf` (<= B) cells of it hold a tag.  rowm[d] /
+// colm[d] select the rows / columns of the neighbour at offset d - 1 that lie
+// within the buffer.  Same map as tag_block_kernel.
+__global__ void tag_dilate_kernel(const unsigned long long* __restrict__ mask, int nbx, int nby,
+                                  unsigned long long rm0, unsigned long long rm2, unsigned long long cm0,
+                                  unsigned long long cm2, unsigned char* map, int* bbox) {
+  const long n = (long)nbx * nby;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long t0 = blockIdx.x * (long)blockDim.x; t0 < n; t0 += stride) {  // trip count uniform per warp
+    const long t = t0 + threadIdx.x;
+    unsigned char any = 0;
+    int bx = 0, by = 0;
+    if (t < n) {
+      bx = (int)(t % nbx);
+      by = (int)(t / nbx);
+      const unsigned long long all = ~0ull;
+      const unsigned long long rm[3] = {rm0, all, rm2}, cm[3] = {cm0, all, cm2};
+      unsigned long long hit = 0;
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int x = bx + dx, y = by + dy;
+          if (x >= 0 && x < nbx && y >= 0 && y < nby) hit |= mask[(long)y * nbx + x] & rm[dy + 1] & cm[dx + 1];
+        }
+      any = hit != 0;
+      map[t] = any;
+    }
+    bbox_merge(bbox, any, bx, by);
+  }
+}
+
+// Block map in one pass, any block size and buffer: each block scans its
+// buffered window.  bbox (device, 4 ints: min bx, max bx, min by, max by;
+// preset to an empty box) receives the bounding box of the tagged blocks.
 __global__ void tag_block_kernel(const int* tags, int nx, int ny, int B, int buf, unsigned char* map, int nbx,
                                  int nby, int* bbox) {
   const long n = (long)nbx * nby;
@@ -1082,18 +1155,7 @@ __global__ void tag_block_kernel(const int* tags, int nx, int ny, int B, int buf
           }
       map[t] = any;
     }
-    if (__ballot_sync(0xffffffffu, any)) {
-      const int x0 = __reduce_min_sync(0xffffffffu, any ? bx : 0x7fffffff);
-      const int x1 = __reduce_max_sync(0xffffffffu, any ? bx : -1);
-      const int y0 = __reduce_min_sync(0xffffffffu, any ? by : 0x7fffffff);
-      const int y1 = __reduce_max_sync(0xffffffffu, any ? by : -1);
-      if ((threadIdx.x & 31) == 0) {
-        atomicMin(&bbox[0], x0);
-        atomicMax(&bbox[1], x1);
-        atomicMin(&bbox[2], y0);
-        atomicMax(&bbox[3], y1);
-      }
-    }
+    bbox_merge(bbox, any, bx, by);
   }
 }
 
@@ -1448,6 +1510,8 @@ struct Engine {
   unsigned char* d_bmap = nullptr;
   int* d_bbox = nullptr;  // bounding box of the tagged blocks of the last block map
   size_t bmap_cap = 0;
+  unsigned long long* d_bmask = nullptr;  // per-block tag bits (block map first pass)
+  size_t bmask_cap = 0;
   double* d_segs = nullptr;
   size_t segs_cap = 0;
   MlpSmem* d_mlp = nullptr;  // learned-sensor network image (BF16 transposed weights)
@@ -1859,8 +1923,9 @@ static int fill_level(Engine* E, int l, int which) {
   return ENL_OK;
 }
 
-static int fill_all(Engine* E, int which) {
-  for (int l = 0; l < E->cfg.nlevels; ++l) {
+// Ghosts of levels 0..last (a level's fill reads only the coarser levels).
+static int fill_all(Engine* E, int which, int last = kL) {
+  for (int l = 0; l < E->cfg.nlevels && l <= last; ++l) {
     if (E->f32s) fill_level<float>(E, l, which);
     else fill_level<double>(E, l, which);
   }
@@ -2255,6 +2320,7 @@ int enl_engine_destroy(void* e) {
     if (E->d_tags[l]) cudaFree(E->d_tags[l]);
   if (E->d_bmap) cudaFree(E->d_bmap);
   if (E->d_bbox) cudaFree(E->d_bbox);
+  if (E->d_bmask) cudaFree(E->d_bmask);
   if (E->d_dt) cudaFree(E->d_dt);
   if (E->d_mlp) cudaFree(E->d_mlp);
   if (E->d_packed) cudaFree(E->d_packed);
@@ -2441,7 +2507,7 @@ int enl_engine_tag(void* e, int level, int* tags) {
   }
   cudaStream_t s = stream();
   Level& L = E->lev[level];
-  fill_all(E, 0);
+  fill_all(E, 0, level);
   // source ghosts: the same physical rule on the H0 canvas (one field)
   if (E->f32s)
     physbc_kernel<float><<<E->nsm, 256, 0, s>>>(L.view<float>(3), 1, E->cfg.bc[0], E->cfg.bc[1], E->cfg.bc[2],
@@ -2642,8 +2708,34 @@ static int tag_blocks_device(Engine* E, int level, int block, int buffer) {
   if (st != ENL_OK) return st;
   static const int empty[4] = {0x7fffffff, -1, 0x7fffffff, -1};
   cudaMemcpyAsync(E->d_bbox, empty, sizeof(empty), cudaMemcpyHostToDevice, s);
-  tag_block_kernel<<<E->nsm * 4, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, buffer, E->d_bmap, nbx, nby,
-                                              E->d_bbox);
+  if (block <= 8 && buffer <= block) {
+    // two passes: a bit mask per block, then the buffer from the 8 neighbours' masks
+    if (nb > E->bmask_cap) {
+      if (E->d_bmask) cudaFree(E->d_bmask);
+      if (cudaMalloc(&E->d_bmask, nb * sizeof(unsigned long long)) != cudaSuccess) {
+        E->d_bmask = nullptr;
+        E->bmask_cap = 0;
+        set_error(ENL_ERR_CUDA);
+        return ENL_ERR_CUDA;
+      }
+      E->bmask_cap = nb;
+    }
+    unsigned long long rows_hi = 0, rows_lo = 0, cols_hi = 0, cols_lo = 0;
+    for (int r = 0; r < block; ++r)
+      for (int c = 0; c < block; ++c) {
+        const unsigned long long bit = 1ull << (r * block + c);
+        if (r >= block - buffer) rows_hi |= bit;  // last rows: in the window of the block at j + 1
+        if (r < buffer) rows_lo |= bit;           // first rows: in the window of the block at j - 1
+        if (c >= block - buffer) cols_hi |= bit;
+        if (c < buffer) cols_lo |= bit;
+      }
+    const unsigned g = (unsigned)std::min<size_t>((nb + 255) / 256, (size_t)E->nsm * 8);
+    tag_mask_kernel<<<g, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, E->d_bmask, nbx, nby);
+    tag_dilate_kernel<<<g, 256, 0, s>>>(E->d_bmask, nbx, nby, rows_hi, rows_lo, cols_hi, cols_lo, E->d_bmap, E->d_bbox);
+  } else {
+    tag_block_kernel<<<E->nsm * 4, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, buffer, E->d_bmap, nbx, nby,
+                                                E->d_bbox);
+  }
   return check_launch("tag_blocks");
 }
 

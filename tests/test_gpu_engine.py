@@ -537,6 +537,39 @@ def test_native_regrid_equals_host_regrid(precision):
         assert np.array_equal(a, b)
 
 
+def _block_map(tags, B, buf):
+    """Block (bx, by) is set when a tag lies in its cells grown by buf cells
+    (clipped to the level): the block map the regrid clusters."""
+    ny, nx = tags.shape
+    nbx, nby = -(-nx // B), -(-ny // B)
+    out = np.zeros((nby, nbx), bool)
+    for by in range(nby):
+        for bx in range(nbx):
+            i0, i1 = max(0, bx * B - buf), min(nx, (bx + 1) * B + buf)
+            j0, j1 = max(0, by * B - buf), min(ny, (by + 1) * B + buf)
+            out[by, bx] = tags[j0:j1, i0:i1].any()
+    return out
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_block_map_matches_tag_map(precision):
+    """enl_engine_tag_blocks (two passes, bit masks of blocks up to 8x8 and a
+    buffer up to the block size; one windowed scan otherwise) gives the map
+    of the level's tag map, ragged edge blocks included."""
+    prm = default_params()
+    E, H, _ = workloads.line_source(prm, nx0=200, ny0=100, dx0=0.5, nlevels=2, nseg=20, precision=precision,
+                                    base_patch=64)
+    for _ in range(3):
+        E.step(1.0)
+    for level in range(2):
+        tags = E.tag(level).cpu().numpy() != 0
+        assert tags.any() and not tags.all()
+        for B, buf in [(4, 2), (4, 0), (4, 4), (2, 1), (8, 3), (8, 8), (3, 2), (1, 1), (16, 2), (4, 5)]:
+            got = E.tag_blocks(level, B, buf)
+            assert np.array_equal(got, _block_map(tags, B, buf)), (level, B, buf)
+    E.close()
+
+
 @pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
 def test_tables_after_regrids_match_a_fresh_engine(precision):
     """A regrid rebuilds only the tables of the levels it changed and copies

@@ -36,7 +36,7 @@ def _worker(rank, ws, port, out):
 def test_replicas_take_the_slowest_rank_and_count_all_work():
     import torch.multiprocessing as mp
     ws = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of this (threaded) process
     out = mgr.dict()
     mp.spawn(_worker, args=(ws, _free_port(), out), nprocs=ws, join=True)
     for r in range(ws):
