@@ -58,11 +58,18 @@ constexpr int kPlaneF = kTH * kBW32;             // 320
 constexpr int kPlaneG = kBH * kTW;               // 448
 constexpr int kPlOffV = kPlane32, kPlOffF = 2 * kPlane32, kPlOffG = kPlOffF + 5 * kPlaneF;
 constexpr int kPlanesBytes = align128((kPlOffG + 5 * kPlaneG) * 4);   // 19840
-// FP32 storage prefetches u^n (5 fields) and H0 of the tile interior with the
-// halo box: boxes of 40 x 8 (x starts at the aligned column of cell i0 - 3)
+// With ENL_STAGE_UN_TMA 1, FP32 storage prefetches u^n (5 fields) and H0 of
+// the tile interior with the halo box: boxes of 40 x 8 (x starts at the
+// aligned column of cell i0 - 3).  By default (0) each cell loads them from
+// the canvases (coalesced rows), which keeps the staging buffers small
+// enough for 4 resident blocks.
+#ifndef ENL_STAGE_UN_TMA
+#define ENL_STAGE_UN_TMA 0
+#endif
+constexpr bool kUnTma = ENL_STAGE_UN_TMA != 0;
 constexpr int kUnBytes = 5 * kTH * kBW32 * 4;    // 6400
 constexpr int kH0Bytes = kTH * kBW32 * 4;        // 1280
-constexpr int kBufS = kTile32Bytes + kUnBytes + kH0Bytes;  // 23424 per staging buffer
+constexpr int kBufS = kTile32Bytes + (kUnTma ? kUnBytes + kH0Bytes : 0);  // per staging buffer
 constexpr int kOffTile32 = 2 * kStageBufBytes;
 constexpr int kOffPlanes = kOffTile32 + kTile32Bytes;
 constexpr int kOffMlp = kOffPlanes + kPlanesBytes;
@@ -71,11 +78,15 @@ constexpr int kOffMlpS = kOffPlanesS + kPlanesBytes;
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
 constexpr int kFeatRows = 32;                    // learned switch: cells per network chunk
 // Resident stage blocks per SM with FP32 storage (bounds the registers per
-// thread: 3 blocks of 256 threads leave 80).
+// thread: 4 blocks of 256 threads leave 64, 3 leave 80).  Four blocks need
+// the smaller staging buffers of ENL_STAGE_UN_TMA 0 (4 x 56 KB of shared
+// memory); measured on the 3-level line source, 4 blocks without the u^n
+// boxes run the stage in 0.346 ms against 0.371 ms for 3 blocks with them.
 #ifndef ENL_STAGE_BLOCKS_F32
-#define ENL_STAGE_BLOCKS_F32 3
+#define ENL_STAGE_BLOCKS_F32 4
 #endif
 constexpr int kStageBlocksF32 = ENL_STAGE_BLOCKS_F32;
+
 
 // Absorbing envelope (enlightning.C:634-786) as per-level tables: for each
 // side, env[i] = 1 - exp(-ln2 d^2 / w^2) at the distance d of cell centre i
@@ -285,6 +296,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   __shared__ unsigned char s_flag[256];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
+  __shared__ int4 s_td[2];  // descriptors of the staged tiles
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
   __shared__ TileInfo s_tile;
@@ -292,6 +304,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   const int ntiles = *A.ntiles;
   auto issue = [&](int t, int b) {
     const int4 td = A.tiles[t];
+    s_td[b] = td;
     // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
     // doubles, a multiple of 4 for floats; set_patches only accepts such
     // patch origins and tiles are 32 wide
@@ -304,10 +317,15 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     if constexpr (kF32S) {
       // halo box, and the interior rows of u^n (unless u^n is the input) and H0;
       // canvas column of cell i0-3 is i0, canvas row of cell j0 is j0+3
-      mbar_arrive_expect_tx(&mbar[b], kTileBytes32 + (A.un_is_in ? 0 : kUnBytes) + kH0Bytes);
-      tma_load_3d(dst[b], &A.tmap[lv], td.x, td.y, 0, &mbar[b]);
-      if (!A.un_is_in) tma_load_3d(dst[b] + kTile32Bytes, &A.tmap_un[lv], td.x, td.y + 3, 0, &mbar[b]);
-      tma_load_3d(dst[b] + kTile32Bytes + kUnBytes, &A.tmap_h0[lv], td.x, td.y + 3, 0, &mbar[b]);
+      if (kUnTma) {
+        mbar_arrive_expect_tx(&mbar[b], kTileBytes32 + (A.un_is_in ? 0 : kUnBytes) + kH0Bytes);
+        tma_load_3d(dst[b], &A.tmap[lv], td.x, td.y, 0, &mbar[b]);
+        if (!A.un_is_in) tma_load_3d(dst[b] + kTile32Bytes, &A.tmap_un[lv], td.x, td.y + 3, 0, &mbar[b]);
+        tma_load_3d(dst[b] + kTile32Bytes + kUnBytes, &A.tmap_h0[lv], td.x, td.y + 3, 0, &mbar[b]);
+      } else {
+        mbar_arrive_expect_tx(&mbar[b], kTileBytes32);
+        tma_load_3d(dst[b], &A.tmap[lv], td.x, td.y, 0, &mbar[b]);
+      }
     } else {
       mbar_arrive_expect_tx(&mbar[b], kTileBytes64);
       // canvas column of cell i0-3 is i0 (ghost offset 3)
@@ -341,7 +359,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     }
     const double* tile = reinterpret_cast<const double*>(dst[b]);  // FP64 storage
     float* tile32 = kF32S ? reinterpret_cast<float*>(dst[b]) : tile32_conv;
-    const int4 td = A.tiles[t];
+    const int4 td = s_td[b];
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     const int i0 = td.x, j0 = td.y;
     if (!mbar_wait_bounded(&mbar[b], phase[b], kWaitIters)) {
@@ -374,7 +392,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     if (FAST) {
       // planes of u, v and the fluxes at every halo position of the tile
       const float rho0f = A.F[lvl].rho0, rT0f = A.F[lvl].rho0T0;
-      for (int e = tid; e < kBH * kBW; e += 256) {
+      // kBH * kBW = 532 positions: the 20 of the third pass fall on the last
+      // warp, not on warp 0, which also stages the next tile
+      for (int e = 255 - tid; e < kBH * kBW; e += 256) {
         const int row = e / kBW, col = e - row * kBW, o = row * kBW32 + col;
         const float ir = rcp_approx(rho0f + tile32[o]);
         const float u = tile32[kPlane32 + o] * ir, v = tile32[2 * kPlane32 + o] * ir;
@@ -414,20 +434,24 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     // compaction counts: DRP cells first, then WENO cells, each in tile order
     unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
     unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
-    if (lane == 0) {
-      s_cnt[0][warp] = __popc(bd);
-      s_cnt[1][warp] = __popc(bw);
-    }
-    __syncthreads();
     int nd = 0, nw = 0, od = 0, ow = 0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (q < warp) {
-        od += s_cnt[0][q];
-        ow += s_cnt[1][q];
+    if (!__syncthreads_or(bw != 0u)) {
+      nd = w * h;  // no WENO cell: the natural order, no counts needed
+    } else {
+      if (lane == 0) {
+        s_cnt[0][warp] = __popc(bd);
+        s_cnt[1][warp] = __popc(bw);
       }
-      nd += s_cnt[0][q];
-      nw += s_cnt[1][q];
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (q < warp) {
+          od += s_cnt[0][q];
+          ow += s_cnt[1][q];
+        }
+        nd += s_cnt[0][q];
+        nw += s_cnt[1][q];
+      }
     }
     int nfb = 0;
     if (learned && lvl == 0 && nw > 0) {
@@ -520,14 +544,15 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
         float* out = static_cast<float*>(A.out[lvl]);
         SAcc32R acc{acc32(tile32, planes, cx, cy)};
         float H[5], K[5], wn[5];
-        H[0] = h0b[ci];
+        H[0] = kUnTma ? h0b[ci] : static_cast<const float*>(A.h0[lvl])[g];
         sources_fast(acc, A.F[lvl], H);
         fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
         const float a1 = A.a1f, a2 = A.a2f, bdtf = s_tile.bdtf;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
           const float w = tile32[k * kPlane32 + c32];
-          const float u0 = A.un_is_in ? w : unb[k * (kTH * kBW32) + ci];
+          const float u0 = A.un_is_in ? w : (kUnTma ? unb[k * (kTH * kBW32) + ci]
+                                                   : static_cast<const float*>(A.un[lvl])[k * fs + g]);
           wn[k] = fmaf(bdtf, K[k], fmaf(a1, u0, a2 * w));
         }
         // update_state in perturbation form (update_state.m4:90-105)
