@@ -389,6 +389,24 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       }
       __syncthreads();
     }
+    // switch first: it reads the staged density only, so the barrier that
+    // completes the planes also tells whether the tile has a WENO cell
+    const int tx = lane, ty = warp;
+    const bool valid = tx < w && ty < h;
+    const int cc = (ty + 3) * kBW + (tx + 3);
+    const int cc32 = (ty + 3) * kBW32 + (tx + 3);
+    int flag = 0;
+    if (valid) {
+      if (FAST) {
+        SAcc32R acc{acc32(tile32, planes, tx, ty)};
+        flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
+      } else {
+        SAcc64R acc{SAcc64{tile, cc}};
+        flag = rhs_switch<SCHEME, ORDER, LLF>(acc, A.P[lvl]);
+      }
+    }
+    unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
+    unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
     if (FAST) {
       // planes of u, v and the fluxes at every halo position of the tile
       const float rho0f = A.F[lvl].rho0, rT0f = A.F[lvl].rho0T0;
@@ -415,25 +433,8 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
             planes[kPlOffG + k * kPlaneG + row * kTW + (col - 3)] = fmaf(v, wk[k], k == 2 ? pp : 0.0f);
         }
       }
-      __syncthreads();
-    }
-    const int tx = lane, ty = warp;
-    const bool valid = tx < w && ty < h;
-    const int cc = (ty + 3) * kBW + (tx + 3);
-    const int cc32 = (ty + 3) * kBW32 + (tx + 3);
-    int flag = 0;
-    if (valid) {
-      if (FAST) {
-        SAcc32R acc{acc32(tile32, planes, tx, ty)};
-        flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
-      } else {
-        SAcc64R acc{SAcc64{tile, cc}};
-        flag = rhs_switch<SCHEME, ORDER, LLF>(acc, A.P[lvl]);
-      }
     }
     // compaction counts: DRP cells first, then WENO cells, each in tile order
-    unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
-    unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
     int nd = 0, nw = 0, od = 0, ow = 0;
     if (!__syncthreads_or(bw != 0u)) {
       nd = w * h;  // no WENO cell: the natural order, no counts needed
