@@ -1551,8 +1551,27 @@ struct Engine {
   long long prof_launches = 0, prof_cells = 0;
   DevArray<long long> d_tileoff;
   std::vector<long long> h_tileoff;
-  void* d_packed = nullptr;
-  size_t packed_cap = 0;  // bytes
+  // host exchange (upload/download): two device staging slots per direction,
+  // copies on the engine's own streams, ordered with the library stream by
+  // events (see pack_common)
+  struct Xfer {
+    void* dev[2] = {nullptr, nullptr};
+    size_t cap[2] = {0, 0};                 // bytes
+    cudaEvent_t copied[2] = {};             // the slot's copy is done
+    cudaEvent_t used[2] = {};               // the slot's kernel (pack / unpack) is done
+    bool pending[2] = {false, false};       // download: the slot's copy may be in flight
+    int slot = 0;
+  } xin, xout;
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  // downloads whose copy to the host may still run: an upload from an
+  // overlapping host range waits for them
+  struct HostWrite {
+    const void* host;
+    size_t bytes;
+    cudaEvent_t done;
+  };
+  std::vector<HostWrite> host_writes;
+  std::vector<cudaEvent_t> spare_events;
   unsigned long long* d_smax = nullptr;
   // virtual microphones
   int nmics = 0;
@@ -2349,7 +2368,25 @@ int enl_engine_destroy(void* e) {
   if (E->d_bmask) cudaFree(E->d_bmask);
   if (E->d_dt) cudaFree(E->d_dt);
   if (E->d_mlp) cudaFree(E->d_mlp);
-  if (E->d_packed) cudaFree(E->d_packed);
+  for (Engine::Xfer* X : {&E->xin, &E->xout})
+    for (int q = 0; q < 2; ++q) {
+      if (X->copied[q]) {
+        cudaEventSynchronize(X->copied[q]);
+        cudaEventDestroy(X->copied[q]);
+      }
+      if (X->used[q]) {
+        cudaEventSynchronize(X->used[q]);
+        cudaEventDestroy(X->used[q]);
+      }
+      if (X->dev[q]) cudaFree(X->dev[q]);
+    }
+  for (auto& w : E->host_writes) {
+    cudaEventSynchronize(w.done);
+    cudaEventDestroy(w.done);
+  }
+  for (cudaEvent_t ev : E->spare_events) cudaEventDestroy(ev);
+  if (E->s_in) cudaStreamDestroy(E->s_in);
+  if (E->s_out) cudaStreamDestroy(E->s_out);
   for (int q = 0; q < 6; ++q)
     if (E->pev[q]) cudaEventDestroy(E->pev[q]);
   if (E->d_smax) cudaFree(E->d_smax);
@@ -3051,7 +3088,7 @@ int enl_engine_storage(void* e, int* elem_bytes, double* offsets) {
 }  // extern "C"
 
 template <typename S>
-static void pack_t(Engine* E, long long cells, int unpack, int nfields) {
+static void pack_t(Engine* E, long long cells, int unpack, int nfields, void* packed) {
   PackArgs<S> A;
   memset(&A, 0, sizeof(A));
   for (int l = 0; l < E->cfg.nlevels; ++l) {
@@ -3066,57 +3103,150 @@ static void pack_t(Engine* E, long long cells, int unpack, int nfields) {
   A.off = E->d_tileoff.p;
   A.ntiles = (int)E->h_tiles.size();
   A.total = cells;
-  A.packed = static_cast<S*>(E->d_packed);
+  A.packed = static_cast<S*>(packed);
   A.unpack = unpack;
   pack_kernel<S><<<std::min(A.ntiles, E->nsm * 8), 256, 0, stream()>>>(A);
 }
 
 extern "C" {
 
-static int pack_common(Engine* E, void* host, int unpack, int nfields) {
-  long long cells = packed_cells(E);
-  if (cells == 0) return ENL_OK;
-  const size_t bytes = (size_t)cells * nfields * E->esize;
-  if (bytes > E->packed_cap) {
-    if (E->d_packed) cudaFree(E->d_packed);
-    if (cudaMalloc(&E->d_packed, bytes) != cudaSuccess) {
-      E->d_packed = nullptr;
-      E->packed_cap = 0;
+// Host exchange.  An upload copies the host data into a device staging slot
+// on the engine's upload stream, and the library stream waits for that copy
+// before the unpack kernel; a download packs on the library stream into a
+// slot and copies it to the host on the download stream.  Slots alternate,
+// so the copies of one exchange overlap the kernels of the steps around it;
+// a slot is reused only after its previous kernel and copy are done, and an
+// upload whose host range overlaps a pending download waits for that
+// download.  The host memory stays in use until enl_engine_sync.
+static bool overlap(const void* a, size_t na, const void* b, size_t nb) {
+  const char *pa = static_cast<const char*>(a), *pb = static_cast<const char*>(b);
+  return na && nb && pa < pb + nb && pb < pa + na;
+}
+
+static int xfer_slot(Engine* E, Engine::Xfer& X, size_t bytes, int& q) {
+  if (!E->s_in && (cudaStreamCreateWithFlags(&E->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+                   cudaStreamCreateWithFlags(&E->s_out, cudaStreamNonBlocking) != cudaSuccess)) {
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  q = X.slot;
+  X.slot ^= 1;
+  if (!X.copied[q] && (cudaEventCreateWithFlags(&X.copied[q], cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&X.used[q], cudaEventDisableTiming) != cudaSuccess)) {
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  if (bytes > X.cap[q]) {
+    // the slot's previous kernel and copy must be done before it is freed
+    cudaEventSynchronize(X.used[q]);
+    cudaEventSynchronize(X.copied[q]);
+    if (X.dev[q]) cudaFree(X.dev[q]);
+    if (cudaMalloc(&X.dev[q], bytes) != cudaSuccess) {
+      X.dev[q] = nullptr;
+      X.cap[q] = 0;
       set_error(ENL_ERR_CUDA);
       return ENL_ERR_CUDA;
     }
-    E->packed_cap = bytes;
+    X.cap[q] = bytes;
+  }
+  return ENL_OK;
+}
+
+static int pack_common(Engine* E, void* host, long long host_bytes, int unpack, int nfields) {
+  long long cells = packed_cells(E);
+  if (cells == 0) return ENL_OK;
+  const size_t bytes = (size_t)cells * nfields * E->esize;
+  if (host_bytes < 0 || (size_t)host_bytes < bytes) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
   }
   cudaStream_t s = stream();
-  if (unpack) cudaMemcpyAsync(E->d_packed, host, bytes, cudaMemcpyHostToDevice, s);
-  if (E->f32s) pack_t<float>(E, cells, unpack, nfields);
-  else pack_t<double>(E, cells, unpack, nfields);
-  if (!unpack) cudaMemcpyAsync(host, E->d_packed, bytes, cudaMemcpyDeviceToHost, s);
+  Engine::Xfer& X = unpack ? E->xin : E->xout;
+  int q = 0;
+  int st = xfer_slot(E, X, bytes, q);
+  if (st != ENL_OK) return st;
+  if (unpack) {
+    // the slot's previous unpack has read it; downloads into this host range
+    // that may still run have written it (finished ones are dropped)
+    cudaStreamWaitEvent(E->s_in, X.used[q], 0);
+    if (cudaGetLastError() != cudaSuccess) {  // report earlier failures before the queries below
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+    auto& W = E->host_writes;
+    for (size_t r = 0; r < W.size();) {
+      if (cudaEventQuery(W[r].done) == cudaSuccess) {
+        E->spare_events.push_back(W[r].done);
+        W[r] = W.back();
+        W.pop_back();
+        continue;
+      }
+      if (overlap(host, bytes, W[r].host, W[r].bytes)) cudaStreamWaitEvent(E->s_in, W[r].done, 0);
+      ++r;
+    }
+    cudaGetLastError();  // a cudaErrorNotReady of the queries is not an error
+    cudaMemcpyAsync(X.dev[q], host, bytes, cudaMemcpyHostToDevice, E->s_in);
+    cudaEventRecord(X.copied[q], E->s_in);
+    cudaStreamWaitEvent(s, X.copied[q], 0);
+    if (E->f32s) pack_t<float>(E, cells, 1, nfields, X.dev[q]);
+    else pack_t<double>(E, cells, 1, nfields, X.dev[q]);
+    cudaEventRecord(X.used[q], s);
+  } else {
+    // the slot's previous copy to the host has read it
+    if (X.pending[q]) cudaStreamWaitEvent(s, X.copied[q], 0);
+    if (E->f32s) pack_t<float>(E, cells, 0, nfields, X.dev[q]);
+    else pack_t<double>(E, cells, 0, nfields, X.dev[q]);
+    cudaEventRecord(X.used[q], s);
+    // (earlier uploads have been read: their unpack precedes this pack)
+    cudaStreamWaitEvent(E->s_out, X.used[q], 0);
+    cudaMemcpyAsync(host, X.dev[q], bytes, cudaMemcpyDeviceToHost, E->s_out);
+    cudaEventRecord(X.copied[q], E->s_out);
+    X.pending[q] = true;
+    cudaEvent_t done = nullptr;
+    if (!E->spare_events.empty()) {
+      done = E->spare_events.back();
+      E->spare_events.pop_back();
+    } else if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+    cudaEventRecord(done, E->s_out);
+    E->host_writes.push_back({host, bytes, done});
+  }
   return check_launch(unpack ? "engine upload" : "engine download");
 }
 
-int enl_engine_download(void* e, void* host) {
+int enl_engine_sync(void* e) {
   Engine* E = (Engine*)e;
-  if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, host, 0, kNF);
+  if (!E) return ENL_ERR_ARG;
+  if (E->s_in) cudaStreamSynchronize(E->s_in);
+  if (E->s_out) cudaStreamSynchronize(E->s_out);
+  cudaStreamSynchronize(stream());
+  return check_launch("engine sync");
 }
 
-int enl_engine_upload(void* e, const void* host) {
+int enl_engine_download(void* e, void* host, long long host_bytes) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, const_cast<void*>(host), 1, kNF);
+  return pack_common(E, host, host_bytes, 0, kNF);
 }
 
-int enl_engine_download_state(void* e, void* host) {
+int enl_engine_upload(void* e, const void* host, long long host_bytes) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, host, 0, 5);
+  return pack_common(E, const_cast<void*>(host), host_bytes, 1, kNF);
 }
 
-int enl_engine_upload_state(void* e, const void* host) {
+int enl_engine_download_state(void* e, void* host, long long host_bytes) {
   Engine* E = (Engine*)e;
   if (!E || !host) return ENL_ERR_ARG;
-  return pack_common(E, const_cast<void*>(host), 1, 5);
+  return pack_common(E, host, host_bytes, 0, 5);
+}
+
+int enl_engine_upload_state(void* e, const void* host, long long host_bytes) {
+  Engine* E = (Engine*)e;
+  if (!E || !host) return ENL_ERR_ARG;
+  return pack_common(E, const_cast<void*>(host), host_bytes, 1, 5);
 }
 
 int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, long long* cells) {

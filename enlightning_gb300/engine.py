@@ -191,13 +191,20 @@ class Engine:
         t = torch.empty(self.packed_size(), dtype=self.dtype)
         return t.pin_memory() if pin else t
 
+    @staticmethod
+    def _host_arg(host: torch.Tensor):
+        assert host.device.type == "cpu" and host.is_contiguous()
+        return C.c_void_p(host.data_ptr()), host.numel() * host.element_size()
+
     def download(self, host: torch.Tensor):
+        """Packed 7-field state to host memory (asynchronous: sync() before reading)."""
         assert host.dtype == self.dtype
-        _lib.check(self.L.enl_engine_download(self.h, C.c_void_p(host.data_ptr())), "enl_engine_download")
+        _lib.check(self.L.enl_engine_download(self.h, *self._host_arg(host)), "enl_engine_download")
 
     def upload(self, host: torch.Tensor):
+        """Packed 7-field state from host memory (asynchronous: keep it unchanged until sync())."""
         assert host.dtype == self.dtype
-        _lib.check(self.L.enl_engine_upload(self.h, C.c_void_p(host.data_ptr())), "enl_engine_upload")
+        _lib.check(self.L.enl_engine_upload(self.h, *self._host_arg(host)), "enl_engine_upload")
 
     def state_host(self, pin=True):
         """Host tensor sized for download_state/upload_state (5 fields)."""
@@ -205,14 +212,20 @@ class Engine:
         return t.pin_memory() if pin else t
 
     def download_state(self, host: torch.Tensor):
-        """Conserved state (5 fields) of every patch interior to host memory."""
+        """Conserved state (5 fields) of every patch interior to host memory
+        (asynchronous: sync() before reading)."""
         assert host.dtype == self.dtype
-        _lib.check(self.L.enl_engine_download_state(self.h, C.c_void_p(host.data_ptr())), "enl_engine_download_state")
+        _lib.check(self.L.enl_engine_download_state(self.h, *self._host_arg(host)), "enl_engine_download_state")
 
     def upload_state(self, host: torch.Tensor):
-        """Conserved state from host memory; p and T follow on the device."""
+        """Conserved state from host memory; p and T follow on the device
+        (asynchronous: keep the host data unchanged until sync())."""
         assert host.dtype == self.dtype
-        _lib.check(self.L.enl_engine_upload_state(self.h, C.c_void_p(host.data_ptr())), "enl_engine_upload_state")
+        _lib.check(self.L.enl_engine_upload_state(self.h, *self._host_arg(host)), "enl_engine_upload_state")
+
+    def sync(self):
+        """Wait for the engine's host copies and the library stream."""
+        _lib.check(self.L.enl_engine_sync(self.h), "enl_engine_sync")
 
     def set_adaptive_dt(self, on=True, cfl=0.5):
         _lib.check(self.L.enl_engine_set_adaptive_dt(self.h, int(on), float(cfl)), "enl_engine_set_adaptive_dt")
@@ -229,7 +242,7 @@ class Engine:
         storage type), the CFL state and the iteration number."""
         host = self.packed_host(pin=False)
         self.download(host)
-        torch.cuda.synchronize()
+        self.sync()
         dt, t = self.time()
         boxes = np.full((self.nlevels, max(1, max(len(b) for b in self.patches)), 4), -1, np.int64)
         for l, bl in enumerate(self.patches):
@@ -254,7 +267,7 @@ class Engine:
         assert host.numel() == E.packed_size() and host.dtype == E.dtype
         E.upload(host)
         _lib.check(E.L.enl_engine_set_time(E.h, float(d["dt"]), float(d["time"])), "enl_engine_set_time")
-        torch.cuda.synchronize()
+        E.sync()
         return E, int(d["iteration"])
 
     def paint_source(self, level, src_type, mode=10, amp=1.0, spread=1.0, pos=(0.0, 0.0), sine_amp=0.0,

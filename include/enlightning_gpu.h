@@ -271,17 +271,29 @@ int enl_engine_set_time(void* engine, double dt_last, double sim_time);
 
 /* State exchange with host memory: the current buffer's patch interiors of
  * every level, packed (7 fields, tile order: level by level, patch by patch,
- * 32x8 tiles row-major).  Asynchronous on the stream; host memory should be
- * pinned.  Elements are of the storage type (enl_engine_storage: doubles,
- * or FP32 perturbations); enl_engine_packed_size gives their number. */
+ * 32x8 tiles row-major).  Elements are of the storage type
+ * (enl_engine_storage: doubles, or FP32 perturbations);
+ * enl_engine_packed_size gives their number.  host_bytes is the size of the
+ * host buffer (ENL_ERR_ARG, and nothing copied, when it is smaller than the
+ * packed state).  Asynchronous: the host copies run on the engine's own
+ * upload and download streams and are ordered with the kernels on the
+ * library stream by events (an upload is what the next step reads; a
+ * download holds the state after the work enqueued before it), so they
+ * overlap the steps around them.  Two device staging slots per direction
+ * alternate.  Host memory should be pinned; a host buffer stays in use until
+ * enl_engine_sync returns (do not change an upload's source or read a
+ * download's target before).  An upload from host memory that a pending
+ * download writes waits for that download. */
 int enl_engine_packed_size(void* engine, long long* nelems);
-int enl_engine_download(void* engine, void* host);
-int enl_engine_upload(void* engine, const void* host);
+int enl_engine_download(void* engine, void* host, long long host_bytes);
+int enl_engine_upload(void* engine, const void* host, long long host_bytes);
 /* The same with the conserved state only (rho, rho u, rho v, rho s,
  * rho T_n: 5 of the 7 fields, nelems * 5/7 elements); the upload recomputes
  * p and T on the device with update_state (update_state.m4:90-105). */
-int enl_engine_download_state(void* engine, void* host);
-int enl_engine_upload_state(void* engine, const void* host);
+int enl_engine_download_state(void* engine, void* host, long long host_bytes);
+int enl_engine_upload_state(void* engine, const void* host, long long host_bytes);
+/* Wait for the engine's host copies and the library stream. */
+int enl_engine_sync(void* engine);
 
 /* Stage-kernel timing: with on = 1 every direct (not graph) enl_engine_step
  * brackets its three stage-kernel launches with CUDA events on the stream.

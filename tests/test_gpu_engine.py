@@ -432,6 +432,85 @@ def test_mic_files_in_reference_format(tmp_path):
         "1\n44100\n(0.7,0.1)\n1 1 1.013250e+05 1.013305e+05\n")
 
 
+def _exchange_engine(prm, precision):
+    E, _ = make_pair(prm, 96, 64, (0.1, 0.1), 2, [[(0, 47, 0, 63), (48, 95, 0, 63)], [(64, 127, 32, 95)]],
+                     (REFLECT,) * 4, "hybrid_high_llf", precision=precision)
+    E.set_adaptive_dt(True, 0.5)
+    return E
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_pipelined_exchange_matches_sequential(ora, precision):
+    """Uploads and downloads run on the engine's copy streams and overlap the
+    steps around them.  Alternating two host inputs and two host outputs with
+    no synchronisation in between gives, per output, exactly the state that a
+    fully synchronised upload -> step -> download of its input gives."""
+    prm = default_params()
+    E = _exchange_engine(prm, precision)
+    ins = [E.state_host(), E.state_host()]
+    E.download_state(ins[0])
+    E.step(1.0)
+    E.download_state(ins[1])
+    E.sync()
+    expect = []
+    for h in ins:
+        o = E.state_host()
+        E.upload_state(h)
+        E.sync()
+        E.step(1.0)
+        E.download_state(o)
+        E.sync()
+        expect.append(o.clone())
+    assert not torch.equal(expect[0], expect[1])
+    outs = [E.state_host(), E.state_host()]
+    for k in range(6):
+        E.upload_state(ins[k % 2])
+        E.step(1.0)
+        E.download_state(outs[k % 2])
+    E.sync()
+    assert E.health() == 0
+    for o, x in zip(outs, expect):
+        assert torch.equal(o, x)
+    E.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_round_trip_through_one_host_buffer(ora, precision):
+    """download -> upload of the same host buffer every step (no
+    synchronisation): the upload waits for the download it overlaps, so the
+    run equals one that never leaves the device.  (The full 7-field state:
+    on coarse cells under a fine patch, p and T are averages of the fine
+    ones, which the 5-field exchange would recompute from the averaged state.)"""
+    prm = default_params()
+    E, F = _exchange_engine(prm, precision), _exchange_engine(prm, precision)
+    h = E.packed_host()
+    for _ in range(4):
+        E.step(1.0)
+        E.download(h)
+        E.upload(h)
+        F.step(1.0)
+    E.sync()
+    F.sync()
+    for l in range(2):
+        a, b = E.level_state(l).cpu().numpy(), F.level_state(l).cpu().numpy()
+        for bx in E.patches[l]:
+            sl = (slice(None), slice(bx[2], bx[3] + 1), slice(bx[0], bx[1] + 1))
+            assert np.array_equal(a[sl], b[sl])
+    E.close()
+    F.close()
+
+
+def test_exchange_refuses_a_small_host_buffer():
+    prm = default_params()
+    E = _exchange_engine(prm, PREC_FP32_STATE)
+    small = torch.empty(E.state_host().numel() - 1, dtype=E.dtype).pin_memory()
+    for fn in (E.download_state, E.upload_state):
+        with pytest.raises(EnlightningError):
+            fn(small)
+        assert _lib.lib().enl_get_last_error() == 1  # ENL_ERR_ARG, consumed here
+    E.close()
+
+
 @pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
 def test_state_exchange_recomputes_p_and_t(ora, precision):
     """download_state/upload_state move the 5 conserved fields; p and T come
