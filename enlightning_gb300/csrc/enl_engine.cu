@@ -1204,25 +1204,45 @@ struct SpeedArgs {
 // max(|rho u|, |rho v|) / |rho| is max(|u|, |v|) bit for bit (a correctly
 // rounded division is monotonic), with one division instead of two.  With
 // perturbation storage the speed is formed in single precision.
+// Each block takes kSpeedTiles tiles per pass with all their loads in flight
+// together (the pass is a chain of dependent loads: descriptor, then fields).
+constexpr int kSpeedTiles = 4;
 template <typename S>
 __global__ void speed_kernel(SpeedArgs<S> A) {
   __shared__ double s_w[8];
   const int n = *A.ntiles;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   double m = 0.0;
-  for (int t = blockIdx.x; t < n; t += gridDim.x) {
-    int4 td = A.tiles[t];
-    int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
-    int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    if (tx < w && ty < h) {
-      const CanvasT<S>& V = A.lev[lvl];
-      int i = td.x + tx, j = td.y + ty;
+  for (int t0 = blockIdx.x; t0 < n; t0 += kSpeedTiles * gridDim.x) {
+    int4 td[kSpeedTiles];
+#pragma unroll
+    for (int u = 0; u < kSpeedTiles; ++u) {
+      const int t = t0 + u * gridDim.x;
+      td[u] = t < n ? A.tiles[t] : make_int4(0, 0, 0, 0);  // w = h = 0: no cell
+    }
+    S r[kSpeedTiles], mu[kSpeedTiles], mv[kSpeedTiles];
+    bool ok[kSpeedTiles];
+#pragma unroll
+    for (int u = 0; u < kSpeedTiles; ++u) {
+      const int lvl = td[u].z & 0xff, w = (td[u].z >> 8) & 0xff, h = (td[u].z >> 16) & 0xff;
+      ok[u] = tx < w && ty < h;
+      if (ok[u]) {
+        const CanvasT<S>& V = A.lev[lvl];
+        const int i = td[u].x + tx, j = td[u].y + ty;
+        r[u] = V.at(0, i, j);
+        mu[u] = V.at(1, i, j);
+        mv[u] = V.at(2, i, j);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kSpeedTiles; ++u) {
+      if (!ok[u]) continue;
       double s;
       if constexpr (std::is_same<S, float>::value) {
-        const float r = (float)A.rho_off + V.at(0, i, j);
-        s = (double)(fmaxf(fabsf(V.at(1, i, j)), fabsf(V.at(2, i, j))) / fabsf(r) + (float)A.c);
+        const float rr = (float)A.rho_off + r[u];
+        s = (double)(fmaxf(fabsf(mu[u]), fabsf(mv[u])) / fabsf(rr) + (float)A.c);
       } else {
-        const double r = V.at(0, i, j);
-        s = fmax(fabs(V.at(1, i, j)), fabs(V.at(2, i, j))) / fabs(r) + A.c;
+        s = fmax(fabs(mu[u]), fabs(mv[u])) / fabs(r[u]) + A.c;
       }
       if (!(s == s)) s = 1e300;  // NaN state: force a tiny dt, health check reports it
       m = fmax(m, s);
