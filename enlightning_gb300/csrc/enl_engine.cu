@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
   __shared__ int4 s_td[2];  // descriptors of the staged tiles
+  __shared__ unsigned s_stats[3 * kL];
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
   __shared__ TileInfo s_tile;
@@ -349,6 +350,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   }
   const bool learned = FAST && SCHEME == kHybrid && A.mlp != nullptr;
   if (tid == 0) {
+    for (int q = 0; q < 3 * kL; ++q) s_stats[q] = 0u;
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     fence_mbar_init();
@@ -547,10 +549,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       int pos = flag ? (nd + ow + __popc(bw & lt)) : (od + __popc(bd & lt));
       s_list[pos] = (ty << 5) | tx | (flag << 16);
     }
-    if (tid == 0 && A.stats) {
-      atomicAdd(&A.stats[3 * lvl + 0], (unsigned long long)nw);
-      atomicAdd(&A.stats[3 * lvl + 1], (unsigned long long)(nd + nw));
-      if (nfb) atomicAdd(&A.stats[3 * lvl + 2], (unsigned long long)nfb);
+    if (tid == 0) {  // per-block counts, added to A.stats when the block leaves
+      s_stats[3 * lvl + 0] += (unsigned)nw;
+      s_stats[3 * lvl + 1] += (unsigned)(nd + nw);
+      s_stats[3 * lvl + 2] += (unsigned)nfb;
     }
     if (!direct) __syncthreads();
     if (direct ? valid : (tid < nd + nw)) {
@@ -678,6 +680,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     t = s_t[b ^ 1];
     b ^= 1;
   }
+  if (tid == 0 && A.stats)
+    for (int q = 0; q < 3 * kL; ++q)
+      if (s_stats[q]) atomicAdd(&A.stats[q], (unsigned long long)s_stats[q]);
 }
 
 // ---------------------------------------------------------------------------
