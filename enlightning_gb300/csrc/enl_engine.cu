@@ -703,8 +703,10 @@ using CanvasView = CanvasT<double>;
 // touches each side): edge ghosts copy the first interior cell of their row or
 // column, corners copy the interior corner cell; the normal momentum is
 // negated on REFLECT sides (both momenta in a corner of two REFLECT sides).
+// sides: bit d set (0..3 = L, R, B, T) fills that side's band; a corner is
+// filled when both of its sides are.
 template <typename S>
-__global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int bcB, int bcT) {
+__global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int bcB, int bcT, int sides = 15) {
   const int nx = V.nx, ny = V.ny;
   const long nedge_x = 3L * ny, nedge_y = 3L * nx;
   const long nband = 2 * nedge_x + 2 * nedge_y + 36;
@@ -721,6 +723,7 @@ __global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int b
       j = (int)(q / 3);
       int d = (int)(q % 3);
       sj = j;
+      if (!(sides & (1 << side))) continue;
       if (side == 0) { i = -1 - d; si = 0; negu = bcL == kReflect; }
       else { i = nx + d; si = nx - 1; negu = bcR == kReflect; }
     } else if (r < 2 * nedge_x + 2 * nedge_y) {
@@ -730,6 +733,7 @@ __global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int b
       i = (int)(q / 3);
       int d = (int)(q % 3);
       si = i;
+      if (!(sides & (4 << side))) continue;
       if (side == 0) { j = -1 - d; sj = 0; negv = bcB == kReflect; }
       else { j = ny + d; sj = ny - 1; negv = bcT == kReflect; }
     } else {
@@ -737,6 +741,7 @@ __global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int b
       int corner = (int)(r / 9), q = (int)(r % 9);
       int dx = q % 3, dy = q / 3;
       int xs = corner & 1, ys = corner >> 1;
+      if (!(sides & (1 << xs)) || !(sides & (4 << ys))) continue;
       i = xs ? nx + dx : -1 - dx;
       j = ys ? ny + dy : -1 - dy;
       si = xs ? nx - 1 : 0;
@@ -1575,6 +1580,10 @@ struct Engine {
   int h_meta[M_SIZE];
   int tables_from = 0;            // first level whose tables are out of date
   bool tables_on_device = false;  // the device tables hold the kept levels
+  // the sides (bit d: 0..3 = L, R, B, T) of the level's physical ghost band
+  // that a step reads (by its own patches' stencils or by the next level's
+  // halo interpolation)
+  int bc_read[kL] = {15, 15, 15, 15};
   DevArray<int4> d_tiles, d_halo, d_ctiles, d_patchtab;
   int* d_meta = nullptr;
   int* d_counters = nullptr;   // 3 stage counters
@@ -1818,6 +1827,25 @@ static int rebuild_tables(Engine* E) {
     acc += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
   }
   E->tables_from = nl;
+  // Which levels' physical ghost bands a step reads: those with a patch
+  // within 3 cells (the stencil reach) of a side, and those under a finer
+  // level with a patch within 3 + ratio fine cells of a side (its halo cells
+  // interpolate from coarse cells one beyond the halo).  The others keep
+  // their band fill out of the step.
+  {
+    auto near = [&](int l, int m) {  // sides within m cells of a patch of level l
+      const Level& L = E->lev[l];
+      int sides = 0;
+      for (const int4& b : L.patches)
+        sides |= (b.x < m ? 1 : 0) | (b.y > L.nx - 1 - m ? 2 : 0) | (b.z < m ? 4 : 0) | (b.w > L.ny - 1 - m ? 8 : 0);
+      return sides;
+    };
+    for (int l = 0; l < nl; ++l) {
+      const int r = near(l, 3) | (l + 1 < nl ? near(l + 1, 3 + E->cfg.ratio) : 0);
+      if (r != E->bc_read[l]) E->graph_valid = false;  // the step's launches change
+      E->bc_read[l] = r;
+    }
+  }
   bool grew = false;
   const bool off_grew = E->d_tileoff.ensure(std::max<size_t>(E->h_tileoff.size(), 1));
   grew |= E->d_tiles.ensure(std::max<size_t>(E->h_tiles.size(), 1));
@@ -1999,7 +2027,7 @@ static StageFn pick_stage(int precision, int variant) {
 }
 
 template <typename S>
-static int fill_level(Engine* E, int l, int which) {
+static int fill_level(Engine* E, int l, int which, bool skip_unread) {
   cudaStream_t s = stream();
   const auto& c = E->cfg;
   Level& L = E->lev[l];
@@ -2012,17 +2040,20 @@ static int fill_level(Engine* E, int l, int which) {
     if (E->patch_cnt[l])
       physbc_patches_kernel<S><<<E->patch_cnt[l], 256, 0, s>>>(L.view<S>(which), E->d_patchtab.p, E->patch_off[l],
                                                                E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
-  } else {
-    physbc_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+  } else if (!skip_unread || E->bc_read[l]) {
+    physbc_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3],
+                                                skip_unread ? E->bc_read[l] : 15);
   }
   return ENL_OK;
 }
 
 // Ghosts of levels 0..last (a level's fill reads only the coarser levels).
-static int fill_all(Engine* E, int which, int last = kL) {
+// skip_unread (the fused step): band fills only of the sides the step reads;
+// every other fill (tagging, regrid, the API) fills whole bands.
+static int fill_all(Engine* E, int which, int last = kL, bool skip_unread = false) {
   for (int l = 0; l < E->cfg.nlevels && l <= last; ++l) {
-    if (E->f32s) fill_level<float>(E, l, which);
-    else fill_level<double>(E, l, which);
+    if (E->f32s) fill_level<float>(E, l, which, skip_unread);
+    else fill_level<double>(E, l, which, skip_unread);
   }
   return check_launch("fill");
 }
@@ -2176,7 +2207,7 @@ static int step_fused(Engine* E, double dt) {
   for (int st = 0; st < 3; ++st) {
     int in = st == 0 ? 0 : st;
     int out = st == 2 ? 0 : st + 1;
-    fill_all(E, in);
+    fill_all(E, in, kL, true);
     StageArgs A = stage_args(E, st, dt);
     void* args[] = {&A};
     if (E->profile) cudaEventRecord(E->pev[2 * st], s);
@@ -2673,8 +2704,13 @@ int enl_engine_launches_per_step(void* e, int plain) {
   int nl = c.nlevels;
   int fills = nl + (nl - 1);  // physbc per level + interp per fine level
   const int dt = (E->adaptive ? 2 : 0) + (E->nmics > 0 ? 2 : 0);  // speed + dt update; microphones
-  // fused: the stage kernel applies the absorbing envelope itself
-  if (!plain) return 3 * (fills + 1) + (nl - 1) + dt;
+  // fused: the stage kernel applies the absorbing envelope itself, and the
+  // band fill of a level whose band the step does not read is left out
+  if (!plain) {
+    int bands = 0;
+    for (int l = 0; l < nl; ++l) bands += (c.independent || E->bc_read[l] != 0) ? 1 : 0;
+    return 3 * (bands + (nl - 1) + 1) + (nl - 1) + dt;
+  }
   const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;
   for (int l = 0; l < nl; ++l) {

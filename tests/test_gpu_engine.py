@@ -92,11 +92,18 @@ def test_single_level_fp64_matches_oracle(ora, variant, plain):
     compare(E, O, 0, 1e-12)
 
 
+# fine patches away from the sides (the fused step leaves the fine level's
+# physical band unfilled: nothing reads it) and touching them (it is filled)
+FINE_SETS = {"inside": [(24, 55, 20, 51), (56, 71, 28, 43)],
+             "at_sides": [(0, 23, 0, 31), (56, 95, 48, 79)]}
+
+
+@pytest.mark.parametrize("fine_set", sorted(FINE_SETS))
 @pytest.mark.parametrize("plain", [False, True])
-def test_two_level_fp64_matches_oracle(ora, plain):
+def test_two_level_fp64_matches_oracle(ora, plain, fine_set):
     prm = default_params(bc_absorb_width=0.5)
     nx, ny = 48, 40
-    fine = [(24, 55, 20, 51), (56, 71, 28, 43)]
+    fine = FINE_SETS[fine_set]
     E, O = make_pair(prm, nx, ny, (0.1, 0.1), 2, [[(0, 23, 0, 39), (24, 47, 0, 39)], fine],
                      (ABSORB, REFLECT, REFLECT, ABSORB), "hybrid_high_llf")
     dt = workloads.pulse_dt(prm, (0.05, 0.05))
