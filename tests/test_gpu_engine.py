@@ -696,6 +696,33 @@ def test_tables_after_regrids_match_a_fresh_engine(precision):
     E.close()
 
 
+def test_line_source_1000_steps_fp32_state_within_budget():
+    """Long horizon: the reduced line source (1024x512 base, 3 levels, regrid
+    every 10 steps) advanced 1000 RK3 steps in FP32 perturbation storage
+    stays within 1e-3 relative L2 of the FP64 engine on the composite level
+    0, on every field and on the perturbations rho - rho0 and p - p0, although
+    the two runs' finest patches come to differ (their tags differ in the
+    last bits)."""
+    prm = default_params()
+    kw = dict(nx0=1024, ny0=512, nseg=50)
+    out = {}
+    for prec in (PREC_FP32_STATE, PREC_FP64):
+        E, H, _ = workloads.line_source(prm, precision=prec, **kw)
+        for s in range(1000):
+            if s and s % 10 == 0:
+                H.regrid()
+            E.step(1.0)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        out[prec] = E.level_state(0).cpu().numpy().copy()
+        E.close()
+    a, b = out[PREC_FP32_STATE], out[PREC_FP64]
+    for k in range(7):
+        assert relL2(a[k], b[k]) <= 1e-3, k
+    assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) <= 1e-3
+    assert relL2(a[5] - prm["p0"], b[5] - prm["p0"]) <= 1e-3
+
+
 def test_four_levels_fp32_state_within_budget(ora):
     """The deepest hierarchy the engine takes (ENL_MAX_LEVELS = 4) in FP32
     storage against FP64, with a regrid between steps."""
