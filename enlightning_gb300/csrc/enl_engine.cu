@@ -2909,6 +2909,23 @@ int enl_engine_tag_blocks(void* e, int level, int block, int buffer, unsigned ch
 
 }  // extern "C"
 
+// The bounded mbarrier wait of the stage kernel on a barrier that completes
+// (arrive = 1: one arrival) or that nothing completes (arrive = 0): out gets
+// ENL_OK or, after `polls` polls, ENL_ERR_TIMEOUT.  No copy is in flight, so
+// giving up leaves nothing behind.
+__global__ void bounded_wait_check_kernel(int polls, int arrive, int* out) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (arrive) mbar_arrive(&bar);
+    *out = mbar_wait_bounded(&bar, 0u, polls) ? ENL_OK : ENL_ERR_TIMEOUT;
+  }
+}
+
 // Rectangles covering box a minus box r (inclusive boxes as int4 ilo, ihi,
 // jlo, jhi): bottom and top slabs, then the left and right pieces between.
 static void box_subtract(const int4& a, const int4& r, std::vector<int4>& out) {
@@ -3025,6 +3042,26 @@ int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_bl
   const double ph[5] = {ms(t0, t1), ms(t1, t2), ms(t2, t3), ms(t3, t4), ms(t4, t5)};
   for (int q = 0; q < 5; ++q) E->regrid_ms[q] += ph[q];
   return st;
+}
+
+int enl_check_bounded_wait(int polls, int arrive) {
+  if (polls < 1) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) {
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  cudaStream_t s = stream();
+  bounded_wait_check_kernel<<<1, 32, 0, s>>>(polls, arrive, d);
+  int h = ENL_ERR_CUDA;
+  cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  cudaFree(d);
+  const int st = check_launch("bounded wait check");
+  return st != ENL_OK ? st : h;
 }
 
 int enl_engine_regrid_timing(void* e, double* ms5) {

@@ -367,6 +367,13 @@ int enl_engine_regrid(void* engine, int level, int block, int tag_buffer,
  * phase: waiting for the steps already queued, device tagging with the block
  * map read back, clustering, tables, refine launches; then reset. */
 int enl_engine_regrid_timing(void* engine, double* ms5);
+
+/* The stage kernel's bounded mbarrier wait, on its own: one block waits on a
+ * barrier that one arrival completes (arrive = 1) or that nothing completes
+ * (arrive = 0).  Returns ENL_OK, or ENL_ERR_TIMEOUT once `polls` polls have
+ * passed — the way a copy that never lands is reported instead of hanging
+ * the GPU (the context stays usable). */
+int enl_check_bounded_wait(int polls, int arrive);
 /* Patch boxes of a level (host array of 4*max_boxes ints); npatch = count. */
 int enl_engine_get_patches(void* engine, int level, int* boxes, int max_boxes,
                            int* npatch);
