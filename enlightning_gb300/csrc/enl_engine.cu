@@ -920,8 +920,12 @@ __device__ __forceinline__ bool ratio_below_f(float fm, float f0, float fp, floa
 // The ratio test depends on differences only, so it reads perturbation
 // storage as it is.
 template <typename S>
+// tags (when not null) gets 1 / 0 per patch cell; mask (when not null) gets
+// the tagged cells as bits of per-block words (block B x B cells, bit
+// r*B + c for cell (c, r) of the block, B <= 8; the words zeroed before).
 __global__ void tag_tiles_kernel(int* tags, CanvasT<S> W, CanvasT<S> H, const int4* tiles, int off, int cnt,
-                                 double ep0, double ep1) {
+                                 double ep0, double ep1, unsigned long long* mask = nullptr, int B = 1,
+                                 int nbx = 0) {
   for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
     int4 td = tiles[off + t];
     int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
@@ -941,7 +945,11 @@ __global__ void tag_tiles_kernel(int* tags, CanvasT<S> W, CanvasT<S> H, const in
            ratio_below_e(W.at(0, i - 1, j), W.at(0, i, j), W.at(0, i + 1, j), ep1) ||
            ratio_below_e(W.at(0, i, j - 1), W.at(0, i, j), W.at(0, i, j + 1), ep1);
     }
-    tags[(long)j * W.nx + i] = tg ? 1 : 0;
+    if (tags) tags[(long)j * W.nx + i] = tg ? 1 : 0;
+    if (mask && tg) {
+      const int bx = i / B, by = j / B;
+      atomicOr(&mask[(long)by * nbx + bx], 1ull << ((j - by * B) * B + (i - bx * B)));
+    }
   }
 }
 
@@ -1137,29 +1145,8 @@ __device__ __forceinline__ void bbox_merge(int* bbox, unsigned char any, int bx,
   }
 }
 
-// Block map, first pass (B <= 8): one 64-bit word per block of B x B cells,
-// bit r*B + c set when cell (c, r) of the block is tagged.  One thread per
-// block; a warp reads 32 neighbouring blocks' rows, so every load instruction
-// is one contiguous run of the tag map.
-__global__ void tag_mask_kernel(const int* __restrict__ tags, int nx, int ny, int B, unsigned long long* mask,
-                                int nbx, int nby) {
-  const long n = (long)nbx * nby;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int bx = (int)(t % nbx), by = (int)(t / nbx);
-    const int i0 = bx * B, j0 = by * B;
-    const int w = min(B, nx - i0), h = min(B, ny - j0);
-    unsigned long long m = 0;
-    for (int r = 0; r < h; ++r) {
-      const int* row = tags + (long)(j0 + r) * nx + i0;
-#pragma unroll 8
-      for (int c = 0; c < w; ++c)
-        if (row[c]) m |= 1ull << (r * B + c);
-    }
-    mask[t] = m;
-  }
-}
-
-// Block map, second pass: a block is tagged when its own cells or the cells
+// Block map from the per-block tag words (B <= 8; tag_tiles_kernel sets
+// them): a block is tagged when its own cells or the cells
 // of its 8 neighbours within `buf` (<= B) cells of it hold a tag.  rowm[d] /
 // colm[d] select the rows / columns of the neighbour at offset d - 1 that lie
 // within the buffer.  Same map as tag_block_kernel.
@@ -2643,12 +2630,9 @@ int enl_engine_graph_replay(void* e, int nsteps) {
   return ENL_OK;
 }
 
-int enl_engine_tag(void* e, int level, int* tags) {
-  Engine* E = (Engine*)e;
-  if (!E || level < 0 || level >= E->cfg.nlevels || !tags) {
-    set_error(ENL_ERR_ARG);
-    return ENL_ERR_ARG;
-  }
+// tag_cells on the patch cells of `level` (ghosts of levels 0..level filled
+// first): into the int map tags and/or the block mask (see tag_tiles_kernel).
+static int tag_level(Engine* E, int level, int* tags, unsigned long long* mask, int B, int nbx) {
   cudaStream_t s = stream();
   Level& L = E->lev[level];
   fill_all(E, 0, level);
@@ -2659,7 +2643,7 @@ int enl_engine_tag(void* e, int level, int* tags) {
   else
     physbc_kernel<double><<<E->nsm, 256, 0, s>>>(L.view<double>(3), 1, E->cfg.bc[0], E->cfg.bc[1], E->cfg.bc[2],
                                                  E->cfg.bc[3]);
-  cudaMemsetAsync(tags, 0, (size_t)L.nx * L.ny * sizeof(int), s);
+  if (tags) cudaMemsetAsync(tags, 0, (size_t)L.nx * L.ny * sizeof(int), s);
   const double xi = 1.0;
   const double* tol = E->cfg.tol;
   double ep0 = ((Lit::c0_9 * tol[0]) * (xi * xi)) / (1.0 - Lit::c0_9 * (tol[0] * tol[0]));
@@ -2668,12 +2652,21 @@ int enl_engine_tag(void* e, int level, int* tags) {
     if (E->f32s)
       tag_tiles_kernel<float><<<E->tile_cnt[level], 256, 0, s>>>(tags, L.view<float>(0), L.view<float>(3),
                                                                  E->d_tiles.p, E->tile_off[level],
-                                                                 E->tile_cnt[level], ep0, ep1);
+                                                                 E->tile_cnt[level], ep0, ep1, mask, B, nbx);
     else
       tag_tiles_kernel<double><<<E->tile_cnt[level], 256, 0, s>>>(tags, L.view<double>(0), L.view<double>(3),
                                                                   E->d_tiles.p, E->tile_off[level],
-                                                                  E->tile_cnt[level], ep0, ep1);
+                                                                  E->tile_cnt[level], ep0, ep1, mask, B, nbx);
   return check_launch("engine tag");
+}
+
+int enl_engine_tag(void* e, int level, int* tags) {
+  Engine* E = (Engine*)e;
+  if (!E || level < 0 || level >= E->cfg.nlevels || !tags) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  return tag_level(E, level, tags, nullptr, 1, 0);
 }
 
 int enl_engine_stats(void* e, long long* counts) {
@@ -2830,7 +2823,8 @@ static int tag_blocks_device(Engine* E, int level, int block, int buffer) {
   Level& L = E->lev[level];
   const int nbx = (L.nx + block - 1) / block, nby = (L.ny + block - 1) / block;
   cudaStream_t s = stream();
-  if (!E->d_tags[level]) {
+  const bool two_pass = block <= 8 && buffer <= block;
+  if (!two_pass && !E->d_tags[level]) {
     if (cudaMalloc(&E->d_tags[level], (size_t)L.nx * L.ny * sizeof(int)) != cudaSuccess) {
       E->d_tags[level] = nullptr;
       set_error(ENL_ERR_CUDA);
@@ -2853,12 +2847,11 @@ static int tag_blocks_device(Engine* E, int level, int block, int buffer) {
     set_error(ENL_ERR_CUDA);
     return ENL_ERR_CUDA;
   }
-  int st = enl_engine_tag(E, level, E->d_tags[level]);
-  if (st != ENL_OK) return st;
   static const int empty[4] = {0x7fffffff, -1, 0x7fffffff, -1};
   cudaMemcpyAsync(E->d_bbox, empty, sizeof(empty), cudaMemcpyHostToDevice, s);
-  if (block <= 8 && buffer <= block) {
-    // two passes: a bit mask per block, then the buffer from the 8 neighbours' masks
+  if (two_pass) {
+    // the tag kernel sets the tagged cells' bits in per-block words, then
+    // each block takes in the buffer from its 8 neighbours' words
     if (nb > E->bmask_cap) {
       if (E->d_bmask) cudaFree(E->d_bmask);
       if (cudaMalloc(&E->d_bmask, nb * sizeof(unsigned long long)) != cudaSuccess) {
@@ -2878,10 +2871,14 @@ static int tag_blocks_device(Engine* E, int level, int block, int buffer) {
         if (c >= block - buffer) cols_hi |= bit;
         if (c < buffer) cols_lo |= bit;
       }
+    cudaMemsetAsync(E->d_bmask, 0, nb * sizeof(unsigned long long), s);
+    const int st = tag_level(E, level, nullptr, E->d_bmask, block, nbx);
+    if (st != ENL_OK) return st;
     const unsigned g = (unsigned)std::min<size_t>((nb + 255) / 256, (size_t)E->nsm * 8);
-    tag_mask_kernel<<<g, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, E->d_bmask, nbx, nby);
     tag_dilate_kernel<<<g, 256, 0, s>>>(E->d_bmask, nbx, nby, rows_hi, rows_lo, cols_hi, cols_lo, E->d_bmap, E->d_bbox);
   } else {
+    const int st = tag_level(E, level, E->d_tags[level], nullptr, 1, 0);
+    if (st != ENL_OK) return st;
     tag_block_kernel<<<E->nsm * 4, 256, 0, s>>>(E->d_tags[level], L.nx, L.ny, block, buffer, E->d_bmap, nbx, nby,
                                                 E->d_bbox);
   }
