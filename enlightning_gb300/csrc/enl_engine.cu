@@ -758,16 +758,19 @@ __global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int b
 // Independent problems: every patch of the table is a domain of its own, and
 // its 3-cell band is filled by the single-patch rule of enlightning.C:830-1008
 // (edges from the first interior cell, corners from the interior corner, the
-// normal momenta negated on REFLECT sides).  One block per patch.
+// normal momenta negated on REFLECT sides).  blockIdx.y picks the patch, the
+// blocks along x share its band (neighbouring threads: neighbouring band
+// cells of one field).
+constexpr int kBandBlocksPerPatch = 32;
 template <typename S>
 __global__ void physbc_patches_kernel(CanvasT<S> V, const int4* patches, int off, int cnt, int bcL, int bcR,
                                       int bcB, int bcT) {
-  for (int p = blockIdx.x; p < cnt; p += gridDim.x) {
+  for (int p = blockIdx.y; p < cnt; p += gridDim.y) {
     const int4 b = patches[off + p];
     const int w = b.y - b.x + 1, h = b.w - b.z + 1;
     const int nband = 6 * h + 6 * w + 36;
-    for (int t = threadIdx.x; t < nband * kNF; t += blockDim.x) {
-      int k = t % kNF, r = t / kNF;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nband * kNF; t += gridDim.x * blockDim.x) {
+      int k = t / nband, r = t - k * nband;
       int i, j, si, sj;
       bool negu = false, negv = false;
       if (r < 6 * h) {
@@ -1377,35 +1380,42 @@ struct PackArgs {
   EosConst32 E32;
 };
 
-template <typename S>
+// One block per 32x8 tile; all NF loads of a cell are issued before its
+// stores.
+template <typename S, int NF, bool UNPACK>
 __global__ void pack_kernel(PackArgs<S> A) {
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
-    int4 td = A.tiles[t];
-    int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
-    int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int4 td = A.tiles[t];
+    const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (tx >= w || ty >= h) continue;
-    long long o = A.off[t] + ty * w + tx;
+    const long long o = A.off[t] + ty * w + tx;
     const CanvasT<S>& V = A.lev[lvl];
     const int i = td.x + tx, j = td.y + ty;
-    for (int k = 0; k < A.nfields; ++k) {
-      S& c = V.at(k, i, j);
-      S& p = A.packed[k * A.total + o];
-      if (A.unpack) c = p;
-      else p = c;
-    }
-    if (A.unpack && A.nfields == 5) {  // p and T follow from the state (update_state)
-      if constexpr (std::is_same<S, float>::value) {
-        float pp, tp;
-        eos_pert32(A.E32, V.at(0, i, j), V.at(3, i, j), row_height32((float)A.ylo, (float)A.dy[lvl], j), pp, tp);
-        V.at(5, i, j) = pp;
-        V.at(6, i, j) = tp;
-      } else {
-        double pv, tv;
-        eos_abs64(A.E64, V.at(0, i, j), V.at(3, i, j), __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)j + 0.5)), pv,
-                  tv);
-        V.at(5, i, j) = pv;
-        V.at(6, i, j) = tv;
+    S v[NF];
+    if (UNPACK) {
+#pragma unroll
+      for (int k = 0; k < NF; ++k) v[k] = A.packed[k * A.total + o];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) V.at(k, i, j) = v[k];
+      if (NF == 5) {  // p and T follow from the state (update_state)
+        if constexpr (std::is_same<S, float>::value) {
+          float pp, tp;
+          eos_pert32(A.E32, v[0], v[3], row_height32((float)A.ylo, (float)A.dy[lvl], j), pp, tp);
+          V.at(5, i, j) = pp;
+          V.at(6, i, j) = tp;
+        } else {
+          double pv, tv;
+          eos_abs64(A.E64, v[0], v[3], __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)j + 0.5)), pv, tv);
+          V.at(5, i, j) = pv;
+          V.at(6, i, j) = tv;
+        }
       }
+    } else {
+#pragma unroll
+      for (int k = 0; k < NF; ++k) v[k] = V.at(k, i, j);
+#pragma unroll
+      for (int k = 0; k < NF; ++k) A.packed[k * A.total + o] = v[k];
     }
   }
 }
@@ -1814,6 +1824,9 @@ static int rebuild_tables(Engine* E) {
     acc += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
   }
   E->tables_from = nl;
+  // independent problems: the band fill takes the patch counts as launch
+  // arguments, so a captured step does not survive new patches
+  if (E->cfg.independent) E->graph_valid = false;
   // Which levels' physical ghost bands a step reads: those with a patch
   // within 3 cells (the stencil reach) of a side, and those under a finer
   // level with a patch within 3 + ratio fine cells of a side (its halo cells
@@ -2025,8 +2038,8 @@ static int fill_level(Engine* E, int l, int which, bool skip_unread) {
   }
   if (c.independent) {
     if (E->patch_cnt[l])
-      physbc_patches_kernel<S><<<E->patch_cnt[l], 256, 0, s>>>(L.view<S>(which), E->d_patchtab.p, E->patch_off[l],
-                                                               E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+      physbc_patches_kernel<S><<<dim3(kBandBlocksPerPatch, std::min(E->patch_cnt[l], 65535)), 256, 0, s>>>(
+          L.view<S>(which), E->d_patchtab.p, E->patch_off[l], E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
   } else if (!skip_unread || E->bc_read[l]) {
     physbc_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3],
                                                 skip_unread ? E->bc_read[l] : 15);
@@ -3225,7 +3238,14 @@ static void pack_t(Engine* E, long long cells, int unpack, int nfields, void* pa
   A.total = cells;
   A.packed = static_cast<S*>(packed);
   A.unpack = unpack;
-  pack_kernel<S><<<std::min(A.ntiles, E->nsm * 8), 256, 0, stream()>>>(A);
+  const unsigned g = (unsigned)std::max(1, std::min(A.ntiles, 1 << 30));
+  if (nfields == 5) {
+    if (unpack) pack_kernel<S, 5, true><<<g, 256, 0, stream()>>>(A);
+    else pack_kernel<S, 5, false><<<g, 256, 0, stream()>>>(A);
+  } else {
+    if (unpack) pack_kernel<S, kNF, true><<<g, 256, 0, stream()>>>(A);
+    else pack_kernel<S, kNF, false><<<g, 256, 0, stream()>>>(A);
+  }
 }
 
 extern "C" {
