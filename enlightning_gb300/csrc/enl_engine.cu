@@ -3054,6 +3054,27 @@ int enl_engine_regrid(void* e, int level, int block, int tag_buffer, int nest_bl
   return st;
 }
 
+int enl_halo_segments(const int* boxes, int nbox, int nx, int ny, int* segs, int max_segs, int* nseg) {
+  if (nbox < 0 || (nbox > 0 && !boxes) || nx < 1 || ny < 1 || max_segs < 0 || (max_segs > 0 && !segs) || !nseg) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  std::vector<int4> P(nbox), out;
+  for (int q = 0; q < nbox; ++q) P[q] = make_int4(boxes[4 * q], boxes[4 * q + 1], boxes[4 * q + 2], boxes[4 * q + 3]);
+  halo_segments(P, nx, ny, out);
+  *nseg = (int)out.size();
+  for (int q = 0; q < (int)out.size() && q < max_segs; ++q) {
+    segs[3 * q] = out[q].x;
+    segs[3 * q + 1] = out[q].y;
+    segs[3 * q + 2] = out[q].z;
+  }
+  if ((int)out.size() > max_segs) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  return ENL_OK;
+}
+
 int enl_check_bounded_wait(int polls, int arrive) {
   if (polls < 1) {
     set_error(ENL_ERR_ARG);

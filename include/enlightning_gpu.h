@@ -414,6 +414,16 @@ int enl_cluster_tags(const unsigned char* tags, const unsigned char* allowed,
                      int min_size, int max_size, int* boxes, int max_boxes,
                      int* nboxes);
 
+/* Host-side: the coarse-fine halo of a level's patches (nbox boxes ilo, ihi,
+ * jlo, jhi) — the cells of [0,nx)x[0,ny) within 3 cells (Chebyshev) of the
+ * patch union and in no patch — as row segments (j, i_begin, i_end) in row
+ * order, left to right, the cells the engine interpolates from the coarser
+ * level.  Writes at most max_segs segments (3 ints each) and the count
+ * needed to nseg (ENL_ERR_ARG when that exceeds max_segs).  No GPU
+ * involved. */
+int enl_halo_segments(const int* boxes, int nbox, int nx, int ny, int* segs,
+                      int max_segs, int* nseg);
+
 /* ---------------------------------------------------------------------------
  * Allocation-free stable time step of one patch.  No counterpart in the
  * reference (its dt, enlightning.C:433-456, needs no reduction); it is for
