@@ -463,7 +463,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     }
     // compaction counts: DRP cells first, then WENO cells, each in tile order
     int nd = 0, nw = 0, od = 0, ow = 0;
-    if (!__syncthreads_or(bw != 0u)) {
+    if constexpr (SCHEME == kWeno) {  // every cell WENO: the natural order
+      __syncthreads();
+      nw = w * h;
+    } else if (!__syncthreads_or(bw != 0u)) {
       nd = w * h;  // no WENO cell: the natural order, no counts needed
     } else {
       if (lane == 0) {
@@ -543,7 +546,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       }
     }
     // a tile without WENO cells keeps its natural order (no list, no barrier)
-    const bool direct = nw == 0;
+    const bool direct = SCHEME == kWeno || nw == 0;  // one branch for the whole tile
     if (valid && !direct) {
       unsigned lt = (1u << lane) - 1u;
       int pos = flag ? (nd + ow + __popc(bw & lt)) : (od + __popc(bd & lt));
@@ -556,7 +559,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     }
     if (!direct) __syncthreads();
     if (direct ? valid : (tid < nd + nw)) {
-      const int e = direct ? ((ty << 5) | tx) : s_list[tid];
+      const int e = direct ? ((ty << 5) | tx | (SCHEME == kWeno ? 1 << 16 : 0)) : s_list[tid];
       const int cx = e & 31, cy = (e >> 5) & 0xff, f = (e >> 16) & 1;
       const int c2 = (cy + 3) * kBW + (cx + 3);
       const int c32 = (cy + 3) * kBW32 + (cx + 3);
