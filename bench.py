@@ -469,6 +469,37 @@ WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource, "pulses64": Pu
 # ---------------------------------------------------------------------------
 
 
+def host_cpu_model():
+    """The host CPU's model name (/proc/cpuinfo, else lscpu), or the machine type."""
+    import platform
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.machine()
+
+
+def cpu_baseline_with_single_core(wl):
+    """The workload's CPU baseline with every host thread, plus the same
+    sample on one thread (a shorter window) and the CPU model."""
+    cb = wl.cpu_baseline()
+    one = wl.cpu_baseline(budget_s=3.0, threads=1)
+    cb["value_1core"] = one["value"]
+    cb["sample_1core"] = one["sample"]
+    cb["cpu_model"] = host_cpu_model()
+    return cb
+
+
 def max_over_ranks(ms, ws, device=None):
     """The slowest rank's time: replicas run the same work, and the job is
     done when the last one is."""
@@ -657,7 +688,7 @@ def run_ours(args):
            "d2h_bytes_per_step": nbytes}
     if rank != 0:
         return
-    cb = wl.cpu_baseline() if not args.no_cpu_baseline else None
+    cb = cpu_baseline_with_single_core(wl) if not args.no_cpu_baseline else None
     traffic = None
     tf = os.path.join(ROOT, "profiles", "rhs_traffic.json")
     if os.path.exists(tf):
@@ -803,7 +834,7 @@ def run_linesource(args):
     if rank != 0:
         return
     health = wl.fast.health()
-    cb = wl.cpu_baseline() if not args.no_cpu_baseline else None
+    cb = cpu_baseline_with_single_core(wl) if not args.no_cpu_baseline else None
     # DRAM bytes of one stage launch from an ncu capture, per cell, scaled to
     # this workload's launch (the capture ran a smaller case of the same kernel)
     traffic = None
