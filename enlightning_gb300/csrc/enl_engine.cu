@@ -85,7 +85,10 @@ constexpr int kOffMlp = kOffPlanes + kPlanesBytes;
 constexpr int kOffPlanesS = 2 * kBufS;
 constexpr int kOffMlpS = kOffPlanesS + kPlanesBytes;
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
-constexpr int kFeatRows = 32;                    // learned switch: cells per network chunk
+// learned switch: cells per network chunk (8 warps x 16 cells); their BF16
+// features take the planes' place while the planes are not yet built
+constexpr int kFeatRows = 128;
+static_assert(kFeatRows * kFeat * 2 <= kPlanesBytes, "the features fit where the planes go");
 // Resident stage blocks per SM with FP32 storage (bounds the registers per
 // thread: 4 blocks of 256 threads leave 64, 3 leave 80).  Four blocks need
 // the smaller staging buffers of ENL_STAGE_UN_TMA 0 (4 x 56 KB of shared
@@ -299,9 +302,8 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   float* tile32_conv = reinterpret_cast<float*>(smem_raw + kOffTile32);  // FP64 storage, FAST
   float* planes = reinterpret_cast<float*>(smem_raw + (kF32S ? kOffPlanesS : kOffPlanes));  // FAST
   // learned sensor (FAST + hybrid only): features of up to kFeatRows cells
-  // at a time; the network image stays in global memory
-  constexpr int kMlpOff = kF32S ? kOffMlpS : kOffMlp;
-  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpOff);
+  // at a time in the planes' place; the network image stays in global memory
+  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(planes);
   __shared__ unsigned char s_flag[256];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
@@ -434,8 +436,8 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     }
     unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
     unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
-    if (FAST) {
-      // planes of u, v and the fluxes at every halo position of the tile
+    // planes of u, v and the fluxes at every halo position of the tile
+    auto build_planes = [&]() {
       const float rho0f = A.F[lvl].rho0, rT0f = A.F[lvl].rho0T0;
       // kBH * kBW = 532 positions: the 20 of the third pass fall on the last
       // warp, not on warp 0, which also stages the next tile
@@ -460,7 +462,11 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
             planes[kPlOffG + k * kPlaneG + row * kTW + (col - 3)] = fmaf(v, wk[k], k == 2 ? pp : 0.0f);
         }
       }
-    }
+    };
+    // the learned review (level 0) keeps its features where the planes go, so
+    // its tiles build the planes after it
+    const bool review = learned && lvl == 0;
+    if (FAST && !review) build_planes();
     // compaction counts: DRP cells first, then WENO cells, each in tile order
     int nd = 0, nw = 0, od = 0, ow = 0;
     if constexpr (SCHEME == kWeno) {  // every cell WENO: the natural order
@@ -485,13 +491,13 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       }
     }
     int nfb = 0;
-    if (learned && lvl == 0 && nw > 0) {
+    if (review && nw > 0) {
       // learned switch: it refines the plain one and can only send cells the
       // plain switch put on WENO back to DRP.  Those cells (numbered in tile
       // order by the counts above) go through the BF16 MLP on the tensor
       // cores in chunks of kFeatRows, one warp per 16 cells; cells with
       // |logit| <= margin keep the plain decision.  Tiles without such cells
-      // (almost all) pay nothing: the counts above were needed anyway.
+      // pay one barrier (the planes follow the review).
       const int slot = ow + __popc(bw & ((1u << lane) - 1u));
       for (int c0 = 0; c0 < nw; c0 += kFeatRows) {
         if (valid && flag && slot >= c0 && slot < c0 + kFeatRows) {
@@ -544,6 +550,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
         nd += s_cnt[0][q];
         nw += s_cnt[1][q];
       }
+    }
+    if (FAST && review) {
+      build_planes();
+      __syncthreads();
     }
     // a tile without WENO cells keeps its natural order (no list, no barrier)
     const bool direct = SCHEME == kWeno || nw == 0;  // one branch for the whole tile
@@ -2406,8 +2416,7 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
   if (E->f32s) E->smem_bytes = kOffMlpS;
   else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kOffMlp : 2 * kStageBufBytes;
-  if (cfg->precision != ENL_PREC_FP64 && cfg->learned)
-    E->smem_bytes += align128(kFeatRows * kFeat * (int)sizeof(__nv_bfloat16));
+  // (the learned switch keeps its features in the planes' place: no more)
   StageFn fn = pick_stage(cfg->precision, cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
   int per_sm = 0;
