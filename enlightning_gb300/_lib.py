@@ -103,6 +103,7 @@ ENGINE_SIGNATURES = {
     "enl_engine_upload_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     "enl_engine_sync": (C.c_int, [C.c_void_p]),
     "enl_check_bounded_wait": (C.c_int, [C.c_int, C.c_int]),
+    "enl_mlp_erf_error": (C.c_int, [C.POINTER(C.c_double)]),
     "enl_halo_segments": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
                                     C.POINTER(C.c_int)]),
     "enl_engine_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

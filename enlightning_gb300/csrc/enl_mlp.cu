@@ -6,6 +6,7 @@
 // below 0.9999.  The learned sensor predicts from 40 stencil features
 // (enl_mlp.cuh) whether WENO is needed, trained on the plain switch and on
 // the local difference between the DRP and WENO right-hand sides.
+#include <cstring>
 #include <cstdio>
 
 #include "enl_mlp.cuh"
@@ -277,7 +278,36 @@ __global__ void adam_kernel(float* P, const float* grad, float* m, float* v, int
 
 using namespace enl;
 
+// Largest |erf_as(x) - erff(x)| over n points evenly spread in [-6, 6]
+// (bits of a non-negative float: ordered as unsigned integers).
+__global__ void erf_check_kernel(int n, unsigned* max_bits) {
+  float m = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float x = -6.0f + 12.0f * (float)i / (float)(n - 1);
+    m = fmaxf(m, fabsf(erf_as(x) - erff(x)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(max_bits, __float_as_uint(m));
+}
+
 extern "C" {
+
+int enl_mlp_erf_error(double* max_err) {
+  if (!max_err) return ENL_ERR_ARG;
+  unsigned* d = nullptr;
+  if (cudaMalloc(&d, sizeof(unsigned)) != cudaSuccess) return ENL_ERR_CUDA;
+  cudaMemsetAsync(d, 0, sizeof(unsigned), stream());
+  erf_check_kernel<<<256, 256, 0, stream()>>>(1 << 22, d);
+  unsigned h = 0;
+  cudaMemcpyAsync(&h, d, sizeof(unsigned), cudaMemcpyDeviceToHost, stream());
+  cudaStreamSynchronize(stream());
+  cudaFree(d);
+  float f;
+  memcpy(&f, &h, sizeof(f));
+  *max_err = f;
+  return check_launch("mlp erf check");
+}
 
 int enl_mlp_nparams(void) { return kNParams; }
 

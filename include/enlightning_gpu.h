@@ -312,6 +312,10 @@ int enl_engine_profile(void* engine, int on, double* ms_total,
  * and activations on the tensor cores, FP32 accumulation.  Cells whose logit
  * is within +-margin of 0 are decided by the plain switch. */
 int enl_mlp_nparams(void);
+/* The network's GELU uses erf by Abramowitz & Stegun 7.1.26 (|error| <=
+ * 1.5e-7 in exact arithmetic, evaluated in FP32); this returns its largest
+ * difference from the CUDA math library's erff over 4M points in [-6, 6]. */
+int enl_mlp_erf_error(double* max_err);
 /* Logits of n feature rows (device BF16 [n][40]) into device float[n]. */
 int enl_mlp_forward(const void* X, long n, const float* params, float* logits);
 /* Sums over the n rows of the weighted BCE-with-logits loss gradient

@@ -124,3 +124,16 @@ def test_trained_network_gains_over_plain_switch(precision):
     for k in (0, 1, 2, 4, 5):
         assert relL2(b[0][k], a[0][k]) <= 1e-3
     assert relL2(b[0][0] - prm["rho0"], a[0][0] - prm["rho0"]) <= 1e-3
+
+
+def test_network_erf_within_published_bound_of_library_erff():
+    """The GELU's erf (Abramowitz & Stegun 7.1.26: |error| <= 1.5e-7 in exact
+    arithmetic, evaluated in FP32 with the hardware reciprocal and
+    exponential) against CUDA's erff on 4M points in [-6, 6]: within 1e-6,
+    three orders of magnitude below the BF16 rounding (2^-8 relative) that
+    every activation takes next."""
+    import ctypes as C
+    from enlightning_gb300 import _lib
+    err = C.c_double()
+    assert _lib.lib().enl_mlp_erf_error(C.byref(err)) == 0
+    assert err.value <= 1e-6, err.value
