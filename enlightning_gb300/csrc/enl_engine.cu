@@ -463,10 +463,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
         }
       }
     };
-    // the learned review (level 0) keeps its features where the planes go, so
-    // its tiles build the planes after it
+    // the learned review (level 0 tiles with WENO cells) keeps its features
+    // where the planes are and rebuilds them after it
     const bool review = learned && lvl == 0;
-    if (FAST && !review) build_planes();
+    if (FAST) build_planes();
     // compaction counts: DRP cells first, then WENO cells, each in tile order
     int nd = 0, nw = 0, od = 0, ow = 0;
     if constexpr (SCHEME == kWeno) {  // every cell WENO: the natural order
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       // order by the counts above) go through the BF16 MLP on the tensor
       // cores in chunks of kFeatRows, one warp per 16 cells; cells with
       // |logit| <= margin keep the plain decision.  Tiles without such cells
-      // pay one barrier (the planes follow the review).
+      // pay nothing; tiles with them build their planes twice.
       const int slot = ow + __popc(bw & ((1u << lane) - 1u));
       for (int c0 = 0; c0 < nw; c0 += kFeatRows) {
         if (valid && flag && slot >= c0 && slot < c0 + kFeatRows) {
@@ -550,9 +550,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
         nd += s_cnt[0][q];
         nw += s_cnt[1][q];
       }
-    }
-    if (FAST && review) {
-      build_planes();
+      build_planes();  // the features took the planes' place
       __syncthreads();
     }
     // a tile without WENO cells keeps its natural order (no list, no barrier)
