@@ -896,7 +896,12 @@ __global__ void copy_tiles_kernel(CanvasT<S> dst, CanvasT<S> src, const int4* ti
 
 // Bilinear fill of whole boxes (new fine data after a regrid).
 template <typename S>
-__global__ void refine_box_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, int ilo, int jlo, int w, int h) {
+// blockIdx.y picks the box (ilo, ihi, jlo, jhi) of `boxes`; the blocks along
+// x share its cells.
+__global__ void refine_box_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4* boxes, int nbox) {
+  for (int q = blockIdx.y; q < nbox; q += gridDim.y) {
+  const int4 bx = boxes[q];
+  const int ilo = bx.x, jlo = bx.z, w = bx.y - bx.x + 1, h = bx.w - bx.z + 1;
   long n = (long)w * h;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     int I = ilo + (int)(t % w), J = jlo + (int)(t / w);
@@ -909,6 +914,7 @@ __global__ void refine_box_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, int ilo
       S hi = ((S)1 - fx) * C.at(k, ic, jc + 1) + fx * C.at(k, ic + 1, jc + 1);
       F.at(k, I, J) = ((S)1 - fy) * lo + fy * hi;
     }
+  }
   }
 }
 
@@ -1593,6 +1599,10 @@ struct Engine {
   // halo interpolation)
   int bc_read[kL] = {15, 15, 15, 15};
   DevArray<int4> d_tiles, d_halo, d_ctiles, d_patchtab;
+  DevArray<int4> d_rboxes;  // boxes of the last refine_init
+  void* rbox_host = nullptr;  // their pinned staging
+  size_t rbox_cap = 0;
+  cudaEvent_t rbox_ev = nullptr;
   int* d_meta = nullptr;
   int* d_counters = nullptr;   // 3 stage counters
   int* d_health = nullptr;
@@ -2481,6 +2491,11 @@ int enl_engine_destroy(void* e) {
   for (int q = 0; q < 6; ++q)
     if (E->pev[q]) cudaEventDestroy(E->pev[q]);
   if (E->d_smax) cudaFree(E->d_smax);
+  if (E->rbox_ev) {
+    cudaEventSynchronize(E->rbox_ev);
+    cudaEventDestroy(E->rbox_ev);
+  }
+  if (E->rbox_host) cudaFreeHost(E->rbox_host);
   if (E->stage_ev) {
     cudaEventSynchronize(E->stage_ev);
     cudaEventDestroy(E->stage_ev);
@@ -2542,21 +2557,42 @@ int enl_engine_refine_init(void* e, int level, int nbox, const int* boxes) {
   }
   cudaStream_t s = stream();
   Level& L = E->lev[level];
+  long most = 0;
   for (int q = 0; q < nbox; ++q) {
     int ilo = boxes[4 * q], ihi = boxes[4 * q + 1], jlo = boxes[4 * q + 2], jhi = boxes[4 * q + 3];
     if (ilo < 0 || jlo < 0 || ihi >= L.nx || jhi >= L.ny || ihi < ilo || jhi < jlo) {
       set_error(ENL_ERR_ARG);
       return ENL_ERR_ARG;
     }
-    long n = (long)(ihi - ilo + 1) * (jhi - jlo + 1);
-    const unsigned g = (unsigned)std::min<long>((n + 255) / 256, 4096);
-    if (E->f32s)
-      refine_box_kernel<float><<<g, 256, 0, s>>>(L.view<float>(0), E->lev[level - 1].view<float>(0), E->cfg.ratio,
-                                                 ilo, jlo, ihi - ilo + 1, jhi - jlo + 1);
-    else
-      refine_box_kernel<double><<<g, 256, 0, s>>>(L.view<double>(0), E->lev[level - 1].view<double>(0),
-                                                   E->cfg.ratio, ilo, jlo, ihi - ilo + 1, jhi - jlo + 1);
+    most = std::max(most, (long)(ihi - ilo + 1) * (jhi - jlo + 1));
   }
+  if (nbox == 0) return ENL_OK;
+  // every box in one launch: the boxes go to the device through a pinned
+  // staging buffer of their own (its previous copy has left it)
+  const size_t bytes = (size_t)nbox * sizeof(int4);
+  E->d_rboxes.ensure(nbox);
+  if (E->rbox_ev) cudaEventSynchronize(E->rbox_ev);
+  if (bytes > E->rbox_cap) {
+    if (E->rbox_host) cudaFreeHost(E->rbox_host);
+    E->rbox_cap = bytes + bytes / 2;
+    if (cudaHostAlloc(&E->rbox_host, E->rbox_cap, cudaHostAllocDefault) != cudaSuccess) {
+      E->rbox_host = nullptr;
+      E->rbox_cap = 0;
+      set_error(ENL_ERR_CUDA);
+      return ENL_ERR_CUDA;
+    }
+  }
+  if (!E->rbox_ev) cudaEventCreateWithFlags(&E->rbox_ev, cudaEventDisableTiming);
+  memcpy(E->rbox_host, boxes, bytes);
+  cudaMemcpyAsync(E->d_rboxes.p, E->rbox_host, bytes, cudaMemcpyHostToDevice, s);
+  cudaEventRecord(E->rbox_ev, s);
+  const dim3 g((unsigned)std::min<long>((most + 255) / 256, 1024), (unsigned)std::min(nbox, 65535));
+  if (E->f32s)
+    refine_box_kernel<float><<<g, 256, 0, s>>>(L.view<float>(0), E->lev[level - 1].view<float>(0), E->cfg.ratio,
+                                               E->d_rboxes.p, nbox);
+  else
+    refine_box_kernel<double><<<g, 256, 0, s>>>(L.view<double>(0), E->lev[level - 1].view<double>(0), E->cfg.ratio,
+                                                E->d_rboxes.p, nbox);
   return check_launch("refine_init");
 }
 
