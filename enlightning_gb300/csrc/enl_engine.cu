@@ -46,8 +46,9 @@ constexpr int kTile32Elems = kNF * kPlane32;     // 3920
 constexpr int kTileBytes32 = kTile32Elems * 4;   // 15680
 // Shared-memory layout of the stage kernel.  A TMA destination must start on
 // a 128-byte boundary, so every region is padded to a multiple of 128 bytes.
-//   FP64 state:  [FP64 box A][FP64 box B][FP32 tile (FAST)][MLP]
-//   FP32 state:  [FP32 tile A][FP32 tile B][MLP]
+//   FP64 state:  [FP64 box A][FP64 box B][FP32 tile (FAST)][planes (FAST)]
+//   FP32 state:  [FP32 tile A][FP32 tile B][planes]
+// (the learned switch's features use the planes' space during its review)
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
 constexpr int kStageBufBytes = align128(kTileBytes64);            // 29824
 constexpr int kTile32Bytes = align128(kTileBytes32);              // 15744
@@ -81,12 +82,13 @@ constexpr int kH0Bytes = kTH * kBW32 * 4;        // 1280
 constexpr int kBufS = kTile32Bytes + (kUnTma ? kUnBytes + kH0Bytes : 0);  // per staging buffer
 constexpr int kOffTile32 = 2 * kStageBufBytes;
 constexpr int kOffPlanes = kOffTile32 + kTile32Bytes;
-constexpr int kOffMlp = kOffPlanes + kPlanesBytes;
+constexpr int kSmemFast64 = kOffPlanes + kPlanesBytes;   // dynamic shared memory, FP64 storage + FP32 rhs
 constexpr int kOffPlanesS = 2 * kBufS;
-constexpr int kOffMlpS = kOffPlanesS + kPlanesBytes;
+constexpr int kSmemFast32 = kOffPlanesS + kPlanesBytes;  // dynamic shared memory, FP32 storage
 constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
 // learned switch: cells per network chunk (8 warps x 16 cells); their BF16
-// features take the planes' place while the planes are not yet built
+// features take the planes' place for the review, and the planes are built
+// again after it
 constexpr int kFeatRows = 128;
 static_assert(kFeatRows * kFeat * 2 <= kPlanesBytes, "the features fit where the planes go");
 // Resident stage blocks per SM with FP32 storage (bounds the registers per
@@ -2422,8 +2424,8 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMemset(E->d_dt, 0, 3 * sizeof(double));
   cudaMalloc(&E->d_smax, sizeof(unsigned long long));
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
-  if (E->f32s) E->smem_bytes = kOffMlpS;
-  else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kOffMlp : 2 * kStageBufBytes;
+  if (E->f32s) E->smem_bytes = kSmemFast32;
+  else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kSmemFast64 : 2 * kStageBufBytes;
   // (the learned switch keeps its features in the planes' place: no more)
   StageFn fn = pick_stage(cfg->precision, cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
