@@ -106,6 +106,7 @@ ENGINE_SIGNATURES = {
     "enl_mlp_erf_error": (C.c_int, [C.POINTER(C.c_double)]),
     "enl_halo_segments": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
                                     C.POINTER(C.c_int)]),
+    "enl_measure_fp_peaks": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "enl_engine_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "enl_engine_tag_blocks": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int),
                                         C.POINTER(C.c_int)]),

@@ -1570,12 +1570,22 @@ template <typename T>
 struct DevArray {
   T* p = nullptr;
   size_t cap = 0;
-  bool ensure(size_t n) {  // returns true if reallocated
+  // Room for n elements.  Returns true if the array was reallocated (its old
+  // contents are gone).  When the allocation fails, p is null and cap 0:
+  // callers check p before any copy or launch.
+  bool ensure(size_t n) {
     if (n <= cap) return false;
     if (p) cudaFree(p);
+    p = nullptr;
     // headroom, so that regrids rarely outgrow a table (and a captured graph)
-    cap = std::max<size_t>(n + n / 2, 2 * cap);
-    cudaMalloc(&p, cap * sizeof(T));
+    const size_t want = std::max<size_t>(n + n / 2, 2 * cap);
+    cap = 0;
+    if (cudaMalloc(&p, want * sizeof(T)) != cudaSuccess) {
+      p = nullptr;
+      cudaGetLastError();  // reported as ENL_ERR_CUDA by the caller
+      return true;
+    }
+    cap = want;
     return true;
   }
   ~DevArray() {
@@ -1876,6 +1886,12 @@ static int rebuild_tables(Engine* E) {
   grew |= E->d_ctiles.ensure(std::max<size_t>(E->h_ctiles.size(), 1));
   grew |= E->d_patchtab.ensure(std::max<size_t>(E->h_patchtab.size(), 1));
   if (grew) E->graph_valid = false;
+  if (!E->d_tileoff.p || !E->d_tiles.p || !E->d_halo.p || !E->d_ctiles.p || !E->d_patchtab.p) {
+    E->tables_on_device = false;
+    E->graph_valid = false;
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
   // entries kept on the device: none when a table was reallocated (its old
   // contents are gone) or when the tables were never copied
   const bool keep_dev = !grew && !off_grew && E->tables_on_device;
@@ -2572,8 +2588,14 @@ int enl_engine_refine_init(void* e, int level, int nbox, const int* boxes) {
   // every box in one launch: the boxes go to the device through a pinned
   // staging buffer of their own (its previous copy has left it)
   const size_t bytes = (size_t)nbox * sizeof(int4);
-  E->d_rboxes.ensure(nbox);
+  // the previous refine's kernel has finished with both the device boxes and
+  // their staging (rbox_ev follows its launch, on whatever stream it ran)
   if (E->rbox_ev) cudaEventSynchronize(E->rbox_ev);
+  E->d_rboxes.ensure(nbox);
+  if (!E->d_rboxes.p) {
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
   if (bytes > E->rbox_cap) {
     if (E->rbox_host) cudaFreeHost(E->rbox_host);
     E->rbox_cap = bytes + bytes / 2;
@@ -2587,7 +2609,6 @@ int enl_engine_refine_init(void* e, int level, int nbox, const int* boxes) {
   if (!E->rbox_ev) cudaEventCreateWithFlags(&E->rbox_ev, cudaEventDisableTiming);
   memcpy(E->rbox_host, boxes, bytes);
   cudaMemcpyAsync(E->d_rboxes.p, E->rbox_host, bytes, cudaMemcpyHostToDevice, s);
-  cudaEventRecord(E->rbox_ev, s);
   const dim3 g((unsigned)std::min<long>((most + 255) / 256, 1024), (unsigned)std::min(nbox, 65535));
   if (E->f32s)
     refine_box_kernel<float><<<g, 256, 0, s>>>(L.view<float>(0), E->lev[level - 1].view<float>(0), E->cfg.ratio,
@@ -2595,6 +2616,7 @@ int enl_engine_refine_init(void* e, int level, int nbox, const int* boxes) {
   else
     refine_box_kernel<double><<<g, 256, 0, s>>>(L.view<double>(0), E->lev[level - 1].view<double>(0), E->cfg.ratio,
                                                 E->d_rboxes.p, nbox);
+  cudaEventRecord(E->rbox_ev, s);
   return check_launch("refine_init");
 }
 

@@ -35,7 +35,7 @@ struct MlpSmem {
 
 // The same image built on the host (the stage kernel reads it from global
 // memory through L1: the network runs on few cells, and keeping it out of
-// shared memory keeps three stage blocks per SM).
+// shared memory keeps four stage blocks per SM).
 inline void mlp_build_image(const float* P, MlpSmem& S) {
   for (int n = 0; n < kHid; ++n)
     for (int k = 0; k < kFeatPad; ++k) S.w1t[n][k] = __float2bfloat16_rn(k < kFeat ? P[kOffW1 + k * kHid + n] : 0.0f);

@@ -418,6 +418,15 @@ int enl_cluster_tags(const unsigned char* tags, const unsigned char* allowed,
                      int min_size, int max_size, int* boxes, int max_boxes,
                      int* nboxes);
 
+/* Arithmetic ceilings of the current device, measured now (no counterpart in
+ * the reference; it states the FP64 ceiling that bounds the FP64 right-hand
+ * side).  Writes out[0] = FP64 fused multiply-add rate (TFLOP/s, 2 flops per
+ * FMA), out[1] = correctly rounded FP64 divisions (G/s), out[2] = FP32 fused
+ * multiply-add rate (TFLOP/s), each the best of three launches of
+ * independent dependency chains over every SM.  n >= 3.  Synchronous; takes
+ * some tens of milliseconds. */
+int enl_measure_fp_peaks(double* out, int n);
+
 /* Host-side: the coarse-fine halo of a level's patches (nbox boxes ilo, ihi,
  * jlo, jhi) — the cells of [0,nx)x[0,ny) within 3 cells (Chebyshev) of the
  * patch union and in no patch — as row segments (j, i_begin, i_end) in row
@@ -439,7 +448,10 @@ int enl_halo_segments(const int* boxes, int nbox, int nx, int ny, int* segs,
  * more than 4096 tiles (1,048,576 cells) are refused with ENL_ERR_ARG.  All
  * calls share that array, so calls that overlap on the GPU race; the first
  * call on a device looks up its address and belongs before any stream
- * capture.  Runs on the stream set with enl_set_stream.
+ * capture (the address is cached per device and context; after a
+ * cudaDeviceReset the next call looks it up again).  A non-finite or non-positive
+ * density in the interior makes dt_out a quiet NaN, never a small finite
+ * step.  Runs on the stream set with enl_set_stream.
  * ------------------------------------------------------------------------- */
 int enl_cfl_dt_static(int ifirst0, int ilast0, int ifirst1, int ilast1,
                       int gcw0, int gcw1, const double* w_n, const double* dx,

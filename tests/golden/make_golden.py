@@ -5,9 +5,9 @@ tag_cells.m4 of the reference tree through tests/golden/f77interp.py on small
 seeded patches and stores inputs and outputs.  The hybrid WENO/DRP switch is
 read from the Fortran's own ``tag`` variable at the point where it is tested.
 
-Run here (the reference tree is only present in this container):
+Run it where the reference tree is checked out, giving its root:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference root>
 
 The fixtures are committed; the tests never read the reference tree.
 """
@@ -151,4 +151,6 @@ PARAM_KEYS = ("alpha", "kappa", "mu", "muB", "R", "T_star_n", "T_star_o", "tau_n
               "rho0", "gamma1", "c_p", "p0", "T0", "c_v", "R_tilde", "M")
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <root of the reference tree>")
+    main(sys.argv[1])

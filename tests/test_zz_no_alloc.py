@@ -24,14 +24,14 @@ from enlightning_gb300.constants import REFLECT, default_params  # noqa: E402
 from enlightning_gb300.engine import PREC_FP64, Engine  # noqa: E402
 
 
-def _static_dt(L, box, g, w, dx, c, cfl, dt_max):
+def _static_dt(L, box, g, w, dx, c, cfl, dt_max, g1=None):
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     fn = L.enl_cfl_dt_static
     fn.restype = C.c_int
     fn.argtypes = [C.c_int] * 6 + [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double,
                                    C.c_void_p]
-    st = fn(box[0], box[1], box[2], box[3], g, g, C.c_void_p(w.data_ptr()), _lib.darr(dx), c, cfl, dt_max,
-            C.c_void_p(out.data_ptr()))
+    st = fn(box[0], box[1], box[2], box[3], g, g if g1 is None else g1, C.c_void_p(w.data_ptr()), _lib.darr(dx),
+            c, cfl, dt_max, C.c_void_p(out.data_ptr()))
     _lib.check(st, "enl_cfl_dt_static")
     torch.cuda.synchronize()
     return float(out.item())
@@ -80,3 +80,52 @@ def test_static_dt_rejects_patches_beyond_its_scratch():
             C.c_void_p(out.data_ptr()))
     assert st == 1  # ENL_ERR_ARG
     assert L.enl_get_last_error() == 1
+
+
+def _samrai_patch(nx, ny, g0, g1, seed):
+    """A random conserved state in SAMRAI layout (5 fields, ghosts g0 x g1;
+    ghost values are garbage the call must not read)."""
+    rng = np.random.default_rng(seed)
+    w = rng.normal(0.0, 1e3, (5, ny + 2 * g1, nx + 2 * g0))
+    rho = 1.2 * (1.0 + 0.3 * rng.random((ny, nx)))
+    w[0, g1:g1 + ny, g0:g0 + nx] = rho
+    w[1, g1:g1 + ny, g0:g0 + nx] = rho * rng.normal(0.0, 50.0, (ny, nx))
+    w[2, g1:g1 + ny, g0:g0 + nx] = rho * rng.normal(0.0, 50.0, (ny, nx))
+    return w
+
+
+def _numpy_dt(w, nx, ny, g0, g1, dx, c, cfl, dt_max):
+    r = w[0, g1:g1 + ny, g0:g0 + nx]
+    u = np.abs(w[1, g1:g1 + ny, g0:g0 + nx] / r)
+    v = np.abs(w[2, g1:g1 + ny, g0:g0 + nx] / r)
+    m = float(np.max(np.maximum(u, v) + c))
+    return min((cfl * min(dx)) / m, dt_max)
+
+
+@pytest.mark.parametrize("nx,ny,g0,g1", [(157, 91, 3, 2), (2048, 512, 3, 3), (33, 9, 0, 4)])
+def test_static_dt_ragged_tiles_and_uneven_ghosts(nx, ny, g0, g1):
+    """Partial tiles, unequal ghost widths and a patch of exactly 4096 tiles
+    (2048 x 512), against the same maximum and division in numpy, twice."""
+    L = _lib.lib()
+    c, cfl, dx, dt_max = 343.0, 0.5, (0.1, 0.07), 1.0
+    for call in range(2):
+        w = _samrai_patch(nx, ny, g0, g1, seed=call)
+        wd = torch.from_numpy(w).cuda()
+        got = _static_dt(L, (5, 5 + nx - 1, -2, -2 + ny - 1), g0, wd, dx, c, cfl, dt_max, g1=g1)
+        assert got == _numpy_dt(w, nx, ny, g0, g1, dx, c, cfl, dt_max), (call, got)
+
+
+def test_static_dt_nonfinite_density_gives_nan():
+    """A NaN or non-positive density in the interior makes the step NaN; a
+    clean state right after gives the exact step again (the shared scratch
+    carries nothing over)."""
+    L = _lib.lib()
+    nx, ny, g, dx = 96, 40, 3, (0.1, 0.1)
+    for bad in (float("nan"), 0.0, -1.0):
+        w = _samrai_patch(nx, ny, g, g, seed=5)
+        w[0, g + 17, g + 60] = bad
+        got = _static_dt(L, (0, nx - 1, 0, ny - 1), g, torch.from_numpy(w).cuda(), dx, 343.0, 0.5, 1.0)
+        assert np.isnan(got), (bad, got)
+        w = _samrai_patch(nx, ny, g, g, seed=6)
+        got = _static_dt(L, (0, nx - 1, 0, ny - 1), g, torch.from_numpy(w).cuda(), dx, 343.0, 0.5, 1.0)
+        assert got == _numpy_dt(w, nx, ny, g, g, dx, 343.0, 0.5, 1.0)
