@@ -266,7 +266,7 @@ class LineSource:
             "sigma 2 cells, hybrid_high_llf, regrid every 10 steps")
     REGRID = 10
 
-    def __init__(self, seed=100, learned=False, scale=1, with_plain=True, precision=2):
+    def __init__(self, seed=100, learned=False, scale=1, with_plain=True, precision=2, dense=False, tile_order=0):
         import torch
 
         from enlightning_gb300 import workloads
@@ -282,7 +282,7 @@ class LineSource:
         if scale > 1:
             self.name = self.name.replace("4096x2048", f"{4096 // scale}x{2048 // scale}")
         self.fast, self.fast_h, self.segs = workloads.line_source(self.prm, seed=seed, precision=precision,
-                                                                  learned=learned, **kw)
+                                                                  learned=learned, dense=dense, tile_order=tile_order, **kw)
         if learned:
             from enlightning_gb300 import sensor
             P, margin = sensor.load_weights()
@@ -390,7 +390,7 @@ class PulseBatch(LineSource):
             "sigma U(4,16) cells, dx 0.1 m, reflect, hybrid_high_llf")
     REGRID = 0
 
-    def __init__(self, seed=7, learned=False, scale=1, with_plain=True, precision=2):
+    def __init__(self, seed=7, learned=False, scale=1, with_plain=True, precision=2, dense=False, tile_order=0):
         import torch
 
         from enlightning_gb300 import workloads
@@ -403,7 +403,7 @@ class PulseBatch(LineSource):
         self.precision = precision
         n = 64 // scale
         self.fast, self.boxes, self.info = workloads.pulse_batch(self.prm, seed=seed, n=n, precision=precision,
-                                                                 learned=learned)
+                                                                 learned=learned, dense=dense, tile_order=tile_order)
         if learned:
             from enlightning_gb300 import sensor
             P, margin = sensor.load_weights()
@@ -728,7 +728,8 @@ def run_linesource(args):
     hbm_peak, peak_kind = peaks()
     t_build = time.perf_counter()
     wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=not args.no_plain,
-                                  precision=args.precision)
+                                  precision=args.precision, dense=args.dense,
+                                  tile_order=args.tile_order)
     if args.regrid_every is not None and wl.REGRID:
         wl.REGRID = args.regrid_every
     esize = 4 if args.precision == 2 else 8
@@ -769,6 +770,7 @@ def run_linesource(args):
     st = wl.fast.stats()
     weno_frac = {f"L{l}": float(st[l, 0] / max(1, st[l, 1])) for l in range(st.shape[0])}
     weno_frac["all"] = float(st[:, 0].sum() / max(1, st[:, 1].sum()))
+    uniform_frac = float(st[:, 3].sum() / max(1, st[:, 1].sum()))
     launches = wl.fast.launches_per_step() * args.steps
     # plain arm (per-patch FP64 launches, same hierarchy logic)
     kp = max(1, min(args.steps, args.plain_steps))
@@ -863,6 +865,7 @@ def run_linesource(args):
                    "plain_value": plain_value, "plain_steps": kp,
                    "speedup_vs_plain": (value / plain_value) if plain_value else None,
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
+                   "uniform_tile_fraction": uniform_frac,
                    "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
@@ -898,6 +901,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm (profiling)")
     ap.add_argument("--regrid-every", type=int, default=None,
                     help="regrid interval of the multi-level workloads (default: the workload's, 10)")
+    ap.add_argument("--tile-order", type=int, default=0, choices=[0, 1],
+                    help="stage-kernel tile order: 0 finest level first, 1 level 0 first")
+    ap.add_argument("--dense", action="store_true",
+                    help="compute every stage tile cell by cell (no uniform-tile reuse; same states)")
     ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
                     help="engine mode: 0 FP64, 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
     args = ap.parse_args()

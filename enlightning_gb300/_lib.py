@@ -48,7 +48,8 @@ class EngineConfig(C.Structure):
         ("c_lr", C.c_double), ("tol", C.c_double * 3), ("rho0", C.c_double), ("gamma1", C.c_double),
         ("c_p", C.c_double), ("p0", C.c_double), ("T0", C.c_double), ("c_v", C.c_double),
         ("absorb_width", C.c_double), ("rk_alpha1", C.c_double * 3), ("rk_alpha2", C.c_double * 3),
-        ("rk_beta", C.c_double * 3), ("independent", C.c_int),
+        ("rk_beta", C.c_double * 3), ("independent", C.c_int), ("dense", C.c_int),
+        ("tile_order", C.c_int),
     ]
 
 

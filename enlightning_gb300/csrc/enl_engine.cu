@@ -21,6 +21,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "enl_cell64.cuh"
 #include "enl_fast.cuh"
 #include "enl_mlp.cuh"
 #include "enl_rhs_cell.cuh"
@@ -84,13 +85,19 @@ constexpr int kOffTile32 = 2 * kStageBufBytes;
 constexpr int kOffPlanes = kOffTile32 + kTile32Bytes;
 constexpr int kSmemFast64 = kOffPlanes + kPlanesBytes;   // dynamic shared memory, FP64 storage + FP32 rhs
 constexpr int kOffPlanesS = 2 * kBufS;
+// FP64 right-hand side: [FP64 box A][FP64 box B][FP64 planes]
+constexpr int kOffPlanes64 = 2 * kStageBufBytes;
+constexpr int kPlanes64Bytes = align128(kPl64Elems * 8);               // 38656
+constexpr int kSmem64 = kOffPlanes64 + kPlanes64Bytes;                  // dynamic shared memory, FP64
+static_assert(kBH * kBW == kPos64 && kBW == kBW64, "FP64 planes follow the staged box");
 constexpr int kSmemFast32 = kOffPlanesS + kPlanesBytes;  // dynamic shared memory, FP32 storage
-constexpr int kWaitIters = 1 << 22;              // bounded mbarrier polls
+constexpr unsigned long long kWaitNs = 200000000ull;  // bounded mbarrier waits: 0.2 s of wall time
 // learned switch: cells per network chunk (8 warps x 16 cells); their BF16
 // features take the planes' place for the review, and the planes are built
 // again after it
 constexpr int kFeatRows = 128;
 static_assert(kFeatRows * kFeat * 2 <= kPlanesBytes, "the features fit where the planes go");
+static_assert(kFeatRows * kFeat * 2 <= align128(kPl64Elems * 8), "the features fit where the FP64 planes go");
 // Resident stage blocks per SM with FP32 storage (bounds the registers per
 // thread: 4 blocks of 256 threads leave 64, 3 leave 80).  Four blocks need
 // the smaller staging buffers of ENL_STAGE_UN_TMA 0 (4 x 56 KB of shared
@@ -110,6 +117,8 @@ struct AbsorbTables {
   const double* env[kL][4];
   const float* envf[kL][4];           // the same factors rounded to float
   const unsigned char* cont[kL][4];   // |1 - env| > 1e-8: the walk goes on past this cell
+  // cells whose factor is not exactly 1: index < act (L, B) or >= act (R, T)
+  int act[kL][4];
 };
 
 // The reference walks every patch row from the L (R) side inwards and stops
@@ -137,19 +146,23 @@ __device__ __forceinline__ int absorb_reach(const AbsorbTables& T, int lvl, int 
 }
 
 // Sides whose walk can reach some cell of the w x h tile at (i0, j0) of patch
-// b: the continuation tests are monotone, so the tile's cell nearest to each
-// side decides.
+// b with a factor other than exactly 1: the continuation tests are monotone,
+// so the tile's cell nearest to each side decides.  (The walk from a patch's
+// own edge reaches its first cell even far from the domain side, where the
+// factor is exactly 1; the batched engine leaves such cells as they are,
+// which is the reference's (q - q_amb) * 1 + q_amb except for a last-place
+// rounding when q is beyond twice its ambient value.)
 __device__ __forceinline__ int absorb_tile_mask(const AbsorbTables& T, int lvl, int i0, int j0, int w, int h,
                                                 const int4& b) {
   int m = 0;
   const unsigned char* c = T.cont[lvl][0];
-  if (c && (i0 == b.x || c[i0 - 1])) m |= 1;
+  if (c && i0 < T.act[lvl][0] && (i0 == b.x || c[i0 - 1])) m |= 1;
   c = T.cont[lvl][1];
-  if (c && (i0 + w - 1 == b.y || c[i0 + w])) m |= 2;
+  if (c && i0 + w - 1 >= T.act[lvl][1] && (i0 + w - 1 == b.y || c[i0 + w])) m |= 2;
   c = T.cont[lvl][2];
-  if (c && c[b.z] && (j0 == b.z || c[j0 - 1])) m |= 4;
+  if (c && j0 < T.act[lvl][2] && c[b.z] && (j0 == b.z || c[j0 - 1])) m |= 4;
   c = T.cont[lvl][3];
-  if (c && c[b.w] && (j0 + h - 1 == b.w || c[j0 + h])) m |= 8;
+  if (c && j0 + h - 1 >= T.act[lvl][3] && c[b.w] && (j0 + h - 1 == b.w || c[j0 + h])) m |= 8;
   return m;
 }
 
@@ -170,6 +183,7 @@ __device__ __forceinline__ double relax_(double q, double amb, double tmp) {
 // reference's rounding; height = centre height of the cell row.
 struct EosConst64 {
   double rho0, c, c_lr, gm1_over_2rho0, c_p, p0, T0, c_v, R;
+  double inv_c_p, inv_c_v;  // 1/c_p, 1/c_v (eos_fast64)
 };
 __device__ __forceinline__ void eos_abs64(const EosConst64& E, double w0, double w3, double height, double& p,
                                           double& T) {
@@ -180,6 +194,26 @@ __device__ __forceinline__ void eos_abs64(const EosConst64& E, double w0, double
       __dadd_rn(__dadd_rn(d, __dmul_rn(E.gm1_over_2rho0, __dmul_rn(d, d))), __dmul_rn(__ddiv_rn(w0, E.c_p), s));
   p = __dadd_rn(__dmul_rn(__dmul_rn(cc, cc), inner), E.p0);
   T = E.T0 * exp((s - E.R * log(E.rho0 / w0)) / E.c_v);
+}
+
+// The same as the batched FP64 engine computes it (stage epilogue and state
+// upload alike, so the two agree bit for bit): one seeded reciprocal of rho
+// (rcp64) instead of two divisions, constant divisors as factors, every
+// operation explicitly rounded (no contraction differences between call
+// sites).  Within a few units in the last place of eos_abs64.
+__device__ __forceinline__ double row_height64(double ylo, double dy, int j) {
+  return __dadd_rn(ylo, __dmul_rn(dy, (double)j + 0.5));
+}
+__device__ __forceinline__ void eos_fast64(const EosConst64& E, double w0, double w3, double height, double& p,
+                                           double& T) {
+  const double cc = __dadd_rn(E.c, __dmul_rn(E.c_lr, height));
+  const double ir = rcp64(w0);
+  const double d = __dsub_rn(w0, E.rho0);
+  const double s = __dmul_rn(w3, ir);
+  const double inner =
+      __dadd_rn(__dadd_rn(d, __dmul_rn(E.gm1_over_2rho0, __dmul_rn(d, d))), __dmul_rn(__dmul_rn(w0, E.inv_c_p), s));
+  p = __dadd_rn(__dmul_rn(__dmul_rn(cc, cc), inner), E.p0);
+  T = __dmul_rn(E.T0, exp(__dmul_rn(__dsub_rn(s, __dmul_rn(E.R, log(__dmul_rn(E.rho0, ir)))), E.inv_c_v)));
 }
 
 // The same in single-precision perturbation form: rp = rho - rho0, w3 = rho s;
@@ -218,7 +252,10 @@ struct StageArgs {
   RhsConst P[kL];
   FastConst F[kL];
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
+  int uniform;              // uniform tiles reuse a computed cell (c_lr == 0 and not dense)
+  int finest_first;         // claim tiles from the end of the table (finest level first)
   EosConst32 E32;  // FP32-storage epilogue
+  EosConst64 E64;  // FP64 epilogue
   double a1, a2, bdt, beta;
   const double* dt_dev;  // adaptive time step in device memory (or null)
   float a1f, a2f, bdtf, betaf;
@@ -227,7 +264,8 @@ struct StageArgs {
   const int* ntiles;
   int* counter;
   int* health;
-  unsigned long long* stats;  // [level][3]: weno cells, cells, cells decided by the plain-sensor fallback
+  unsigned long long* stats;  // [level][4]: weno cells, cells, cells decided by the plain-sensor fallback,
+                              // cells of uniform tiles stored from the cache
   AbsorbTables absorb;        // absorbing envelope, applied to each finished cell
   bool any_absorb;
   const int4* patchtab;       // patch boxes of all levels (tile .w = index)
@@ -280,6 +318,135 @@ struct SAcc32R {
 
 __device__ __forceinline__ void raise_health(int* h, int code) { atomicCAS(h, 0, code); }
 
+// Per-block cache of the result of a uniform tile: a tile whose staged halo
+// box holds one value per field, bit for bit, and whose cells share their
+// u^n and H0 values (and lie in no absorbing band, with c_lr = 0) has the
+// same inputs in every cell, so every cell computes the same outputs.  The
+// first such tile of a level is computed in full and its cell (0, 0) records
+// its inputs (key) and outputs (res); a later uniform tile of the level with
+// the same key stores res without computing it.  The results are those of
+// the full computation by construction.
+template <typename S>
+struct UniEntry {
+  S key[13];  // the 7 staged fields, u^n (5), H0
+  S res[7];   // the 7 stored fields of a cell
+  int weno;   // the switch decision
+  int valid;
+};
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
+// Input k of a uniform tile: the staged fields (0..6), u^n (7..11: the staged
+// fields 0..4 in stage 1, else the first cell's values) and H0 (12).
+template <typename S, int kPl>
+__device__ __forceinline__ S uni_key(const S* box, const S* first, int un_is_in, int k) {
+  return k < 7 ? box[k * kPl] : (k < 12 ? (un_is_in ? box[(k - 7) * kPl] : first[k - 7]) : first[5]);
+}
+
+// The uniform-tile test of the stage kernel, in two out-of-line parts (the
+// stage kernel's cell computation keeps its registers) around one block
+// barrier in the kernel.  uniform_probe: this thread's part of the test, after
+// the tile's halo box has landed in `box` (kPl elements per field, rows of
+// kRow): its share of the box equals each field's first element, and its
+// cell's u^n and H0 equal those of the first cell of its warp, whose values
+// lane 0 writes to wl[warp] (the caller loaded them before the tile's wait,
+// zero in stage 1 where u^n is the staged box).  uniform_hit, after the barrier's AND of the
+// probes: 0 when the tile is not uniform; 1 when it is and the level's cache
+// entry holds its inputs (the cached outputs are stored into every cell of
+// the tile and counted); 2 when it is uniform and must be computed (the
+// caller's cell (0, 0) then fills the entry).  Neither contains a barrier.
+template <typename S, int kPl, int kRow>
+__device__ __noinline__ bool uniform_probe(const S* box, S (*wl)[6], int w, int h, S u0, S u1, S u2, S u3, S u4,
+                                           S hv) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool valid = lane < w && warp < h;
+  const S v[6] = {u0, u1, u2, u3, u4, hv};  // u^n (5 fields) and H0 of this thread's cell
+  // the staged box 16 bytes at a time, every element against its field's
+  // first element (bit patterns OR-ed together: zero when all equal)
+  bool ok;
+  if constexpr (std::is_same<S, double>::value) {
+    static_assert(kRow == 38 && kPl == 532, "FP64 box: rows of 38, 14 rows");
+    const double2* b2 = reinterpret_cast<const double2*>(box);
+    unsigned long long acc = 0ull;
+    for (int q = tid; q < kNF * (kPl / 2); q += 256) {
+      const int k = q / (kPl / 2);
+      const unsigned long long ref = (unsigned long long)__double_as_longlong(box[k * kPl]);
+      const double2 x = b2[q];
+      acc |= ((unsigned long long)__double_as_longlong(x.x) ^ ref) | ((unsigned long long)__double_as_longlong(x.y) ^ ref);
+    }
+    ok = acc == 0ull;
+  } else {
+    static_assert(kRow == 40 && kPl == 560, "FP32 box: rows of 40 (38 used), 14 rows");
+    const float4* b4 = reinterpret_cast<const float4*>(box);
+    unsigned acc = 0u;
+    for (int q = tid; q < kNF * (kPl / 4); q += 256) {
+      const int k = q / (kPl / 4), cv = (q - k * (kPl / 4)) % (kRow / 4);
+      const unsigned ref = __float_as_uint(box[k * kPl]);
+      const float4 x = b4[q];
+      unsigned d = (__float_as_uint(x.x) ^ ref) | (__float_as_uint(x.y) ^ ref);
+      if (cv != kRow / 4 - 1) d |= (__float_as_uint(x.z) ^ ref) | (__float_as_uint(x.w) ^ ref);  // columns 38, 39 unused
+      acc |= d;
+    }
+    ok = acc == 0u;
+  }
+  // every lane takes part in the shuffle (a lane without a cell included:
+  // the full-mask shuffle waits for all 32), only cells compare
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const S first = __shfl_sync(0xffffffffu, v[k], 0);
+    if (valid && !same_bits(v[k], first)) ok = false;
+    if (lane == 0 && valid) wl[warp][k] = v[k];
+  }
+  return ok;
+}
+
+template <typename S, int kPl>
+__device__ __noinline__ int uniform_hit(const StageArgs& A, const S* box, const UniEntry<S>* uc, const S (*wl)[6],
+                                        unsigned* stats, int lvl, int i0, int j0, int w, int h) {
+  for (int q = 1; q < h; ++q)
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+      if (!same_bits(wl[q][k], wl[0][k])) return 0;
+  const UniEntry<S>& U = uc[lvl];
+  bool hit = U.valid != 0;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) hit = hit && same_bits(uni_key<S, kPl>(box, wl[0], A.un_is_in, k), U.key[k]);
+  if (!hit) return 2;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (lane < w && warp < h) {
+    S* out = static_cast<S*>(A.out[lvl]);
+    const long fs = A.fstride[lvl];
+    const long gc = (long)(j0 + warp + 3) * A.pitch[lvl] + (i0 + lane + 3);
+#pragma unroll
+    for (int k = 0; k < kNF; ++k) out[k * fs + gc] = U.res[k];
+  }
+  if (tid == 0) {
+    stats[4 * lvl + 0] += U.weno ? (unsigned)(w * h) : 0u;
+    stats[4 * lvl + 1] += (unsigned)(w * h);
+    stats[4 * lvl + 3] += (unsigned)(w * h);
+  }
+  return 1;
+}
+
+// The cache entry of a uniform tile computed in full: its inputs and the
+// outputs of its cell (0, 0).
+template <typename S, int kPl>
+__device__ __noinline__ void uniform_record(UniEntry<S>* U, const S* box, const S* first, int un_is_in, S w0, S w1,
+                                            S w2, S w3, S w4, S pv, S tv, int weno) {
+#pragma unroll
+  for (int k = 0; k < 13; ++k) U->key[k] = uni_key<S, kPl>(box, first, un_is_in, k);
+  U->res[0] = w0;
+  U->res[1] = w1;
+  U->res[2] = w2;
+  U->res[3] = w3;
+  U->res[4] = w4;
+  U->res[5] = pv;
+  U->res[6] = tv;
+  U->weno = weno;
+  U->valid = 1;
+}
+
 // ---------------------------------------------------------------------------
 // Fused persistent stage kernel: per tile, TMA-stage the (32+6)x(8+6) halo box
 // of all 7 fields, decide WENO/DRP per cell, compact the cells so that each
@@ -287,10 +454,11 @@ __device__ __forceinline__ void raise_health(int* h, int code) { atomicCAS(h, 0,
 // w = a1*u^n + a2*w + beta*dt*KK, then p and T (update_state).
 //
 // S is the storage type of the canvases.  S = double: absolute values, the
-// right-hand side in FP64 (FAST = false) or in FP32 perturbation form after a
-// conversion of the staged box (FAST = true).  S = float (FAST only): the
-// canvases hold perturbations about the ambient state, the box is staged
-// straight into the FP32 tile and the whole cell update is single precision.
+// right-hand side in FP64 from per-tile FP64 planes (FAST = false) or in FP32
+// perturbation form after a conversion of the staged box (FAST = true).
+// S = float (FAST only): the canvases hold perturbations about the ambient
+// state, the box is staged straight into the FP32 tile and the whole cell
+// update is single precision.
 // ---------------------------------------------------------------------------
 template <int SCHEME, int ORDER, bool LLF, bool FAST, typename S>
 __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlocksF32 : 2)
@@ -303,21 +471,24 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   unsigned char* dst[2] = {smem_raw, smem_raw + (kF32S ? kBufS : kStageBufBytes)};
   float* tile32_conv = reinterpret_cast<float*>(smem_raw + kOffTile32);  // FP64 storage, FAST
   float* planes = reinterpret_cast<float*>(smem_raw + (kF32S ? kOffPlanesS : kOffPlanes));  // FAST
-  // learned sensor (FAST + hybrid only): features of up to kFeatRows cells
-  // at a time in the planes' place; the network image stays in global memory
-  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(planes);
+  double* planes64 = reinterpret_cast<double*>(smem_raw + kOffPlanes64);  // FP64 right-hand side
+  // learned sensor (hybrid only): features of up to kFeatRows cells at a
+  // time in the planes' place; the network image stays in global memory
+  __nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(FAST ? (void*)planes : (void*)planes64);
   __shared__ unsigned char s_flag[256];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
   __shared__ int4 s_td[2];  // descriptors of the staged tiles
-  __shared__ unsigned s_stats[3 * kL];
+  __shared__ unsigned s_stats[4 * kL];
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
   __shared__ TileInfo s_tile;
+  __shared__ UniEntry<S> s_uc[kL];
+  __shared__ S s_wl[8][6];  // per warp: u^n (5 fields) and H0 of its first cell
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ntiles = *A.ntiles;
   auto issue = [&](int t, int b) {
-    const int4 td = A.tiles[t];
+    const int4 td = A.tiles[A.finest_first ? ntiles - 1 - t : t];
     s_td[b] = td;
     // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
     // doubles, a multiple of 4 for floats; set_patches only accepts such
@@ -352,9 +523,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     if (tid == 0) raise_health(A.health, ENL_ERR_STATE);
     return;
   }
-  const bool learned = FAST && SCHEME == kHybrid && A.mlp != nullptr;
+  const bool learned = SCHEME == kHybrid && A.mlp != nullptr;
+  if (tid < kL) s_uc[tid].valid = 0;
   if (tid == 0) {
-    for (int q = 0; q < 3 * kL; ++q) s_stats[q] = 0u;
+    for (int q = 0; q < 4 * kL; ++q) s_stats[q] = 0u;
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     fence_mbar_init();
@@ -377,12 +549,24 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     const int4 td = s_td[b];
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     const int i0 = td.x, j0 = td.y;
+    const int tx = lane, ty = warp;
+    const bool valid = tx < w && ty < h;
+    // u^n and H0 of this thread's cell, for the uniform-tile test: loaded
+    // before the wait, so that their latency overlaps it
+    S un_c[5] = {S(0), S(0), S(0), S(0), S(0)}, h0_c = S(0);
+    if (A.uniform && valid) {
+      const long g = (long)(j0 + ty + 3) * A.pitch[lvl] + (i0 + tx + 3);
+      h0_c = static_cast<const S*>(A.h0[lvl])[g];
+      if (!A.un_is_in)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) un_c[k] = static_cast<const S*>(A.un[lvl])[k * A.fstride[lvl] + g];
+    }
 #if ENL_PREFETCH_UN
     if constexpr (kF32S && !kUnTma) {
       // u^n and H0 of this thread's cell are read in the epilogue: start
       // their way towards the SM now
-      if (lane < w && warp < h) {
-        const long g = (long)(j0 + warp + 3) * A.pitch[lvl] + (i0 + lane + 3);
+      if (!A.uniform && valid) {
+        const long g = (long)(j0 + ty + 3) * A.pitch[lvl] + (i0 + tx + 3);
         const float* h0p = static_cast<const float*>(A.h0[lvl]) + g;
         asm volatile(ENL_PREFETCH_OP " [%0];" ::"l"(h0p));
         if (!A.un_is_in) {
@@ -393,11 +577,11 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       }
     }
 #endif
-    if (!mbar_wait_bounded(&mbar[b], phase[b], kWaitIters)) {
+    if (!mbar_wait_timed(&mbar[b], phase[b], kWaitNs)) {
       if (tid == 0) raise_health(A.health, ENL_ERR_TIMEOUT);
       // let copies in flight land (bounded) before the block leaves
-      mbar_wait_bounded(&mbar[b], phase[b], kWaitIters);
-      mbar_wait_bounded(&mbar[b ^ 1], phase[b ^ 1], kWaitIters);
+      mbar_wait_timed(&mbar[b], phase[b], kWaitNs);
+      mbar_wait_timed(&mbar[b ^ 1], phase[b ^ 1], kWaitNs);
       break;
     }
     phase[b] ^= 1u;
@@ -409,284 +593,326 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       s_tile.absorb = A.any_absorb ? absorb_tile_mask(A.absorb, lvl, i0, j0, w, h, pb) : 0;
       s_tile.bdtf = A.dtf_dev ? A.betaf * (*A.dtf_dev) : A.bdtf;
     }
-    if (FAST && !kF32S) {
-      // FP64 box (rows of kBW) -> FP32 perturbations (rows of kBW32)
-      for (int e = tid; e < kTileElems; e += 256) {
-        const int k = e / (kBH * kBW), r = e - k * (kBH * kBW);
-        const int row = r / kBW, col = r - row * kBW;
-        double v = tile[e];
-        double amb = k == 0 ? A.rho0 : (k == 4 ? A.rho0 * A.T0 : (k == 5 ? A.p0 : (k == 6 ? A.T0 : 0.0)));
-        tile32[k * kPlane32 + row * kBW32 + col] = (float)(v - amb);
-      }
-      __syncthreads();
+    // ---- uniform tile: one value per staged field, shared u^n and H0 ----
+    constexpr int kPl = kF32S ? kPlane32 : kBH * kBW;  // elements per staged field
+    int ucode = 0;
+    if (A.uniform) {
+      const S* box = reinterpret_cast<const S*>(dst[b]);
+      const bool ok = uniform_probe<S, kPl, kF32S ? kBW32 : kBW>(box, s_wl, w, h, un_c[0], un_c[1], un_c[2],
+                                                                 un_c[3], un_c[4], h0_c);
+      const bool all = __syncthreads_and(ok) != 0;  // (also publishes s_tile and s_wl)
+      if (all && s_tile.absorb == 0) ucode = uniform_hit<S, kPl>(A, box, s_uc, s_wl, s_stats, lvl, i0, j0, w, h);
     }
-    // switch first: it reads the staged density only, so the barrier that
-    // completes the planes also tells whether the tile has a WENO cell
-    const int tx = lane, ty = warp;
-    const bool valid = tx < w && ty < h;
-    const int cc = (ty + 3) * kBW + (tx + 3);
-    const int cc32 = (ty + 3) * kBW32 + (tx + 3);
-    int flag = 0;
-    if (valid) {
-      if (FAST) {
-        SAcc32R acc{acc32(tile32, planes, tx, ty)};
-        flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
-      } else {
-        SAcc64R acc{SAcc64{tile, cc}};
-        flag = rhs_switch<SCHEME, ORDER, LLF>(acc, A.P[lvl]);
-      }
-    }
-    unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
-    unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
-    // planes of u, v and the fluxes at every halo position of the tile
-    auto build_planes = [&]() {
-      const float rho0f = A.F[lvl].rho0, rT0f = A.F[lvl].rho0T0;
-      // kBH * kBW = 532 positions: the 20 of the third pass fall on the last
-      // warp, not on warp 0, which also stages the next tile
-      for (int e = 255 - tid; e < kBH * kBW; e += 256) {
-        const int row = e / kBW, col = e - row * kBW, o = row * kBW32 + col;
-        const float ir = rcp_approx(rho0f + tile32[o]);
-        const float u = tile32[kPlane32 + o] * ir, v = tile32[2 * kPlane32 + o] * ir;
-        const float pp = tile32[5 * kPlane32 + o];
-        planes[o] = u;
-        planes[kPlOffV + o] = v;
-        float wk[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) wk[k] = tile32[k * kPlane32 + o] + (k == 0 ? rho0f : (k == 4 ? rT0f : 0.0f));
-        if (row >= 3 && row < 3 + kTH) {  // x-fluxes on the interior rows
-#pragma unroll
-          for (int k = 0; k < 5; ++k)
-            planes[kPlOffF + k * kPlaneF + (row - 3) * kBW32 + col] = fmaf(u, wk[k], k == 1 ? pp : 0.0f);
-        }
-        if (col >= 3 && col < 3 + kTW) {  // y-fluxes on the interior columns
-#pragma unroll
-          for (int k = 0; k < 5; ++k)
-            planes[kPlOffG + k * kPlaneG + row * kTW + (col - 3)] = fmaf(v, wk[k], k == 2 ? pp : 0.0f);
-        }
-      }
-    };
-    // the learned review (level 0 tiles with WENO cells) keeps its features
-    // where the planes are and rebuilds them after it
-    const bool review = learned && lvl == 0;
-    if (FAST) build_planes();
-    // compaction counts: DRP cells first, then WENO cells, each in tile order
-    int nd = 0, nw = 0, od = 0, ow = 0;
-    if constexpr (SCHEME == kWeno) {  // every cell WENO: the natural order
-      __syncthreads();
-      nw = w * h;
-    } else if (!__syncthreads_or(bw != 0u)) {
-      nd = w * h;  // no WENO cell: the natural order, no counts needed
-    } else {
-      if (lane == 0) {
-        s_cnt[0][warp] = __popc(bd);
-        s_cnt[1][warp] = __popc(bw);
-      }
-      __syncthreads();
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (q < warp) {
-          od += s_cnt[0][q];
-          ow += s_cnt[1][q];
-        }
-        nd += s_cnt[0][q];
-        nw += s_cnt[1][q];
-      }
-    }
-    int nfb = 0;
-    if (review && nw > 0) {
-      // learned switch: it refines the plain one and can only send cells the
-      // plain switch put on WENO back to DRP.  Those cells (numbered in tile
-      // order by the counts above) go through the BF16 MLP on the tensor
-      // cores in chunks of kFeatRows, one warp per 16 cells; cells with
-      // |logit| <= margin keep the plain decision.  Tiles without such cells
-      // pay nothing; tiles with them build their planes twice.
-      const int slot = ow + __popc(bw & ((1u << lane) - 1u));
-      for (int c0 = 0; c0 < nw; c0 += kFeatRows) {
-        if (valid && flag && slot >= c0 && slot < c0 + kFeatRows) {
-          float fv[kFeat];
-          SAcc32R acc{acc32(tile32, planes, tx, ty)};
-          cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
-#pragma unroll
-          for (int q = 0; q < kFeat; q += 2)
-            *reinterpret_cast<uint32_t*>(feat + (slot - c0) * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
-          s_list[slot - c0] = tid;
+    // a uniform tile whose outputs came from the cache (ucode 1) goes to the
+    // end of the tile; one missing from the cache (ucode 2) is computed in
+    // full and its cell (0, 0) fills the entry (after the barriers that
+    // follow, when no thread reads it)
+    const bool uni = ucode == 2;
+    if (ucode != 1) {
+      if (FAST && !kF32S) {
+        // FP64 box (rows of kBW) -> FP32 perturbations (rows of kBW32)
+        for (int e = tid; e < kTileElems; e += 256) {
+          const int k = e / (kBH * kBW), r = e - k * (kBH * kBW);
+          const int row = r / kBW, col = r - row * kBW;
+          double v = tile[e];
+          double amb = k == 0 ? A.rho0 : (k == 4 ? A.rho0 * A.T0 : (k == 5 ? A.p0 : (k == 6 ? A.T0 : 0.0)));
+          tile32[k * kPlane32 + row * kBW32 + col] = (float)(v - amb);
         }
         __syncthreads();
-        const int g0 = warp * 16;
-        if (g0 < kFeatRows && c0 + g0 < nw) {
-          float logit[2];
-          mlp_logits16(*A.mlp, feat + g0 * kFeat, kFeat, lane, logit);
-          if ((lane & 3) == 0) {
+      }
+      // switch first: it reads the staged density only, so the barrier that
+      // completes the planes also tells whether the tile has a WENO cell
+      int flag = 0;
+      if (valid) {
+        if constexpr (FAST) {
+          SAcc32R acc{acc32(tile32, planes, tx, ty)};
+          flag = SCHEME == kWeno ? 1 : (SCHEME == kDrp ? 0 : sensor_fast(acc, A.F[lvl]));
+        } else {
+          flag = switch64<SCHEME>(acc64p(tile, planes64, tx, ty), A.P[lvl]);
+        }
+      }
+      unsigned bd = __ballot_sync(0xffffffffu, valid && !flag);
+      unsigned bw = __ballot_sync(0xffffffffu, valid && flag);
+      // planes of u, v and the fluxes at every halo position of the tile
+      auto build_planes = [&]() {
+        if constexpr (FAST) {
+          const float rho0f = A.F[lvl].rho0, rT0f = A.F[lvl].rho0T0;
+          // kBH * kBW = 532 positions: the 20 of the third pass fall on the last
+          // warp, not on warp 0, which also stages the next tile
+          for (int e = 255 - tid; e < kBH * kBW; e += 256) {
+            const int row = e / kBW, col = e - row * kBW, o = row * kBW32 + col;
+            const float ir = rcp_approx(rho0f + tile32[o]);
+            const float u = tile32[kPlane32 + o] * ir, v = tile32[2 * kPlane32 + o] * ir;
+            const float pp = tile32[5 * kPlane32 + o];
+            planes[o] = u;
+            planes[kPlOffV + o] = v;
+            float wk[5];
 #pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-              const int sl = g0 + (lane >> 2) + 8 * hh;
-              if (c0 + sl < nw)
-                s_flag[s_list[sl]] =
-                    (unsigned char)(logit[hh] > 0.f ? 2 : 1) | (fabsf(logit[hh]) <= A.margin ? 4 : 0);
+            for (int k = 0; k < 5; ++k) wk[k] = tile32[k * kPlane32 + o] + (k == 0 ? rho0f : (k == 4 ? rT0f : 0.0f));
+            if (row >= 3 && row < 3 + kTH) {  // x-fluxes on the interior rows
+#pragma unroll
+              for (int k = 0; k < 5; ++k)
+                planes[kPlOffF + k * kPlaneF + (row - 3) * kBW32 + col] = fmaf(u, wk[k], k == 1 ? pp : 0.0f);
+            }
+            if (col >= 3 && col < 3 + kTW) {  // y-fluxes on the interior columns
+#pragma unroll
+              for (int k = 0; k < 5; ++k)
+                planes[kPlOffG + k * kPlaneG + row * kTW + (col - 3)] = fmaf(v, wk[k], k == 2 ? pp : 0.0f);
+            }
+          }
+        } else {
+          // FP64: one seeded reciprocal of rho per halo position
+          for (int e = 255 - tid; e < kPos64; e += 256) {
+            const int row = e / kBW64, col = e - row * kBW64;
+            const double ir = rcp64(tile[e]);
+            const double u = tile[kPos64 + e] * ir, v = tile[2 * kPos64 + e] * ir;
+            const double pp = tile[5 * kPos64 + e];
+            planes64[e] = u;
+            planes64[kPl64OffV + e] = v;
+            if (row >= 3 && row < 3 + kTH) {
+#pragma unroll
+              for (int k = 0; k < 5; ++k)
+                planes64[kPl64OffF + k * kPl64F + (row - 3) * kBW64 + col] =
+                    k == 1 ? fma(u, tile[kPos64 + e], pp) : u * tile[k * kPos64 + e];
+            }
+            if (col >= 3 && col < 3 + kTW) {
+#pragma unroll
+              for (int k = 0; k < 5; ++k)
+                planes64[kPl64OffG + k * kPl64G + row * kTW + (col - 3)] =
+                    k == 2 ? fma(v, tile[2 * kPos64 + e], pp) : v * tile[k * kPos64 + e];
             }
           }
         }
+      };
+      // the learned review (level 0 tiles with WENO cells) keeps its features
+      // where the planes are and rebuilds them after it
+      const bool review = learned && lvl == 0;
+      build_planes();
+      // compaction counts: DRP cells first, then WENO cells, each in tile order
+      int nd = 0, nw = 0, od = 0, ow = 0;
+      if constexpr (SCHEME == kWeno) {  // every cell WENO: the natural order
+        __syncthreads();
+        nw = w * h;
+      } else if (!__syncthreads_or(bw != 0u)) {
+        nd = w * h;  // no WENO cell: the natural order, no counts needed
+      } else {
+        if (lane == 0) {
+          s_cnt[0][warp] = __popc(bd);
+          s_cnt[1][warp] = __popc(bw);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          if (q < warp) {
+            od += s_cnt[0][q];
+            ow += s_cnt[1][q];
+          }
+          nd += s_cnt[0][q];
+          nw += s_cnt[1][q];
+        }
+      }
+      int nfb = 0;
+      if (review && nw > 0) {
+        // learned switch: it refines the plain one and can only send cells the
+        // plain switch put on WENO back to DRP.  Those cells (numbered in tile
+        // order by the counts above) go through the BF16 MLP on the tensor
+        // cores in chunks of kFeatRows, one warp per 16 cells; cells with
+        // |logit| <= margin keep the plain decision.  Tiles without such cells
+        // pay nothing; tiles with them build their planes twice.
+        const int slot = ow + __popc(bw & ((1u << lane) - 1u));
+        for (int c0 = 0; c0 < nw; c0 += kFeatRows) {
+          if (valid && flag && slot >= c0 && slot < c0 + kFeatRows) {
+            float fv[kFeat];
+            if constexpr (FAST) {
+              SAcc32R acc{acc32(tile32, planes, tx, ty)};
+              cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
+            } else {
+              SAcc64Feat acc{tile, (ty + 3) * kBW64 + tx + 3, A.rho0, A.p0};
+              cell_features(acc, A.feat_eps, A.feat_eps_p, A.feat_inv_sqrt_eps, fv);
+            }
+#pragma unroll
+            for (int q = 0; q < kFeat; q += 2)
+              *reinterpret_cast<uint32_t*>(feat + (slot - c0) * kFeat + q) = pack_bf16(fv[q], fv[q + 1]);
+            s_list[slot - c0] = tid;
+          }
+          __syncthreads();
+          const int g0 = warp * 16;
+          if (g0 < kFeatRows && c0 + g0 < nw) {
+            float logit[2];
+            mlp_logits16(*A.mlp, feat + g0 * kFeat, kFeat, lane, logit);
+            if ((lane & 3) == 0) {
+#pragma unroll
+              for (int hh = 0; hh < 2; ++hh) {
+                const int sl = g0 + (lane >> 2) + 8 * hh;
+                if (c0 + sl < nw)
+                  s_flag[s_list[sl]] =
+                      (unsigned char)(logit[hh] > 0.f ? 2 : 1) | (fabsf(logit[hh]) <= A.margin ? 4 : 0);
+              }
+            }
+          }
+          __syncthreads();
+        }
+        int fallback = 0;
+        if (valid && flag) {
+          const unsigned char d = s_flag[tid];
+          if (d & 4) fallback = 1;       // plain decision (WENO) kept
+          else flag = (d & 2) ? 1 : 0;
+        }
+        nfb = __syncthreads_count(fallback);  // also orders the counts' reuse below
+        bd = __ballot_sync(0xffffffffu, valid && !flag);
+        bw = __ballot_sync(0xffffffffu, valid && flag);
+        if (lane == 0) {
+          s_cnt[0][warp] = __popc(bd);
+          s_cnt[1][warp] = __popc(bw);
+        }
+        __syncthreads();
+        nd = nw = od = ow = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          if (q < warp) {
+            od += s_cnt[0][q];
+            ow += s_cnt[1][q];
+          }
+          nd += s_cnt[0][q];
+          nw += s_cnt[1][q];
+        }
+        build_planes();  // the features took the planes' place
         __syncthreads();
       }
-      int fallback = 0;
-      if (valid && flag) {
-        const unsigned char d = s_flag[tid];
-        if (d & 4) fallback = 1;       // plain decision (WENO) kept
-        else flag = (d & 2) ? 1 : 0;
+      // a tile without WENO cells keeps its natural order (no list, no barrier)
+      const bool direct = SCHEME == kWeno || nw == 0;  // one branch for the whole tile
+      if (valid && !direct) {
+        unsigned lt = (1u << lane) - 1u;
+        int pos = flag ? (nd + ow + __popc(bw & lt)) : (od + __popc(bd & lt));
+        s_list[pos] = (ty << 5) | tx | (flag << 16);
       }
-      nfb = __syncthreads_count(fallback);  // also orders the counts' reuse below
-      bd = __ballot_sync(0xffffffffu, valid && !flag);
-      bw = __ballot_sync(0xffffffffu, valid && flag);
-      if (lane == 0) {
-        s_cnt[0][warp] = __popc(bd);
-        s_cnt[1][warp] = __popc(bw);
+      if (tid == 0) {  // per-block counts, added to A.stats when the block leaves
+        s_stats[4 * lvl + 0] += (unsigned)nw;
+        s_stats[4 * lvl + 1] += (unsigned)(nd + nw);
+        s_stats[4 * lvl + 2] += (unsigned)nfb;
       }
-      __syncthreads();
-      nd = nw = od = ow = 0;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (q < warp) {
-          od += s_cnt[0][q];
-          ow += s_cnt[1][q];
-        }
-        nd += s_cnt[0][q];
-        nw += s_cnt[1][q];
-      }
-      build_planes();  // the features took the planes' place
-      __syncthreads();
-    }
-    // a tile without WENO cells keeps its natural order (no list, no barrier)
-    const bool direct = SCHEME == kWeno || nw == 0;  // one branch for the whole tile
-    if (valid && !direct) {
-      unsigned lt = (1u << lane) - 1u;
-      int pos = flag ? (nd + ow + __popc(bw & lt)) : (od + __popc(bd & lt));
-      s_list[pos] = (ty << 5) | tx | (flag << 16);
-    }
-    if (tid == 0) {  // per-block counts, added to A.stats when the block leaves
-      s_stats[3 * lvl + 0] += (unsigned)nw;
-      s_stats[3 * lvl + 1] += (unsigned)(nd + nw);
-      s_stats[3 * lvl + 2] += (unsigned)nfb;
-    }
-    if (!direct) __syncthreads();
-    if (direct ? valid : (tid < nd + nw)) {
-      const int e = direct ? ((ty << 5) | tx | (SCHEME == kWeno ? 1 << 16 : 0)) : s_list[tid];
-      const int cx = e & 31, cy = (e >> 5) & 0xff, f = (e >> 16) & 1;
-      const int c2 = (cy + 3) * kBW + (cx + 3);
-      const int c32 = (cy + 3) * kBW32 + (cx + 3);
-      const int gi = i0 + cx, gj = j0 + cy;  // level index
-      const long g = (long)(gj + 3) * A.pitch[lvl] + (gi + 3);
-      const long fs = A.fstride[lvl];
-      if constexpr (kF32S) {
-        // single precision throughout: perturbations in, perturbations out
-        // u^n and H0 of this cell from the prefetched interior boxes
-        const float* unb = reinterpret_cast<const float*>(dst[b] + kTile32Bytes);
-        const float* h0b = reinterpret_cast<const float*>(dst[b] + kTile32Bytes + kUnBytes);
-        const int ci = cy * kBW32 + cx + 3;
-        float* out = static_cast<float*>(A.out[lvl]);
-        SAcc32R acc{acc32(tile32, planes, cx, cy)};
-        float H[5], K[5], wn[5];
-        H[0] = kUnTma ? h0b[ci] : static_cast<const float*>(A.h0[lvl])[g];
-        sources_fast(acc, A.F[lvl], H);
-        fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
-        const float a1 = A.a1f, a2 = A.a2f, bdtf = s_tile.bdtf;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          const float w = tile32[k * kPlane32 + c32];
-          const float u0 = A.un_is_in ? w : (kUnTma ? unb[k * (kTH * kBW32) + ci]
-                                                   : static_cast<const float*>(A.un[lvl])[k * fs + g]);
-          wn[k] = fmaf(bdtf, K[k], fmaf(a1, u0, a2 * w));
-        }
-        // update_state in perturbation form (update_state.m4:90-105)
-        const FastConst& F = A.F[lvl];
-        const float rho = F.rho0 + wn[0];
-        float pq, tp;
-        eos_pert32(A.E32, wn[0], wn[3], row_height32(F.ylo, F.dy, gj), pq, tp);
-        if (s_tile.absorb) {  // perturbations relax towards 0
-          const int reach = absorb_reach(A.absorb, lvl, gi, gj, s_tile.box, s_tile.absorb);
-#pragma unroll
-          for (int sd = 0; sd < 4; ++sd) {
-            if (!(reach & (1 << sd))) continue;
-            const float t_ = A.absorb.envf[lvl][sd][sd < 2 ? gi : gj];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) wn[k] *= t_;
-            pq *= t_;
-            tp *= t_;
-          }
-        }
-#pragma unroll
-        for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
-        out[5 * fs + g] = pq;
-        out[6 * fs + g] = tp;
-        if (!(rho > 0.f) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
-      } else {
-        const double* un = static_cast<const double*>(A.un[lvl]);
-        double* out = static_cast<double*>(A.out[lvl]);
-        double wn[5], pv, tv;
-        if (FAST) {
+      if (!direct) __syncthreads();
+      if (direct ? valid : (tid < nd + nw)) {
+        const int e = direct ? ((ty << 5) | tx | (SCHEME == kWeno ? 1 << 16 : 0)) : s_list[tid];
+        const int cx = e & 31, cy = (e >> 5) & 0xff, f = (e >> 16) & 1;
+        const int c2 = (cy + 3) * kBW + (cx + 3);
+        const int c32 = (cy + 3) * kBW32 + (cx + 3);
+        const int gi = i0 + cx, gj = j0 + cy;  // level index
+        const long g = (long)(gj + 3) * A.pitch[lvl] + (gi + 3);
+        const long fs = A.fstride[lvl];
+        // the uniform tile's first cell records the tile's inputs and outputs
+        const bool record = uni && cx == 0 && cy == 0;
+        if constexpr (kF32S) {
+          // single precision throughout: perturbations in, perturbations out
+          // u^n and H0 of this cell from the prefetched interior boxes
+          const float* unb = reinterpret_cast<const float*>(dst[b] + kTile32Bytes);
+          const float* h0b = reinterpret_cast<const float*>(dst[b] + kTile32Bytes + kUnBytes);
+          const int ci = cy * kBW32 + cx + 3;
+          float* out = static_cast<float*>(A.out[lvl]);
           SAcc32R acc{acc32(tile32, planes, cx, cy)};
-          float H[5], K[5];
-          H[0] = (float)static_cast<const double*>(A.h0[lvl])[g];
+          float H[5], K[5], wn[5];
+          H[0] = kUnTma ? h0b[ci] : static_cast<const float*>(A.h0[lvl])[g];
           sources_fast(acc, A.F[lvl], H);
           fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
+          const float a1 = A.a1f, a2 = A.a2f, bdtf = s_tile.bdtf;
 #pragma unroll
           for (int k = 0; k < 5; ++k) {
-            double win = tile[k * (kBH * kBW) + c2];
-            wn[k] = fma(bdt, (double)K[k], fma(A.a1, un[k * fs + g], A.a2 * win));
+            const float w = tile32[k * kPlane32 + c32];
+            const float u0 = A.un_is_in ? w : (kUnTma ? unb[k * (kTH * kBW32) + ci]
+                                                     : static_cast<const float*>(A.un[lvl])[k * fs + g]);
+            wn[k] = fmaf(bdtf, K[k], fmaf(a1, u0, a2 * w));
           }
           // update_state in perturbation form (update_state.m4:90-105)
-          const float rp = (float)(wn[0] - A.rho0);
-          const float inv_r = 1.0f / (float)wn[0];
-          const float s = (float)wn[3] * inv_r;
-          const float h = (float)(A.ylo + A.dy[lvl] * ((double)gj + 0.5));
-          const float ccl = (float)A.c + (float)A.c_lr * h;
-          const float pp = (ccl * ccl) * ((rp + (float)A.gm1_over_2rho0 * (rp * rp)) + (float)wn[3] / (float)A.c_p);
-          const float x = (s + (float)A.R * log1pf(rp / (float)A.rho0)) / (float)A.c_v;
-          const float tp = (float)A.T0 * expm1f(x);
-          pv = A.p0 + (double)pp;
-          tv = A.T0 + (double)tp;
+          const FastConst& F = A.F[lvl];
+          const float rho = F.rho0 + wn[0];
+          float pq, tp;
+          eos_pert32(A.E32, wn[0], wn[3], row_height32(F.ylo, F.dy, gj), pq, tp);
+          if (s_tile.absorb) {  // perturbations relax towards 0
+            const int reach = absorb_reach(A.absorb, lvl, gi, gj, s_tile.box, s_tile.absorb);
+#pragma unroll
+            for (int sd = 0; sd < 4; ++sd) {
+              if (!(reach & (1 << sd))) continue;
+              const float t_ = A.absorb.envf[lvl][sd][sd < 2 ? gi : gj];
+#pragma unroll
+              for (int k = 0; k < 5; ++k) wn[k] *= t_;
+              pq *= t_;
+              tp *= t_;
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
+          out[5 * fs + g] = pq;
+          out[6 * fs + g] = tp;
+          if (record)
+            uniform_record<S, kPl>(&s_uc[lvl], reinterpret_cast<const S*>(dst[b]), s_wl[0], A.un_is_in, wn[0], wn[1],
+                                   wn[2], wn[3], wn[4], pq, tp, f);
+          if (!(rho > 0.f) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
         } else {
-          SAcc64R acc{SAcc64{tile, c2}};
-          double H[5], K[5];
-          H[0] = static_cast<const double*>(A.h0[lvl])[g];
-          rhs_sources(acc, A.P[lvl], H);
-          rhs_fluxes<SCHEME, ORDER, LLF>(acc, A.P[lvl], gj, f, H, K);
+          const double* un = static_cast<const double*>(A.un[lvl]);
+          double* out = static_cast<double*>(A.out[lvl]);
+          double wn[5], pv, tv;
+          if constexpr (FAST) {
+            SAcc32R acc{acc32(tile32, planes, cx, cy)};
+            float H[5], K[5];
+            H[0] = (float)static_cast<const double*>(A.h0[lvl])[g];
+            sources_fast(acc, A.F[lvl], H);
+            fluxes_fast<ORDER, LLF>(acc, A.F[lvl], gj, f, H, K);
 #pragma unroll
-          for (int k = 0; k < 5; ++k) {
-            double win = tile[k * (kBH * kBW) + c2];
-            wn[k] = __dadd_rn(__dadd_rn(__dmul_rn(A.a1, un[k * fs + g]), __dmul_rn(A.a2, win)),
-                              __dmul_rn(bdt, K[k]));
+            for (int k = 0; k < 5; ++k) {
+              double win = tile[k * (kBH * kBW) + c2];
+              wn[k] = fma(bdt, (double)K[k], fma(A.a1, un[k * fs + g], A.a2 * win));
+            }
+            // update_state in perturbation form (update_state.m4:90-105)
+            const float rp = (float)(wn[0] - A.rho0);
+            const float inv_r = 1.0f / (float)wn[0];
+            const float s = (float)wn[3] * inv_r;
+            const float h = (float)(A.ylo + A.dy[lvl] * ((double)gj + 0.5));
+            const float ccl = (float)A.c + (float)A.c_lr * h;
+            const float pp = (ccl * ccl) * ((rp + (float)A.gm1_over_2rho0 * (rp * rp)) + (float)wn[3] / (float)A.c_p);
+            const float x = (s + (float)A.R * log1pf(rp / (float)A.rho0)) / (float)A.c_v;
+            const float tp = (float)A.T0 * expm1f(x);
+            pv = A.p0 + (double)pp;
+            tv = A.T0 + (double)tp;
+          } else {
+            SAcc64P acc = acc64p(tile, planes64, cx, cy);
+            double H[5], K[5];
+            H[0] = static_cast<const double*>(A.h0[lvl])[g];
+            sources64(acc, A.P[lvl], H);
+            fluxes64<ORDER, LLF>(acc, A.P[lvl], gj, f, H, K);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+              double win = tile[k * (kBH * kBW) + c2];
+              wn[k] = (A.a1 * un[k * fs + g] + A.a2 * win) + bdt * K[k];
+            }
+            // update_state (update_state.m4:90-105), as the state upload computes it
+            eos_fast64(A.E64, wn[0], wn[3], row_height64(A.ylo, A.dy[lvl], gj), pv, tv);
           }
-          const double hgt = __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)gj + 0.5));
-          const double cc_ = __dadd_rn(A.c, __dmul_rn(A.c_lr, hgt));
-          const double d = __dsub_rn(wn[0], A.rho0);
-          const double s = __ddiv_rn(wn[3], wn[0]);
-          const double inner = __dadd_rn(__dadd_rn(d, __dmul_rn(A.gm1_over_2rho0, __dmul_rn(d, d))),
-                                         __dmul_rn(__ddiv_rn(wn[0], A.c_p), s));
-          pv = __dadd_rn(__dmul_rn(__dmul_rn(cc_, cc_), inner), A.p0);
-          tv = A.T0 * exp((s - A.R * log(A.rho0 / wn[0])) / A.c_v);
-        }
-        if (s_tile.absorb) {  // absolute values relax towards the ambient state
-          const int reach = absorb_reach(A.absorb, lvl, gi, gj, s_tile.box, s_tile.absorb);
-          const double rT = __dmul_rn(A.T0, A.rho0);
+          if (s_tile.absorb) {  // absolute values relax towards the ambient state
+            const int reach = absorb_reach(A.absorb, lvl, gi, gj, s_tile.box, s_tile.absorb);
+            const double rT = __dmul_rn(A.T0, A.rho0);
 #pragma unroll
-          for (int sd = 0; sd < 4; ++sd) {
-            if (!(reach & (1 << sd))) continue;
-            const double fa = A.absorb.env[lvl][sd][sd < 2 ? gi : gj];
-            pv = relax_(pv, A.p0, fa);
-            tv = relax_(tv, A.T0, fa);
-            wn[0] = relax_(wn[0], A.rho0, fa);
-            wn[1] = __dmul_rn(wn[1], fa);
-            wn[2] = __dmul_rn(wn[2], fa);
-            wn[3] = __dmul_rn(wn[3], fa);
-            wn[4] = relax_(wn[4], rT, fa);
+            for (int sd = 0; sd < 4; ++sd) {
+              if (!(reach & (1 << sd))) continue;
+              const double fa = A.absorb.env[lvl][sd][sd < 2 ? gi : gj];
+              pv = relax_(pv, A.p0, fa);
+              tv = relax_(tv, A.T0, fa);
+              wn[0] = relax_(wn[0], A.rho0, fa);
+              wn[1] = __dmul_rn(wn[1], fa);
+              wn[2] = __dmul_rn(wn[2], fa);
+              wn[3] = __dmul_rn(wn[3], fa);
+              wn[4] = relax_(wn[4], rT, fa);
+            }
           }
-        }
-        out[5 * fs + g] = pv;
-        out[6 * fs + g] = tv;
+          out[5 * fs + g] = pv;
+          out[6 * fs + g] = tv;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
-        if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4]))
-          raise_health(A.health, ENL_ERR_NONFINITE);
+          for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
+          if (record)
+            uniform_record<S, kPl>(&s_uc[lvl], reinterpret_cast<const S*>(dst[b]), s_wl[0], A.un_is_in, wn[0], wn[1],
+                                   wn[2], wn[3], wn[4], pv, tv, f);
+          if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4]))
+            raise_health(A.health, ENL_ERR_NONFINITE);
+        }
       }
     }
     __syncthreads();  // this staging buffer is refilled two tiles later
@@ -694,7 +920,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     b ^= 1;
   }
   if (tid == 0 && A.stats)
-    for (int q = 0; q < 3 * kL; ++q)
+    for (int q = 0; q < 4 * kL; ++q)
       if (s_stats[q]) atomicAdd(&A.stats[q], (unsigned long long)s_stats[q]);
 }
 
@@ -1036,7 +1262,7 @@ __global__ void eos_plain_kernel(CanvasView S, int ilo, int jlo, int w, int h, E
   // update_state.m4:88 uses the patch's xlo and (j - ifirst1); with the level
   // origin that is the same centre height.
   const double height = __dadd_rn(E.ylo, __dmul_rn(E.dy, (double)j + 0.5));
-  const EosConst64 K{E.rho0, E.c, E.c_lr, E.gm1_over_2rho0, E.c_p, E.p0, E.T0, E.c_v, E.R};
+  const EosConst64 K{E.rho0, E.c, E.c_lr, E.gm1_over_2rho0, E.c_p, E.p0, E.T0, E.c_v, E.R, 1.0 / E.c_p, 1.0 / E.c_v};
   double p, T;
   eos_abs64(K, S.at(0, i, j), S.at(3, i, j), height, p, T);
   S.at(5, i, j) = p;
@@ -1425,7 +1651,7 @@ __global__ void pack_kernel(PackArgs<S> A) {
           V.at(6, i, j) = tp;
         } else {
           double pv, tv;
-          eos_abs64(A.E64, v[0], v[3], __dadd_rn(A.ylo, __dmul_rn(A.dy[lvl], (double)j + 0.5)), pv, tv);
+          eos_fast64(A.E64, v[0], v[3], row_height64(A.ylo, A.dy[lvl], j), pv, tv);
           V.at(5, i, j) = pv;
           V.at(6, i, j) = tv;
         }
@@ -1677,6 +1903,7 @@ struct Engine {
   bool f32s = false;
   size_t esize = 8;
   double* d_env[kL][4] = {};  // absorbing-envelope tables (null: side not ABSORB)
+  int env_act[kL][4] = {};    // AbsorbTables::act
   double regrid_ms[5] = {0, 0, 0, 0, 0};  // host wall time of enl_engine_regrid phases
   void* stage_host = nullptr;  // pinned staging of the tables
   size_t stage_cap = 0;
@@ -1953,7 +2180,8 @@ static EosConst32 eos_const32(const enl_engine_config& c) {
 }
 
 static EosConst64 eos_const64(const enl_engine_config& c) {
-  return EosConst64{c.rho0, c.c, c.c_lr, (c.gamma1 - 1.0) / (2.0 * c.rho0), c.c_p, c.p0, c.T0, c.c_v, c.R};
+  return EosConst64{c.rho0, c.c, c.c_lr, (c.gamma1 - 1.0) / (2.0 * c.rho0), c.c_p, c.p0, c.T0, c.c_v, c.R,
+                    1.0 / c.c_p, 1.0 / c.c_v};
 }
 
 static StageArgs stage_args(Engine* E, int stage, double dt) {
@@ -2012,6 +2240,8 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.gm1_over_2rho0 = (c.gamma1 - 1.0) / (2.0 * c.rho0);
   A.c_p = c.c_p;
   A.c_v = c.c_v;
+  A.uniform = (!c.dense && c.c_lr == 0.0) ? 1 : 0;
+  A.finest_first = c.tile_order == 0 ? 1 : 0;
   A.R = c.R;
   A.ylo = c.xlo[1];
   A.un_is_in = in == 0 ? 1 : 0;
@@ -2020,6 +2250,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.bdt = c.rk_beta[stage] * dt;
   A.beta = c.rk_beta[stage];
   A.E32 = eos_const32(c);
+  A.E64 = eos_const64(c);
   A.dt_dev = E->adaptive ? E->d_dt : nullptr;
   A.dtf_dev = E->adaptive ? reinterpret_cast<const float*>(E->d_dt + 2) : nullptr;
   A.a1f = (float)A.a1;
@@ -2034,7 +2265,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.counter = E->d_counters + stage;
   A.health = E->d_health;
   A.stats = E->d_stats;
-  A.mlp = (E->cfg.learned && E->cfg.precision != ENL_PREC_FP64) ? E->d_mlp : nullptr;  // null until set_mlp
+  A.mlp = E->cfg.learned ? E->d_mlp : nullptr;  // null until set_mlp
   A.margin = E->margin;
   A.feat_eps = (float)A.P[0].sensor_eps;
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
@@ -2109,6 +2340,7 @@ static AbsorbTables absorb_tables(const Engine* E) {
       T.env[l][d] = E->d_env[l][d];
       T.envf[l][d] = E->d_envf[l][d];
       T.cont[l][d] = E->d_cont[l][d];
+      T.act[l][d] = E->env_act[l][d];
     }
   return T;
 }
@@ -2137,6 +2369,14 @@ static int build_absorb_tables(Engine* E) {
         hf[q] = (float)h[q];
         hc[q] = std::fabs(1.0 - h[q]) > 1.0e-8 ? 1 : 0;  // the reference's loop test
       }
+      // cells from the side inwards up to the last factor that is not exactly 1
+      int act = (d == 0 || d == 2) ? 0 : n[d];
+      for (int q = 0; q < n[d]; ++q)
+        if (h[q] != 1.0) {
+          if (d == 0 || d == 2) act = std::max(act, q + 1);
+          else act = std::min(act, q);
+        }
+      E->env_act[l][d] = act;
       if (cudaMalloc(&E->d_env[l][d], n[d] * sizeof(double)) != cudaSuccess ||
           cudaMalloc(&E->d_envf[l][d], n[d] * sizeof(float)) != cudaSuccess ||
           cudaMalloc(&E->d_cont[l][d], n[d]) != cudaSuccess)
@@ -2374,6 +2614,7 @@ extern "C" {
 int enl_engine_create(const enl_engine_config* cfg, void** out) {
   if (!cfg || !out || cfg->nlevels < 1 || cfg->nlevels > kL || cfg->ratio < 2 || cfg->nx0 < 8 || cfg->ny0 < 8 ||
       cfg->variant < 0 || cfg->variant > 8 || cfg->precision < ENL_PREC_FP64 || cfg->precision > ENL_PREC_FP32_STATE ||
+      cfg->tile_order < 0 || cfg->tile_order > 1 ||
       (cfg->independent && (cfg->nlevels != 1 || cfg->bc[0] == kAbsorb || cfg->bc[1] == kAbsorb ||
                             cfg->bc[2] == kAbsorb || cfg->bc[3] == kAbsorb))) {
     set_error(ENL_ERR_ARG);
@@ -2434,14 +2675,14 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMalloc(&E->d_counters, 4 * sizeof(int));
   cudaMalloc(&E->d_health, sizeof(int));
   cudaMemset(E->d_health, 0, sizeof(int));
-  cudaMalloc(&E->d_stats, 3 * kL * sizeof(unsigned long long));
-  cudaMemset(E->d_stats, 0, 3 * kL * sizeof(unsigned long long));
+  cudaMalloc(&E->d_stats, 4 * kL * sizeof(unsigned long long));
+  cudaMemset(E->d_stats, 0, 4 * kL * sizeof(unsigned long long));
   cudaMalloc(&E->d_dt, 3 * sizeof(double));  // dt, simulated time, dt as float
   cudaMemset(E->d_dt, 0, 3 * sizeof(double));
   cudaMalloc(&E->d_smax, sizeof(unsigned long long));
   cudaMemset(E->d_smax, 0, sizeof(unsigned long long));
   if (E->f32s) E->smem_bytes = kSmemFast32;
-  else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kSmemFast64 : 2 * kStageBufBytes;
+  else E->smem_bytes = cfg->precision == ENL_PREC_FP32 ? kSmemFast64 : kSmem64;
   // (the learned switch keeps its features in the planes' place: no more)
   StageFn fn = pick_stage(cfg->precision, cfg->variant);
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
@@ -2755,10 +2996,10 @@ int enl_engine_tag(void* e, int level, int* tags) {
 int enl_engine_stats(void* e, long long* counts) {
   Engine* E = (Engine*)e;
   if (!E || !counts) return ENL_ERR_ARG;
-  unsigned long long h[3 * kL];
+  unsigned long long h[4 * kL];
   cudaMemcpyAsync(h, E->d_stats, sizeof(h), cudaMemcpyDeviceToHost, stream());
   cudaStreamSynchronize(stream());
-  for (int q = 0; q < 3 * kL; ++q) counts[q] = (long long)h[q];
+  for (int q = 0; q < 4 * kL; ++q) counts[q] = (long long)h[q];
   cudaMemsetAsync(E->d_stats, 0, sizeof(h), stream());
   return check_launch("engine stats");
 }
@@ -3501,7 +3742,7 @@ int enl_engine_set_mlp(void* e, const float* params_host, float margin) {
     set_error(ENL_ERR_ARG);
     return ENL_ERR_ARG;
   }
-  if (!(E->cfg.precision != ENL_PREC_FP64 && E->cfg.learned)) {
+  if (!E->cfg.learned) {
     set_error(ENL_ERR_STATE);
     return ENL_ERR_STATE;
   }

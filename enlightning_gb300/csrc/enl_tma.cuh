@@ -54,6 +54,27 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait on an mbarrier phase for at most max_ns nanoseconds of wall time:
+// false when the phase has not completed by then (a copy that never lands
+// becomes an error status within that time, whatever try_wait's own
+// suspension interval is).
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t* bar, uint32_t parity, unsigned long long max_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (int it = 0; it < (1 << 26); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > max_ns) return false;
+  }
+  return false;
+}
+
 // 3-D tiled TMA load global -> shared, completion signalled on an mbarrier.
 // c0 (innermost) must be a multiple of 2 for 8-byte elements (16-byte rule).
 __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, int c0, int c1, int c2,

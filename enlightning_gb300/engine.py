@@ -42,7 +42,7 @@ class Engine:
 
     def __init__(self, params: dict, nx0: int, ny0: int, dx0, nlevels=1, ratio=2, xlo=(0.0, 0.0),
                  bc=(REFLECT,) * 4, variant="hybrid_high_llf", precision=PREC_FP64, learned=False,
-                 independent=False):
+                 independent=False, dense=False, tile_order=0):
         self.L = _lib.lib()
         p = params
         cfg = EngineConfig()
@@ -61,11 +61,13 @@ class Engine:
         cfg.rk_alpha2[:] = list(RK3_ALPHA2)
         cfg.rk_beta[:] = list(RK3_BETA)
         cfg.independent = int(bool(independent))
+        cfg.dense = int(bool(dense))
+        cfg.tile_order = int(tile_order)
         self.cfg = cfg
         self.params = dict(p)
         self._init_args = dict(nx0=nx0, ny0=ny0, dx0=tuple(dx0), nlevels=nlevels, ratio=ratio, xlo=tuple(xlo),
                                bc=tuple(bc), variant=variant, precision=int(precision), learned=bool(learned),
-                               independent=bool(independent))
+                               independent=bool(independent), dense=bool(dense), tile_order=int(tile_order))
         self.nlevels, self.ratio = nlevels, ratio
         self.dx0 = tuple(dx0)
         self.xlo = tuple(xlo)
@@ -153,10 +155,11 @@ class Engine:
         return int(self.L.enl_engine_launches_per_step(self.h, int(plain)))
 
     def stats(self):
-        """Per level: [WENO cells, cells, cells decided by the plain fallback] since the last call."""
-        arr = (C.c_longlong * (3 * MAX_LEVELS))()
+        """Per level: [WENO cells, cells, cells decided by the plain fallback, cells of uniform
+        tiles stored from the cache] since the last call."""
+        arr = (C.c_longlong * (4 * MAX_LEVELS))()
         _lib.check(self.L.enl_engine_stats(self.h, arr), "enl_engine_stats")
-        a = np.array(arr[:], dtype=np.int64).reshape(MAX_LEVELS, 3)
+        a = np.array(arr[:], dtype=np.int64).reshape(MAX_LEVELS, 4)
         return a[: self.nlevels]
 
     def health(self):
@@ -169,7 +172,7 @@ class Engine:
         return tags
 
     def set_mlp(self, params, margin):
-        """Install the learned switch (FP32 parameter vector) in a learned FP32 engine."""
+        """Install the learned switch (FP32 parameter vector) in an engine created with learned=True."""
         P = np.ascontiguousarray(np.asarray(params, np.float32))
         _lib.check(self.L.enl_engine_set_mlp(self.h, P.ctypes.data_as(C.c_void_p), float(margin)),
                    "enl_engine_set_mlp")

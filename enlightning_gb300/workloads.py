@@ -100,7 +100,7 @@ def gaussian_spread(sigma):
 
 def line_source(prm, nx0=4096, ny0=2048, dx0=0.5, nlevels=3, seed=100, nseg=200, precision=1,
                 variant="hybrid_high_llf", learned=False, base_patch=256, cfl=0.5, amp_frac=10.0,
-                sigma_cells=2.0, min_size=16, max_size=256, native_regrid=True):
+                sigma_cells=2.0, min_size=16, max_size=256, native_regrid=True, dense=False, tile_order=0):
     """Thunder-like line source on a multi-level hierarchy (synthetic).
 
     A seeded random-walk channel of `nseg` segments (lengths U(1, 3) m, turns
@@ -121,7 +121,7 @@ def line_source(prm, nx0=4096, ny0=2048, dx0=0.5, nlevels=3, seed=100, nseg=200,
     Hh = ny0 * dx0
     segs = random_walk_channel(rng, nseg=nseg, start=(0.5 * L, 0.85 * Hh), heading_deg=-90.0)
     E = Engine(prm, nx0, ny0, (dx0, dx0), nlevels=nlevels, ratio=2, bc=(ABSORB, ABSORB, REFLECT, ABSORB),
-               variant=variant, precision=precision, learned=learned)
+               variant=variant, precision=precision, learned=learned, dense=dense, tile_order=tile_order)
     E.set_adaptive_dt(True, cfl)
     Hy = Hierarchy(E, min_size=min_size, max_size=max_size, tag_buffer=2, native=native_regrid)
     Hy.base_patches(base_patch)
@@ -150,7 +150,7 @@ def eos_state(rho, u, v, p, prm):
 
 
 def mach_shock(prm, seed=0, nx0=1024, ny0=512, dx0=0.1, nlevels=2, mach=1.5, precision=1, learned=False,
-               variant="hybrid_high_llf", base_patch=128, cfl=0.5, min_size=32, max_size=128):
+               variant="hybrid_high_llf", base_patch=128, cfl=0.5, min_size=32, max_size=128, dense=False, tile_order=0):
     """Planar shock moving +x into ambient air with 1 % i.i.d. density noise.
 
     Post-shock state from the ideal-gas Rankine-Hugoniot relations at
@@ -166,7 +166,7 @@ def mach_shock(prm, seed=0, nx0=1024, ny0=512, dx0=0.1, nlevels=2, mach=1.5, pre
     p = dict(prm)
     p["bc_absorb_width"] = 1e-9
     E = Engine(p, nx0, ny0, (dx0, dx0), nlevels=nlevels, ratio=2, bc=(ABSORB, ABSORB, REFLECT, REFLECT),
-               variant=variant, precision=precision, learned=learned)
+               variant=variant, precision=precision, learned=learned, dense=dense, tile_order=tile_order)
     E.set_adaptive_dt(True, cfl)
     Hy = Hierarchy(E, min_size=min_size, max_size=max_size, tag_buffer=2)
     Hy.base_patches(base_patch)
@@ -205,7 +205,7 @@ def shelf_pack(sides, width, gap=8):
 
 
 def pulse_batch(prm, seed=7, n=64, side_range=(128, 1024), precision=1, learned=False, variant="hybrid_high_llf",
-                width=8192, dx=0.1):
+                width=8192, dx=0.1, dense=False, tile_order=0):
     """Batched independent pulse problems: n square patches with sides drawn
     uniformly from multiples of 32 in side_range, Gaussian overpressure
     U(0.01, 0.5) p0 with sigma U(4, 16) cells at each centre, reflective
@@ -221,7 +221,7 @@ def pulse_batch(prm, seed=7, n=64, side_range=(128, 1024), precision=1, learned=
     pos, height = shelf_pack(sides, width)
     height = int(-(-height // 8) * 8)
     E = Engine(prm, width, height, (dx, dx), nlevels=1, bc=(REFLECT,) * 4, variant=variant, precision=precision,
-               learned=learned, independent=True)
+               learned=learned, independent=True, dense=dense, tile_order=tile_order)
     boxes = [(x, x + s - 1, y, y + s - 1) for (x, y), s in zip(pos, sides)]
     E.set_patches(0, boxes)
     k = (prm["gamma1"] - 1.0) / (2.0 * prm["rho0"])

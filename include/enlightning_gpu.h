@@ -190,7 +190,7 @@ typedef struct {
   int bc[4];              /* L, R, B, T: 10 = REFLECT, 20 = ABSORB           */
   int variant;            /* ENL_* scheme id                                 */
   int precision;          /* ENL_PREC_FP64, ENL_PREC_FP32, ENL_PREC_FP32_STATE */
-  int learned;            /* 1: learned switch on level 0 (FP32 modes only)  */
+  int learned;            /* 1: learned switch on level 0                    */
   double weno_alpha, kappa, mu, muB, R, T_star_n, tau_n, c, c_lr;
   double tol[3];
   double rho0, gamma1, c_p, p0, T0, c_v;
@@ -200,6 +200,19 @@ typedef struct {
                              sides are physical boundaries (batched independent
                              problems; nlevels must be 1, patches >= 6 cells
                              apart on the canvas)                         */
+  int dense;              /* 0 (default): a stage tile whose staged inputs are
+                             bitwise uniform (one value per field over the
+                             halo box, shared u^n and H0, no absorbing band,
+                             c_lr = 0) stores the outputs the block computed
+                             for an earlier tile with the same inputs, which
+                             are the outputs every one of its cells would
+                             compute; 1: every tile is computed cell by cell.
+                             The states are identical either way.          */
+  int tile_order;         /* order in which the stage kernel's blocks claim
+                             tiles: 0 (default) finest level first (the WENO
+                             tiles of the fine levels start first and the
+                             cheaper coarse tiles balance the end), 1 level 0
+                             first.  Either order gives the same states.   */
 } enl_engine_config;
 
 /* Create / destroy.  Allocates the canvases of every level (device memory). */
@@ -246,8 +259,9 @@ int enl_engine_graph_valid(void* engine);
  * the patches are 0.  Fills ghosts of the current buffer and H0 first. */
 int enl_engine_tag(void* engine, int level, int* tags);
 /* Counters of the last steps: per level, cells advanced with WENO, cells in
- * total, and cells the learned switch left to the plain switch (host array of
- * 3*ENL_MAX_LEVELS long long), then reset. */
+ * total, cells the learned switch left to the plain switch, and cells of
+ * uniform tiles whose outputs came from the block's cache (host array of
+ * 4*ENL_MAX_LEVELS long long), then reset. */
 int enl_engine_stats(void* engine, long long* counts);
 /* Health word: 0, or the first code a kernel raised since the last call:
  * ENL_ERR_NONFINITE (rho <= 0 or non-finite state), ENL_ERR_TIMEOUT (a
@@ -327,7 +341,7 @@ int enl_mlp_adam(float* params, const float* grad, float* m, float* v,
                  float lr, float beta1, float beta2, float eps, float inv_n,
                  int step);
 /* Install the network (host FP32 vector) in an engine created with
- * precision ENL_PREC_FP32 or ENL_PREC_FP32_STATE and learned = 1. */
+ * learned = 1 (any precision). */
 int enl_engine_set_mlp(void* engine, const float* params_host, float margin);
 /* Harvest training rows from a level of the engine (plain FP64 arithmetic):
  * features (device BF16 [capacity][40]), labels (device float [capacity][2]
