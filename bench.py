@@ -325,10 +325,11 @@ class LineSource:
             self.steps_done[which] += 1
         return done
 
-    def compare(self):
-        """rel-L2 of the fast arm against the plain FP64 arm on level 0 (composite)."""
-        a = self.fast.level_state(0).cpu().numpy()
-        b = self.plain.level_state(0).cpu().numpy()
+    def compare(self, a_engine=None, b_engine=None):
+        """rel-L2 of the fast arm (or a_engine) against the plain FP64 arm (or
+        b_engine) on level 0 (composite)."""
+        a = (a_engine or self.fast).level_state(0).cpu().numpy()
+        b = (b_engine or self.plain).level_state(0).cpu().numpy()
         p = self.prm
         out = {}
         names = ["rho", "rho_u", "rho_v", "rho_s", "rho_Tn", "p", "T"]
@@ -419,9 +420,9 @@ class PulseBatch(LineSource):
         self.graph_ok = False
         self.dt_cap = self.info["dt"]
 
-    def compare(self):
-        a = self.fast.level_state(0).cpu().numpy()
-        b = self.plain.level_state(0).cpu().numpy()
+    def compare(self, a_engine=None, b_engine=None):
+        a = (a_engine or self.fast).level_state(0).cpu().numpy()
+        b = (b_engine or self.plain).level_state(0).cpu().numpy()
         m = np.zeros(a.shape[1:], bool)
         for bx in self.boxes:
             m[bx[2]:bx[3] + 1, bx[0]:bx[1] + 1] = True
@@ -562,10 +563,13 @@ def linesource_cpu_sample(seed=100, patch=128):
     return prm, out
 
 
-def run_reference_linesource(args):
+def linesource_reference_rate(steps, warmup, threads):
+    """The reference's CPU path (the oracle's restated Fortran) on the
+    line-source sample, one RK3 step per pass over its patches: the median
+    rate of `steps` passes after `warmup`.  The reference arm and the bench
+    line's cpu_baseline both report this measurement."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as ora
-    threads = os.cpu_count() or 1
     ora.set_threads(threads)
     prm, sample = linesource_cpu_sample()
     patches = []
@@ -586,17 +590,22 @@ def run_reference_linesource(args):
             nc += P.nx * P.ny
         return nc, time.perf_counter() - t0
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         one_pass()
     vals = []
-    for _ in range(args.steps):
+    for _ in range(max(1, steps)):
         nc, el = one_pass()
         vals.append(nc / el)
-    v = float(np.median(vals))
     cells = sum(P.nx * P.ny for P in patches)
-    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-          "sample": f"{len(patches)} patches of 128x128 ({cells} cells) of the line-source state across the 3 "
-                    f"levels' resolutions, one RK3 step per timed step"}
+    return {"value": float(np.median(vals)), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(patches)} patches of 128x128 ({cells} cells) of the line-source initial state across "
+                      f"the 3 levels' resolutions, one RK3 step per pass, median of {max(1, steps)} passes after "
+                      f"{max(1, warmup)}"}
+
+
+def run_reference_linesource(args):
+    cb = linesource_reference_rate(args.steps, args.warmup, os.cpu_count() or 1)
+    v = cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist_env()[0],
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": LineSource.name},
@@ -714,6 +723,59 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def fp_peaks():
+    """FP64 FMA (TFLOP/s), FP64 division (G/s) and FP32 FMA (TFLOP/s) rates of
+    this GPU, measured now by the library (enl_measure_fp_peaks)."""
+    import ctypes as C
+    from enlightning_gb300 import _lib
+    o = (C.c_double * 3)()
+    _lib.check(_lib.lib().enl_measure_fp_peaks(o, 3), "enl_measure_fp_peaks")
+    return {"fp64_fma_tflops": o[0], "fp64_div_per_s": o[1] * 1e9, "fp32_fma_tflops": o[2]}
+
+
+def fp64_flops_per_cell():
+    """FP64 flops (2 per FMA, 1 per add or multiply) of one dense stage-kernel
+    cell by branch, from the ncu instruction counts in profiles/."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "stage_fp64_flops.json")) as f:
+            d = json.load(f)
+        return float(d["weno_flops_per_cell"]), float(d["drp_flops_per_cell"])
+    except Exception:
+        return None, None
+
+
+def stage_timing(wl, which="fast", steps=3):
+    """Stage-kernel launches of `steps` direct steps timed with CUDA events on
+    the engine's stream: (ms per launch, cells per launch, counters)."""
+    E = wl.fast if which == "fast" else wl.plain
+    E.stats()
+    E.profile(True)
+    wl.advance(which, steps, use_graph=False)
+    kms, kl, kcells = E.profile(False)
+    st = E.stats()
+    return kms / max(1, kl), kcells / max(1, kl), st, max(1, kl)
+
+
+def run_stats_only(args):
+    """`args.steps` direct steps of the batched engine (no timing, no other
+    arm), then the engine's counters summed over those steps: the companion
+    of an ncu capture of the same command (FP64 instruction counts per cell
+    in profiles/)."""
+    import torch
+    torch.cuda.set_device(0)
+    torch.cuda.set_stream(torch.cuda.Stream())
+    wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=False,
+                                  precision=args.precision, dense=args.dense, tile_order=args.tile_order)
+    wl.fast.stats()
+    wl.advance("fast", args.steps, use_graph=False)
+    torch.cuda.synchronize()
+    st = wl.fast.stats()
+    print(json.dumps({"workload": wl.name, "precision": PREC_NAMES[args.precision], "dense": bool(args.dense),
+                      "steps": args.steps, "stage_launches": 3 * args.steps,
+                      "weno_cells": int(st[:, 0].sum()), "cells": int(st[:, 1].sum()),
+                      "uniform_cells": int(st[:, 3].sum())}), flush=True)
+
+
 def run_linesource(args):
     import torch
     ws, rank, local = dist_env()
@@ -727,11 +789,18 @@ def run_linesource(args):
     torch.cuda.set_stream(torch.cuda.Stream())
     hbm_peak, peak_kind = peaks()
     t_build = time.perf_counter()
-    wl = WORKLOADS[args.workload](learned=args.learned, scale=args.scale, with_plain=not args.no_plain,
-                                  precision=args.precision, dense=args.dense,
-                                  tile_order=args.tile_order)
-    if args.regrid_every is not None and wl.REGRID:
-        wl.REGRID = args.regrid_every
+    cls = WORKLOADS[args.workload]
+    wl = cls(learned=args.learned, scale=args.scale, with_plain=not args.no_plain, precision=args.precision,
+             dense=args.dense, tile_order=args.tile_order)
+    # the FP32-perturbation-storage engine on the same workload, reported beside
+    # the FP64 headline (same switch, its own error against the plain arm)
+    wl32 = None
+    if args.precision == 0 and not args.no_secondary:
+        wl32 = cls(learned=args.learned, scale=args.scale, with_plain=False, precision=2, dense=args.dense,
+                   tile_order=args.tile_order)
+    for w_ in (wl, wl32):
+        if w_ is not None and args.regrid_every is not None and w_.REGRID:
+            w_.REGRID = args.regrid_every
     esize = 4 if args.precision == 2 else 8
     t_build = time.perf_counter() - t_build
 
@@ -740,15 +809,21 @@ def run_linesource(args):
         if ws > 1:
             torch.distributed.barrier()
 
-    # accuracy: both arms from the same initial state, same regrid cadence
+    # accuracy: every arm from the same initial state, same regrid cadence
     ncmp = args.compare_steps
-    err = None
-    if wl.plain is not None:
+    err, err32, err32_fp64 = None, None, None
+    if wl.plain is not None or wl32 is not None:
         wl.advance("fast", ncmp, use_graph=True)
-        wl.advance("plain", ncmp)
-        barrier()
-        err = wl.compare()
-    weno = wl.fast.stats()
+        if wl32 is not None:
+            wl32.advance("fast", ncmp, use_graph=True)
+            barrier()
+            err32_fp64 = wl.compare(wl32.fast, wl.fast)
+        if wl.plain is not None:
+            wl.advance("plain", ncmp)
+            barrier()
+            err = wl.compare()
+            if wl32 is not None:
+                err32 = wl.compare(wl32.fast, wl.plain)
     # warm-up, then the timed region (graph replay, regrids included)
     wl.advance("fast", max(3, args.warmup), use_graph=True)
     barrier()
@@ -783,16 +858,47 @@ def run_linesource(args):
         p1.record()
         barrier()
         plain_value = cup / (p0.elapsed_time(p1) * 1e-3)
-    # dominant kernel: stage kernel timed with events around each launch
-    wl.fast.profile(True)
-    wl.advance("fast", 3, use_graph=False)
-    barrier()
-    kms, kl, kcells = wl.fast.profile(False)
-    per_launch_ms = kms / max(1, kl)
-    cells_per_launch = kcells / max(1, kl)
-    # 320 B per RK3 cell-update with FP64 fields; FP32 storage moves half of it
+    # dominant kernel: the stage kernel, timed with events around each launch
+    per_launch_ms, cells_per_launch, kst, nl = stage_timing(wl)
+    # 320 B per RK3 cell-update of 5 FP64 fields (106.7 B per stage launch);
+    # FP32 storage moves half of it
     bytes_per_cell_launch = STEP_BYTES_PER_CELL / 3.0 * esize / 8.0
-    achieved = cells_per_launch * bytes_per_cell_launch / (per_launch_ms * 1e-3) / 1e9
+    hbm_achieved = cells_per_launch * bytes_per_cell_launch / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
+    if os.path.exists(tf):
+        try:
+            with open(tf) as f:
+                rec = json.load(f).get(PREC_NAMES[args.precision])
+            if rec:
+                traffic = rec["dram_bytes_per_cell_launch"] * cells_per_launch
+        except Exception:
+            traffic = None
+    hbm = {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
+           "peak_kind": peak_kind, "bytes_per_cell_launch": bytes_per_cell_launch, "traffic": traffic}
+    fpk = fp_peaks()
+    roof = {"kernel": "stage_kernel (" + PREC_NAMES[args.precision] + ")", "kernel_ms": per_launch_ms,
+            "cells_per_launch": cells_per_launch}
+    if args.precision == 0:
+        f_weno, f_drp = fp64_flops_per_cell()
+        dense_cells = float(kst[:, 1].sum() - kst[:, 3].sum()) / nl
+        weno_cells = float(kst[:, 0].sum()) / nl
+        flops = None if f_weno is None else weno_cells * f_weno + max(0.0, dense_cells - weno_cells) * f_drp
+        fp64_achieved = None if flops is None else flops / (per_launch_ms * 1e-3) / 1e12
+        fp64_peak = fpk["fp64_fma_tflops"]
+        roof.update({"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": None if fp64_achieved is None else fp64_achieved / fp64_peak,
+                     "peak_kind": "measured in this run (FP64 FMA chains on every SM, enl_measure_fp_peaks)",
+                     "traffic": traffic,
+                     "flops_per_launch": flops, "dense_cells_per_launch": dense_cells,
+                     "weno_cells_per_launch": weno_cells,
+                     "flops_per_cell": {"weno": f_weno, "drp": f_drp,
+                                        "source": "profiles/stage_fp64_flops.json (ncu FP64 instruction counts)"},
+                     "hbm": hbm})
+    else:
+        roof.update({"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": hbm_achieved / hbm_peak, "peak_kind": peak_kind,
+                     "bytes_per_cell_launch": bytes_per_cell_launch, "traffic": traffic})
     # e2e: every step takes its input state (the 5 conserved fields of every
     # patch interior) from pinned host memory and returns its result state to
     # pinned host memory, through the public API; p and T are recomputed on
@@ -833,45 +939,62 @@ def run_linesource(args):
     cue = E.cells() * ke
     e2e_value = aggregate_rate(cue, ws, e2e_ms)
     nbytes = int(n * esize)
+    # the FP32-storage engine: its own timed region (graph replay, regrids)
+    secondary = None
+    if wl32 is not None:
+        wl32.advance("fast", max(3, args.warmup), use_graph=True)
+        barrier()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        cu32 = wl32.advance("fast", args.steps, use_graph=True)
+        s1.record()
+        barrier()
+        ms32 = s0.elapsed_time(s1)
+        k32, c32, _, _ = stage_timing(wl32)
+        a32 = c32 * (STEP_BYTES_PER_CELL / 6.0) / (k32 * 1e-3) / 1e9
+        secondary = {"dtype": "f32 (perturbation state and rhs)", "value": aggregate_rate(cu32, ws, ms32),
+                     "ms_per_step": ms32 / args.steps,
+                     "rel_l2_vs_plain_fp64": err32, "rel_l2_vs_fp64_same_switch": err32_fp64,
+                     "compare_steps": ncmp, "stage_kernel_ms": k32,
+                     "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm_peak, "unit": "GB/s",
+                                  "frac": a32 / hbm_peak, "bytes_per_cell_launch": STEP_BYTES_PER_CELL / 6.0}}
     if rank != 0:
         return
     health = wl.fast.health()
-    cb = cpu_baseline_with_single_core(wl) if not args.no_cpu_baseline else None
-    # DRAM bytes of one stage launch from an ncu capture, per cell, scaled to
-    # this workload's launch (the capture ran a smaller case of the same kernel)
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "stage_traffic.json")
-    if os.path.exists(tf):
-        try:
-            with open(tf) as f:
-                rec = json.load(f).get(PREC_NAMES[args.precision])
-            if rec:
-                traffic = rec["dram_bytes_per_cell_launch"] * cells_per_launch
-        except Exception:
-            traffic = None
+    cb = None
+    if not args.no_cpu_baseline:
+        if args.workload == "linesource":
+            cb = linesource_reference_rate(args.steps, args.warmup, os.cpu_count() or 1)
+            one = linesource_reference_rate(max(2, args.steps // 4), 1, 1)
+            cb["value_1core"] = one["value"]
+            cb["sample_1core"] = one["sample"]
+            cb["cpu_model"] = host_cpu_model()
+        else:
+            cb = cpu_baseline_with_single_core(wl)
     dt_last, sim_t = wl.fast.time()
+    path = ("batched: persistent fused stage kernel over all levels, " + PREC_PATH[args.precision]
+            + ", CUDA graph" + (", learned sensor" if wl.learned else ", plain sensor")
+            + ("" if args.dense else ", uniform tiles reuse a block-cached cell result"))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": PREC_DTYPE[args.precision], "data": "synthetic",
-        "config": {"workload": wl.name, "path": "batched: persistent fused stage kernel over all levels, "
-                   + PREC_PATH[args.precision] + ", CUDA graph"
-                   + (", learned sensor" if wl.learned else ", plain sensor"),
+        "config": {"workload": wl.name, "path": path,
                    "cells_per_step": cu / args.steps, "patches": [len(p) for p in wl.fast.patches],
                    "l2": "inputs larger than L2 (state of every level, > 1 GB)", "regrid_every": wl.REGRID,
                    "timed_regrids": regrid_info,
                    "dt": ("device CFL reduction, cfl 0.5 on max(|u|+c)" if wl.REGRID else "cfl*dx/c (reference)"),
                    "dt_last": dt_last, "sim_time": sim_t,
                    "plain_value": plain_value, "plain_steps": kp,
+                   "plain_path": "per-patch FP64 rhs / runge_kutta / update_state launches, plain sensor",
                    "speedup_vs_plain": (value / plain_value) if plain_value else None,
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
-                   "uniform_tile_fraction": uniform_frac,
-                   "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic,
-                     "kernel": "stage_kernel (" + PREC_NAMES[args.precision] + ")",
-                     "peak_kind": peak_kind, "bytes_per_cell_launch": bytes_per_cell_launch,
-                     "kernel_ms": per_launch_ms, "cells_per_launch": cells_per_launch},
+                   "uniform_tile_fraction": uniform_frac, "tile_order": "finest level first"
+                   if args.tile_order == 0 else "level 0 first",
+                   "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "fp_peaks": fpk},
+        "fp32_state": secondary,
+        "roofline": roof,
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": ke, "ms_per_step": e2e_ms / ke,
@@ -905,12 +1028,18 @@ def main():
                     help="stage-kernel tile order: 0 finest level first, 1 level 0 first")
     ap.add_argument("--dense", action="store_true",
                     help="compute every stage tile cell by cell (no uniform-tile reuse; same states)")
-    ap.add_argument("--precision", type=int, default=2, choices=[0, 1, 2],
-                    help="engine mode: 0 FP64, 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2],
+                    help="engine mode: 0 FP64 (default), 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
+    ap.add_argument("--stats-only", action="store_true",
+                    help="run --steps direct steps of the batched engine and print its counters (profiling)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the FP32-storage engine reported beside the FP64 line")
     args = ap.parse_args()
     if args.learned < 0:  # the metric's configuration: batched + learned switch
         args.learned = int(os.path.exists(os.path.join(ROOT, "enlightning_gb300", "learned_sensor.npz")))
-    if args.impl == "reference":
+    if args.stats_only:
+        run_stats_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload in ("linesource", "pulses64"):
         run_linesource(args)
