@@ -35,7 +35,13 @@
 // produced by executing the reference's own Fortran source text with a
 // Fortran-77 subset interpreter (tests/golden/f77interp.py); this oracle is
 // checked against them bit for bit.  The C++ parts (absorb, BC fill) are
-// restated from enlightning.C without an executable pin.
+// pinned to the reference's own C++: oracle/ref_bc.py compiles the text of
+// enlightning::setAbsorbingBoundaryConditions and
+// enlightning::setPhysicalBoundaryConditions unchanged against stand-ins for
+// the SAMRAI types (oracle/samrai_stub.h), tests/golden/make_bc_golden.py
+// records its outputs, and ora_absorb / ora_phys_bc match them bit for bit.
+// SAMRAI's own boundary-box construction is restated in the stand-ins (SAMRAI
+// is not available), so that part stays unpinned.
 // ===========================================================================
 #include <cmath>
 #include <cstdint>

@@ -80,3 +80,95 @@ def test_f32_literal_switch_changes_results(golden, ora):
     finally:
         ora.set_f32_literals(True)
     assert not np.array_equal(KK, golden["smooth/KK/hybrid_high_llf/L0"])
+
+
+# ---------------------------------------------------------------------------
+# The absorbing envelope and the physical-boundary ghost fill against the
+# reference's own C++ (enlightning.C:634-1013, compiled unchanged against
+# stand-ins for the SAMRAI types by oracle/ref_bc.py; fixtures made by
+# tests/golden/make_bc_golden.py).
+# ---------------------------------------------------------------------------
+def _bc_cases():
+    import make_bc_golden
+    return make_bc_golden, make_bc_golden.cases()
+
+
+@pytest.fixture(scope="module")
+def bc_golden():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "enl_bc_golden.npz"))
+
+
+def test_absorb_and_phys_bc_bit_exact_against_reference_code(bc_golden, ora):
+    mk, cases = _bc_cases()
+    L = ora.lib()
+    named = {n for n, _, _ in mk.NAMED}
+    for name, kind, args, arrays in cases:
+        out = mk.run(L, "ora", kind, args, arrays)
+        assert mk.digest(out) == str(bc_golden[f"{name}/sha256"]), name
+        if name in named:
+            for k, a in enumerate(out):
+                assert np.array_equal(a.view(np.int64), bc_golden[f"{name}/out{k}"].view(np.int64)), (name, k)
+
+
+def test_bc_fixture_cases_exercise_the_routines(bc_golden):
+    """The named cases change what they are meant to change: the partial
+    envelope touches only some columns (the row loop's early stop and the
+    `tmp = 0` reset), the far patch is untouched, a one-sided physical patch
+    fills both of its corners."""
+    mk, cases = _bc_cases()
+    by = {n: (k, a, arr) for n, k, a, arr in cases}
+    _, args, arr = by["absorb_left_partial"]
+    g0, g1 = args[1]
+    d = bc_golden["absorb_left_partial/out1"] != arr[1]
+    cols = np.nonzero(d.any(axis=0))[0]
+    rows = np.nonzero(d.any(axis=1))[0]
+    nx = args[0][1] - args[0][0] + 1
+    ny = args[0][3] - args[0][2] + 1
+    assert cols.min() == g0 and cols.max() < g0 + nx - 1  # stops before the far side
+    assert len(rows) == ny                                 # every row restarted
+    _, args, arr = by["absorb_far_patch"]
+    assert all(np.array_equal(bc_golden[f"absorb_far_patch/out{k}"], arr[k]) for k in range(3))
+    _, args, arr = by["phys_left_only"]
+    g0, g1 = args[1]
+    out = bc_golden["phys_left_only/out1"]
+    assert not np.array_equal(out[:g1, :g0], arr[1][:g1, :g0])    # lower-left corner filled
+    assert not np.array_equal(out[-g1:, :g0], arr[1][-g1:, :g0])  # upper-left corner filled
+    assert np.array_equal(out[:g1, g0:], arr[1][:g1, g0:])        # bottom side untouched
+
+
+def test_reference_build_matches_oracle_on_fresh_cases(ora):
+    """Where the reference's routines were built here (oracle/_ref), run them
+    and the oracle on new random cases."""
+    import os
+    import ref_bc
+    if not os.path.exists(ref_bc.LIB):
+        pytest.skip("reference boundary routines not built on this machine")
+    try:
+        R = ref_bc.load()
+    except OSError as e:
+        pytest.skip(f"reference build not loadable here: {e}")
+    mk, _ = _bc_cases()
+    L = ora.lib()
+    rng = np.random.default_rng(77)
+    for k in range(200):
+        nx, ny = (int(v) for v in rng.integers(1, 24, 2))
+        g = tuple(int(v) for v in rng.integers(1, 4, 2))
+        i0, j0 = (int(v) for v in rng.integers(-8, 64, 2))
+        box = (i0, i0 + nx - 1, j0, j0 + ny - 1)
+        bc = tuple(int(v) for v in rng.choice([10, 20], 4))
+        arrays = mk._arrays(rng, nx, ny, g, True)
+        if k % 2:
+            dx = rng.uniform(0.02, 2.0, 2)
+            gxlo = rng.uniform(-5, 5, 2)
+            pxlo = gxlo + rng.uniform(0, 10, 2) * rng.integers(0, 2, 2)
+            gxhi = pxlo + dx * np.array([nx, ny]) + rng.uniform(0, 10, 2) * rng.integers(0, 2, 2)
+            args = (box, g, pxlo, dx, gxlo, gxhi, bc, float(rng.uniform(0.1, 20.0)))
+            kind, arrays = "absorb", arrays[:3]
+        else:
+            touches = tuple(int(v) for v in rng.integers(0, 2, 4))
+            fw = (int(rng.integers(0, g[0] + 1)), int(rng.integers(0, g[1] + 1)))
+            args, kind = (box, g, touches, bc, fw), "phys"
+        a = mk.run(R, "ref", kind, args, arrays)
+        b = mk.run(L, "ora", kind, args, arrays)
+        assert mk.digest(a) == mk.digest(b), (k, kind, args)
