@@ -21,6 +21,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -377,7 +378,7 @@ class LineSource:
             if el >= budget_s or steps >= 50:
                 break
         return {"value": ncell / el, "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": f"{len(sample)} patches ({ncell // steps} cells) across the 3 levels x {steps} RK3 "
+                "sample": f"{len(sample)} patches ({ncell // steps} cells) across the {E.nlevels} levels x {steps} RK3 "
                           f"steps ({el:.1f} s)"}
 
 
@@ -464,7 +465,48 @@ class PulseBatch(LineSource):
                 "sample": f"4 of the 64 problems ({ncell // steps} cells) x {steps} RK3 steps ({el:.1f} s)"}
 
 
-WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource, "pulses64": PulseBatch}
+class MachShock(LineSource):
+    """Planar Mach 1.5 shock into air with 1 % i.i.d. density noise, 1024x512
+    base grid (dx 0.1 m), 2 levels of ratio 2 by tag_cells gradient tagging,
+    patches of 32 to 128 cells, regrid every 10 steps, device CFL time step
+    (workloads.mach_shock).  The plain switch sends most noisy level-0 cells to
+    WENO: the workload on which a learned switch can save work."""
+
+    name = ("mach2L: Mach 1.5 shock into 1% density noise, 1024x512 base, dx 0.1 m, 2 levels ratio 2, "
+            "patches 32-128, hybrid_high_llf, regrid every 10 steps")
+    REGRID = 10
+
+    def __init__(self, seed=0, learned=False, scale=1, with_plain=True, precision=2, dense=False, tile_order=0):
+        import torch
+
+        from enlightning_gb300 import workloads
+        from enlightning_gb300.constants import default_params
+        from enlightning_gb300.engine import PREC_FP64
+
+        self.torch = torch
+        self.prm = default_params()
+        self.learned = learned
+        self.precision = precision
+        kw = dict(nx0=1024 // scale, ny0=512 // scale) if scale > 1 else {}
+        self.fast, self.fast_h = workloads.mach_shock(self.prm, seed=seed, precision=precision, learned=learned,
+                                                      dense=dense, tile_order=tile_order, **kw)
+        if learned:
+            from enlightning_gb300 import sensor
+            P, margin = sensor.load_weights()
+            self.fast.set_mlp(P, margin)
+        self.plain, self.plain_h = None, None
+        if with_plain:
+            self.plain, self.plain_h = workloads.mach_shock(self.prm, seed=seed, precision=PREC_FP64, **kw)
+        self.segs = None
+        self.steps_done = {"fast": 0, "plain": 0}
+        self.regrid_s = {"fast": 0.0, "plain": 0.0}
+        self.regrids = {"fast": 0, "plain": 0}
+        self.captures = 0
+        self.graph_ok = False
+        self.dt_cap = 1.0
+
+
+WORKLOADS = {"pulse512": Pulse512Plain, "linesource": LineSource, "pulses64": PulseBatch, "mach": MachShock}
 
 
 # ---------------------------------------------------------------------------
@@ -776,6 +818,25 @@ def run_stats_only(args):
                       "uniform_cells": int(st[:, 3].sum())}), flush=True)
 
 
+def tune_schedule(wl, cache):
+    """Autotune the stage kernel's schedule of a workload's fast engine
+    (cached by workload signature); returns what the bench line reports."""
+    t0 = time.perf_counter()
+    res = wl.fast.autotune(wl.dt_cap, steps=3, cache=cache)
+    wl.graph_ok = False  # a new schedule needs a new graph
+    out = {"chosen": {k: res["schedule"][k] for k in wl.fast.SCHEDULE_KEYS}, "source": res["source"],
+           "signature": res["signature"], "tune_s": time.perf_counter() - t0}
+    if res["table"]:
+        ms = sorted(res["table"], key=lambda r: r[1])
+        out["candidates"] = len(ms)
+        out["fastest_ms_per_step"] = ms[0][1]
+        out["slowest_ms_per_step"] = ms[-1][1]
+        dflt = [t for sc, t in ms if sc["tile_order"] == 0 and sc["reuse"] == 1 and sc["run"] == 1
+                and sc["blocks_per_sm"] == res["schedule"]["max_blocks_per_sm"]]
+        out["default_ms_per_step"] = dflt[0] if dflt else None
+    return out
+
+
 def run_linesource(args):
     import torch
     ws, rank, local = dist_env()
@@ -824,6 +885,14 @@ def run_linesource(args):
             err = wl.compare()
             if wl32 is not None:
                 err32 = wl.compare(wl32.fast, wl.plain)
+    # the stage kernel's schedule for this workload: stored under the
+    # workload's signature, or picked by the library's tuner (which leaves the
+    # state where it was); untimed
+    tune, tune32 = None, None
+    if not args.no_autotune:
+        tune = tune_schedule(wl, args.schedule_cache)
+        if wl32 is not None:
+            tune32 = tune_schedule(wl32, args.schedule_cache)
     # warm-up, then the timed region (graph replay, regrids included)
     wl.advance("fast", max(3, args.warmup), use_graph=True)
     barrier()
@@ -955,7 +1024,7 @@ def run_linesource(args):
         secondary = {"dtype": "f32 (perturbation state and rhs)", "value": aggregate_rate(cu32, ws, ms32),
                      "ms_per_step": ms32 / args.steps,
                      "rel_l2_vs_plain_fp64": err32, "rel_l2_vs_fp64_same_switch": err32_fp64,
-                     "compare_steps": ncmp, "stage_kernel_ms": k32,
+                     "compare_steps": ncmp, "stage_kernel_ms": k32, "schedule": tune32,
                      "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm_peak, "unit": "GB/s",
                                   "frac": a32 / hbm_peak, "bytes_per_cell_launch": STEP_BYTES_PER_CELL / 6.0}}
     if rank != 0:
@@ -989,8 +1058,7 @@ def run_linesource(args):
                    "plain_path": "per-patch FP64 rhs / runge_kutta / update_state launches, plain sensor",
                    "speedup_vs_plain": (value / plain_value) if plain_value else None,
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
-                   "uniform_tile_fraction": uniform_frac, "tile_order": "finest level first"
-                   if args.tile_order == 0 else "level 0 first",
+                   "uniform_tile_fraction": uniform_frac, "schedule": tune or wl.fast.schedule(),
                    "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "fp_peaks": fpk},
         "fp32_state": secondary,
@@ -1032,6 +1100,9 @@ def main():
                     help="engine mode: 0 FP64 (default), 1 FP32 RHS on FP64 state, 2 FP32 perturbation state")
     ap.add_argument("--stats-only", action="store_true",
                     help="run --steps direct steps of the batched engine and print its counters (profiling)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default stage-kernel schedule")
+    ap.add_argument("--schedule-cache", default=os.path.join(tempfile.gettempdir(), "enlightning_gb300_schedules.json"),
+                    help="JSON file of tuned schedules by workload signature")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the FP32-storage engine reported beside the FP64 line")
     args = ap.parse_args()
@@ -1041,7 +1112,7 @@ def main():
         run_stats_only(args)
     elif args.impl == "reference":
         run_reference(args)
-    elif args.workload in ("linesource", "pulses64"):
+    elif args.workload in ("linesource", "pulses64", "mach"):
         run_linesource(args)
     else:
         run_ours(args)

@@ -15,6 +15,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -254,6 +255,7 @@ struct StageArgs {
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
   int uniform;              // uniform tiles reuse a computed cell (c_lr == 0 and not dense)
   int finest_first;         // claim tiles from the end of the table (finest level first)
+  int chunk;                // a block claims runs of `chunk` consecutive tiles (>= 1)
   EosConst32 E32;  // FP32-storage epilogue
   EosConst64 E64;  // FP64 epilogue
   double a1, a2, bdt, beta;
@@ -487,6 +489,13 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   __shared__ S s_wl[8][6];  // per warp: u^n (5 fields) and H0 of its first cell
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ntiles = *A.ntiles;
+  // the block's next tile: the rest of its run of A.chunk consecutive tiles
+  // (neighbours in the table: the next tile to the right in a patch row),
+  // then a new run from the counter
+  auto claim_next = [&](int cur) -> int {
+    if (cur >= 0 && (cur + 1) % A.chunk != 0 && cur + 1 < ntiles) return cur + 1;
+    return atomicAdd(A.counter, A.chunk);
+  };
   auto issue = [&](int t, int b) {
     const int4 td = A.tiles[A.finest_first ? ntiles - 1 - t : t];
     s_td[b] = td;
@@ -530,7 +539,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     fence_mbar_init();
-    int t = atomicAdd(A.counter, 1);
+    int t = claim_next(-1);
     if (t < ntiles && !issue(t, 0)) t = ntiles;
     s_t[0] = t;
   }
@@ -540,7 +549,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   int t = s_t[0];
   while (t < ntiles) {
     if (tid == 0) {
-      int nt = atomicAdd(A.counter, 1);
+      int nt = claim_next(t);
       if (nt < ntiles && !issue(nt, b ^ 1)) nt = ntiles;
       s_t[b ^ 1] = nt;
     }
@@ -1898,6 +1907,12 @@ struct Engine {
   int nsm = 148;
   int stage_blocks = 0;
   size_t smem_bytes = 0;
+  // stage-kernel schedule (enl_engine_set_schedule / enl_engine_autotune):
+  // resident blocks per SM of the persistent grid (the occupancy limit by
+  // default) and the length of the tile runs a block claims
+  int max_blocks_per_sm = 1;
+  int sched_bps = 0;  // 0: max_blocks_per_sm
+  int sched_chunk = 1;
   // storage: FP64 absolute values, or FP32 perturbations about the ambient
   // state (absolute = off[k] + stored)
   bool f32s = false;
@@ -2242,6 +2257,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.c_v = c.c_v;
   A.uniform = (!c.dense && c.c_lr == 0.0) ? 1 : 0;
   A.finest_first = c.tile_order == 0 ? 1 : 0;
+  A.chunk = std::max(1, E->sched_chunk);
   A.R = c.R;
   A.ylo = c.xlo[1];
   A.un_is_in = in == 0 ? 1 : 0;
@@ -2688,7 +2704,8 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_bytes);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, 256, E->smem_bytes);
-  E->stage_blocks = E->nsm * std::max(1, per_sm);
+  E->max_blocks_per_sm = std::max(1, per_sm);
+  E->stage_blocks = E->nsm * E->max_blocks_per_sm;
   E->tile_off.assign(cfg->nlevels, 0);
   E->tile_cnt.assign(cfg->nlevels, 0);
   E->patch_off.assign(cfg->nlevels, 0);
@@ -3489,6 +3506,189 @@ int enl_engine_mic_records(void* e, void* host, long long max, long long* n, lon
   *n = take;
   if (dropped) *dropped = (long long)cnt - take;
   return check_launch("mic_records");
+}
+
+// ---------------------------------------------------------------------------
+// Stage-kernel schedule and its autotuner.  The reference balances patches
+// over MPI ranks with SAMRAI's load balancer (main.C:268-301); here all
+// patches of all levels share one persistent grid, and what decides the
+// balance is how the grid's blocks take tiles.  A schedule is
+//   [0] resident blocks per SM of the persistent grid (0: occupancy limit),
+//   [1] tile order: 0 finest level first, 1 level 0 first,
+//   [2] uniform-tile reuse: 1 on (when the configuration allows it), 0 every
+//       tile computed cell by cell (results identical either way),
+//   [3] run length: a block claims this many consecutive tiles at a time
+//       (1, 2, 4: 32x8, 64x8, 128x8 cells of a patch row per claim).
+// ---------------------------------------------------------------------------
+static int apply_schedule(Engine* E, const int* v) {
+  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 1 || v[2] < 0 || v[2] > 1 || v[3] < 1 ||
+      v[3] > 16)
+    return ENL_ERR_ARG;
+  E->sched_bps = v[0];
+  E->cfg.tile_order = v[1];
+  E->cfg.dense = v[2] ? 0 : 1;
+  E->sched_chunk = v[3];
+  E->stage_blocks = E->nsm * (v[0] ? v[0] : E->max_blocks_per_sm);
+  E->graph_valid = false;  // grid size and kernel arguments change
+  return ENL_OK;
+}
+
+static void get_schedule(const Engine* E, int* v) {
+  v[0] = E->sched_bps ? E->sched_bps : E->max_blocks_per_sm;
+  v[1] = E->cfg.tile_order;
+  v[2] = E->cfg.dense ? 0 : 1;
+  v[3] = E->sched_chunk;
+}
+
+int enl_engine_set_schedule(void* e, const int* sched, int n) {
+  Engine* E = (Engine*)e;
+  if (!E || !sched || n < 4) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  const int r = apply_schedule(E, sched);
+  if (r != ENL_OK) set_error(r);
+  return r;
+}
+
+int enl_engine_get_schedule(void* e, int* sched, int n) {
+  Engine* E = (Engine*)e;
+  if (!E || !sched || n < 5) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  get_schedule(E, sched);
+  sched[4] = E->max_blocks_per_sm;
+  return ENL_OK;
+}
+
+// Times every candidate schedule on the engine's current hierarchy and
+// state: for each, the state is put back to where it was, one step runs
+// untimed and `steps` steps are timed with CUDA events on the engine's
+// stream; the three fastest and the schedule in force are timed once more
+// and the fastest of that second round is applied.  The state (current
+// canvases of every level), time step, simulated time, statistics and health
+// word are restored afterwards, and microphones record nothing meanwhile, so
+// tuning leaves the simulation where it was.  tried (4 ints per candidate)
+// and ms (milliseconds per step, the best of the candidate's rounds) receive
+// up to `cap` candidates; *ntried their number.  Device memory for one copy
+// of the current canvases is allocated for the duration of the call.
+int enl_engine_autotune(void* e, double dt, int steps, int cap, int* tried, float* ms, int* ntried) {
+  Engine* E = (Engine*)e;
+  if (!E || steps < 1 || cap < 0 || (cap > 0 && (!tried || !ms))) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  if (E->h_tiles.empty()) {
+    set_error(ENL_ERR_STATE);
+    return ENL_ERR_STATE;
+  }
+  cudaStream_t s = stream();
+  const int nl = E->cfg.nlevels;
+  // snapshot
+  std::vector<void*> snap(nl, nullptr);
+  size_t extra = 3 * sizeof(double) + 4 * kL * sizeof(unsigned long long) + sizeof(int);
+  void* snap_misc = nullptr;
+  bool ok = cudaMalloc(&snap_misc, extra) == cudaSuccess;
+  for (int l = 0; ok && l < nl; ++l)
+    ok = cudaMalloc(&snap[l], (size_t)kNF * E->lev[l].fstride * E->esize) == cudaSuccess;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  ok = ok && cudaEventCreate(&ev[0]) == cudaSuccess && cudaEventCreate(&ev[1]) == cudaSuccess;
+  auto release = [&]() {
+    for (void* p : snap)
+      if (p) cudaFree(p);
+    if (snap_misc) cudaFree(snap_misc);
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+  };
+  if (!ok) {
+    cudaGetLastError();
+    release();
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
+  unsigned char* misc = static_cast<unsigned char*>(snap_misc);
+  const size_t o_stats = 3 * sizeof(double), o_health = o_stats + 4 * kL * sizeof(unsigned long long);
+  auto save_restore = [&](bool save) {
+    for (int l = 0; l < nl; ++l) {
+      const size_t bytes = (size_t)kNF * E->lev[l].fstride * E->esize;
+      if (save) cudaMemcpyAsync(snap[l], E->lev[l].buf[0], bytes, cudaMemcpyDeviceToDevice, s);
+      else cudaMemcpyAsync(E->lev[l].buf[0], snap[l], bytes, cudaMemcpyDeviceToDevice, s);
+    }
+    struct {
+      void* dev;
+      size_t off, bytes;
+    } m[3] = {{E->d_dt, 0, 3 * sizeof(double)},
+              {E->d_stats, o_stats, 4 * kL * sizeof(unsigned long long)},
+              {E->d_health, o_health, sizeof(int)}};
+    for (auto& x : m) {
+      if (save) cudaMemcpyAsync(misc + x.off, x.dev, x.bytes, cudaMemcpyDeviceToDevice, s);
+      else cudaMemcpyAsync(x.dev, misc + x.off, x.bytes, cudaMemcpyDeviceToDevice, s);
+    }
+  };
+  const int nmics = E->nmics;
+  const int profile = E->profile;
+  E->nmics = 0;
+  E->profile = 0;
+  int current[4];
+  get_schedule(E, current);
+  save_restore(true);
+  // candidates: the upper half of the occupancy range, both orders, reuse on
+  // and off (when the configuration allows reuse), runs of 1, 2, 4 tiles
+  std::vector<std::array<int, 4>> cand;
+  const bool reuse_ok = E->cfg.c_lr == 0.0;
+  for (int bps = (E->max_blocks_per_sm + 1) / 2; bps <= E->max_blocks_per_sm; ++bps)
+    for (int order = 0; order <= 1; ++order)
+      for (int reuse = reuse_ok ? 1 : 0; reuse >= 0; --reuse)
+        for (int chunk : {1, 2, 4}) cand.push_back({bps, order, reuse, chunk});
+  std::vector<float> best(cand.size(), 1e30f);
+  int rc = ENL_OK;
+  auto time_one = [&](size_t k) -> float {
+    apply_schedule(E, cand[k].data());
+    save_restore(false);
+    rc = step_fused(E, dt);
+    cudaEventRecord(ev[0], s);
+    for (int q = 0; q < steps && rc == ENL_OK; ++q) rc = step_fused(E, dt);
+    cudaEventRecord(ev[1], s);
+    cudaEventSynchronize(ev[1]);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[0], ev[1]);
+    return t / steps;
+  };
+  for (size_t k = 0; k < cand.size() && rc == ENL_OK; ++k) best[k] = time_one(k);
+  if (rc == ENL_OK) {
+    // second round: the three fastest and the schedule in force
+    std::vector<size_t> idx(cand.size());
+    for (size_t k = 0; k < idx.size(); ++k) idx[k] = k;
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return best[a] < best[b]; });
+    std::vector<size_t> again(idx.begin(), idx.begin() + std::min<size_t>(3, idx.size()));
+    for (size_t k = 0; k < cand.size(); ++k)
+      if (cand[k][0] == current[0] && cand[k][1] == current[1] && cand[k][2] == current[2] &&
+          cand[k][3] == current[3] && std::find(again.begin(), again.end(), k) == again.end())
+        again.push_back(k);
+    for (size_t k : again) {
+      if (rc != ENL_OK) break;
+      best[k] = std::min(best[k], time_one(k));
+    }
+  }
+  size_t win = 0;
+  for (size_t k = 1; k < cand.size(); ++k)
+    if (best[k] < best[win]) win = k;
+  save_restore(false);
+  cudaStreamSynchronize(s);
+  E->nmics = nmics;
+  E->profile = profile;
+  if (rc == ENL_OK) apply_schedule(E, cand[win].data());
+  else apply_schedule(E, current);
+  const int n = (int)std::min<size_t>(cand.size(), (size_t)cap);
+  for (int k = 0; k < n; ++k) {
+    for (int q = 0; q < 4; ++q) tried[4 * k + q] = cand[k][q];
+    ms[k] = best[k];
+  }
+  if (ntried) *ntried = (int)cand.size();
+  release();
+  if (rc != ENL_OK) return rc;
+  return check_launch("engine autotune");
 }
 
 int enl_engine_set_adaptive_dt(void* e, int on, double cfl) {

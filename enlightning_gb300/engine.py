@@ -132,6 +132,71 @@ class Engine:
     def cells(self):
         return sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1) for lv in self.patches for b in lv)
 
+    # -- schedule and autotuner ---------------------------------------------
+    SCHEDULE_KEYS = ("blocks_per_sm", "tile_order", "reuse", "run")
+
+    def schedule(self):
+        """The stage kernel's schedule in force (enl_engine_get_schedule)."""
+        v = (C.c_int * 5)()
+        _lib.check(self.L.enl_engine_get_schedule(self.h, v, 5), "enl_engine_get_schedule")
+        out = dict(zip(self.SCHEDULE_KEYS, v[:4]))
+        out["max_blocks_per_sm"] = v[4]
+        return out
+
+    def set_schedule(self, blocks_per_sm=0, tile_order=0, reuse=1, run=1):
+        v = (C.c_int * 4)(int(blocks_per_sm), int(tile_order), int(reuse), int(run))
+        _lib.check(self.L.enl_engine_set_schedule(self.h, v, 4), "enl_engine_set_schedule")
+
+    def signature(self):
+        """Workload signature the tuned schedule is kept under: device, storage
+        precision, scheme, learned switch, and per level the patch count and
+        cell count (two significant digits)."""
+        props = torch.cuda.get_device_properties(torch.cuda.current_device())
+        parts = [props.name.replace(" ", "_"), f"sm{props.multi_processor_count}",
+                 f"p{self.cfg.precision}", f"v{self.cfg.variant}", f"l{self.cfg.learned}", f"i{self.cfg.independent}",
+                 f"clr{int(self.params.get('c_lr', 0.0) != 0.0)}"]
+        for lv, boxes in enumerate(self.patches):
+            cells = sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1) for b in boxes)
+            parts.append(f"L{lv}:{len(boxes)}:{float(f'{cells:.2g}'):.0f}")
+        return "/".join(parts)
+
+    def autotune(self, dt, steps=3, cache=None):
+        """Pick the stage kernel's schedule for this workload.
+
+        With `cache` (a JSON file path), a schedule stored under this engine's
+        signature() is applied without timing; otherwise the library's tuner
+        (enl_engine_autotune) times the candidates on the current state, which
+        it leaves unchanged, applies the fastest and, with `cache`, stores it.
+        Returns dict(schedule, signature, source "cache"|"tuned", table of
+        (schedule, ms per step) rows when tuned)."""
+        import json
+        import os
+        sig = self.signature()
+        store = {}
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                store = json.load(f)
+            if sig in store:
+                self.set_schedule(**{k: store[sig][k] for k in self.SCHEDULE_KEYS})
+                return dict(schedule=self.schedule(), signature=sig, source="cache", table=[])
+        cap = 64
+        tried = (C.c_int * (4 * cap))()
+        ms = (C.c_float * cap)()
+        n = C.c_int()
+        _lib.check(self.L.enl_engine_autotune(self.h, float(dt), int(steps), cap, tried, ms, C.byref(n)),
+                   "enl_engine_autotune")
+        table = [(dict(zip(self.SCHEDULE_KEYS, tried[4 * k:4 * k + 4])), float(ms[k])) for k in range(min(cap, n.value))]
+        sched = self.schedule()
+        if cache:
+            store[sig] = {k: sched[k] for k in self.SCHEDULE_KEYS}
+            d = os.path.dirname(os.path.abspath(cache))
+            os.makedirs(d, exist_ok=True)
+            tmp = cache + ".tmp%d" % os.getpid()
+            with open(tmp, "w") as f:
+                json.dump(store, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+        return dict(schedule=sched, signature=sig, source="tuned", table=table)
+
     # -- stepping -----------------------------------------------------------
     def fill(self, which=0):
         _lib.check(self.L.enl_engine_fill(self.h, which), "enl_engine_fill")

@@ -316,6 +316,34 @@ int enl_engine_sync(void* engine);
 int enl_engine_profile(void* engine, int on, double* ms_total,
                        long long* launches, long long* cells);
 
+/* Stage-kernel schedule.  Replaces SAMRAI's patch-to-rank load balancing
+ * (main.C:268-301): every patch of every level shares one persistent grid,
+ * and the schedule decides how its blocks take the tiles.
+ *   sched[0] resident blocks per SM (0 = the occupancy limit),
+ *   sched[1] tile order (as enl_engine_config.tile_order),
+ *   sched[2] uniform-tile reuse: 1 on, 0 off (as enl_engine_config.dense = 1),
+ *   sched[3] run length: tiles a block claims at a time (1..16; consecutive
+ *            tiles of a patch row, so 2 and 4 claim 64x8 and 128x8 cells).
+ * Every schedule gives the same states.  Setting one invalidates a captured
+ * graph.  get_schedule writes sched[0..3] (sched[0] as the actual count) and
+ * sched[4] = the occupancy limit; n is the length of the array (>= 4 to set,
+ * >= 5 to get). */
+int enl_engine_set_schedule(void* engine, const int* sched, int n);
+int enl_engine_get_schedule(void* engine, int* sched, int n);
+/* Autotuner: times candidate schedules (blocks per SM in the upper half of
+ * the occupancy range x both tile orders x reuse on/off x runs of 1, 2, 4
+ * tiles) on the current hierarchy and state, `steps` timed steps each after
+ * one untimed step, with CUDA events on the library stream; the three
+ * fastest and the schedule in force are timed again and the fastest is
+ * applied.  The current canvases, time step, simulated time, statistics and
+ * health word are restored after every candidate and at the end, and
+ * microphones record nothing meanwhile: the simulation is left where it
+ * was.  tried[4*k..4*k+3] and ms[k] (milliseconds per step, best of the
+ * candidate's rounds) receive up to cap candidates; *ntried (may be NULL)
+ * their number.  Allocates one copy of the current canvases for the call. */
+int enl_engine_autotune(void* engine, double dt, int steps, int cap, int* tried,
+                        float* ms, int* ntried);
+
 /* ---------------------------------------------------------------------- */
 /* Learned hybrid sensor                                                   */
 /* ---------------------------------------------------------------------- */
