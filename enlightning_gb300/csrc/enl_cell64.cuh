@@ -78,8 +78,8 @@ __device__ __forceinline__ int sensor_line_fast(const double r[5], double ep) {
 }
 
 // FP64 planes of a 38 x 14 halo tile (rows of kBW64 doubles): u and v at
-// every position, F_0..4 on the 8 interior rows, G_0..4 on the 32 interior
-// columns (rows of 32).
+// every position, the half fluxes F_0..4 / 2 on the 8 interior rows and
+// G_0..4 / 2 on the 32 interior columns (rows of 32).
 constexpr int kBW64 = 38, kBH64 = 14;
 constexpr int kPos64 = kBW64 * kBH64;       // 532
 constexpr int kPl64F = 8 * kBW64;           // 304
@@ -174,35 +174,65 @@ __device__ __forceinline__ void sources64(const SAcc64P& A, const RhsConst& P, d
   H[4] = (rho * P.inv_tau_n) * (Tc - T_n);
 }
 
-// WENO reconstructions with the seeded reciprocal for the weights' sum
-// (the same formulas as weno5 / weno3 of enl_physics.cuh).
+// WENO5 reconstruction (the formulas of weno5 in enl_physics.cuh) from its
+// five inputs and the squares of its three second differences tt0..tt2
+// (S0 = c,d,e; S1 = b,c,d; S2 = a,b,c), arranged for the FP64 pipe:
+//   * the weights omega_k = (d_k / q_k) / sum_j (d_j / q_j) do not change
+//     when every q_k is multiplied by the same number, so with
+//     q_k = (13/12 t_k^2 + s_k^2 / 4 + eps)^2 the routine uses 16 q_k =
+//     (13/3 t_k^2 + s_k^2 + 4 eps)^2, formed by two fused multiply-adds and
+//     a square;
+//   * omega_k f_k / 6 = P_k (d_k f_k / 6) / sum_j d_j P_j with P_k the product
+//     of the other two q: the linear weights d_k and the 1/6 go into the
+//     candidate polynomials' coefficients (compile-time constants), and the
+//     normalisation is one seeded reciprocal.
+// The result agrees with weno5 to rounding.
 template <bool PLUS>
-__device__ __forceinline__ double weno5r(double a, double b, double c, double d, double e) {
-  const double k1312 = Lit::c13_12;
-  double t0 = fma(-2.0, d, c) + e, s0 = fma(3.0, c, fma(-4.0, d, e));
-  double t1 = fma(-2.0, c, b) + d, s1 = b - d;
-  double t2 = fma(-2.0, b, a) + c, s2 = fma(-4.0, b, a) + 3.0 * c;
-  double q0 = fma(k1312, t0 * t0, 0.25 * (s0 * s0)) + Lit::weno_eps;
-  double q1 = fma(k1312, t1 * t1, 0.25 * (s1 * s1)) + Lit::weno_eps;
-  double q2 = fma(k1312, t2 * t2, 0.25 * (s2 * s2)) + Lit::weno_eps;
+__device__ __forceinline__ double weno5q(double a, double b, double c, double d, double e, double tt0, double tt1,
+                                         double tt2) {
+  constexpr double k4 = 4.0 * Lit::c13_12;        // exact
+  constexpr double eps4 = 4.0 * Lit::weno_eps;    // exact
+  const double s0 = fma(3.0, c, fma(-4.0, d, e)), s1 = b - d, s2 = fma(3.0, c, fma(-4.0, b, a));
+  double q0 = fma(k4, tt0, fma(s0, s0, eps4));
+  double q1 = fma(k4, tt1, fma(s1, s1, eps4));
+  double q2 = fma(k4, tt2, fma(s2, s2, eps4));
   q0 *= q0;
   q1 *= q1;
   q2 *= q2;
-  const double d0 = PLUS ? Lit::c0_3 : Lit::c0_1;
-  const double d2 = PLUS ? Lit::c0_1 : Lit::c0_3;
-  double n0 = d0 * (q1 * q2), n1 = Lit::c0_6 * (q0 * q2), n2 = d2 * (q0 * q1);
-  double f0, f1, f2;
+  constexpr double d0 = PLUS ? Lit::c0_3 : Lit::c0_1;
+  constexpr double d1 = Lit::c0_6;
+  constexpr double d2 = PLUS ? Lit::c0_1 : Lit::c0_3;
+  constexpr double w0 = d0 * Lit::c1_6, w1 = d1 * Lit::c1_6, w2 = d2 * Lit::c1_6;
+  const double P0 = q1 * q2, P1 = q0 * q2, P2 = q0 * q1;
+  const double den = fma(d0, P0, fma(d1, P1, d2 * P2));
+  double g0, g1, g2;  // d_k f_k / 6
   if (PLUS) {
-    f0 = fma(2.0, c, 5.0 * d) - e;
-    f1 = fma(5.0, c, -b) + 2.0 * d;
-    f2 = fma(2.0, a, -7.0 * b) + 11.0 * c;
+    g0 = fma(2.0 * w0, c, fma(5.0 * w0, d, -w0 * e));
+    g1 = fma(-w1, b, fma(5.0 * w1, c, (2.0 * w1) * d));
+    g2 = fma(2.0 * w2, a, fma(-7.0 * w2, b, (11.0 * w2) * c));
   } else {
-    f0 = fma(11.0, c, -7.0 * d) + 2.0 * e;
-    f1 = fma(2.0, b, 5.0 * c) - d;
-    f2 = fma(5.0, b, -a) + 2.0 * c;
+    g0 = fma(11.0 * w0, c, fma(-7.0 * w0, d, (2.0 * w0) * e));
+    g1 = fma(2.0 * w1, b, fma(5.0 * w1, c, -w1 * d));
+    g2 = fma(-w2, a, fma(5.0 * w2, b, (2.0 * w2) * c));
   }
-  double num = fma(n0, f0, fma(n1, f1, n2 * f2));
-  return (Lit::c1_6 * num) * rcp64((n0 + n1) + n2);
+  const double num = fma(P0, g0, fma(P1, g1, P2 * g2));
+  return num * rcp64(den);
+}
+
+// The two WENO5 reconstructions of one sign along one direction of a cell:
+// x[0..5] are the split fluxes at offsets -3..2; lo is the reconstruction
+// from x[0..4], hi from x[1..5].  The two stencils share two of their three
+// second differences and those differences' squares.
+template <bool PLUS>
+__device__ __forceinline__ void weno5_pair(const double x[6], double& lo, double& hi) {
+  double tt[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const double t = fma(-2.0, x[j + 1], x[j]) + x[j + 2];
+    tt[j] = t * t;
+  }
+  lo = weno5q<PLUS>(x[0], x[1], x[2], x[3], x[4], tt[2], tt[1], tt[0]);
+  hi = weno5q<PLUS>(x[1], x[2], x[3], x[4], x[5], tt[3], tt[2], tt[1]);
 }
 
 template <bool PLUS>
@@ -221,27 +251,31 @@ __device__ __forceinline__ double weno3r(double b, double c, double d) {
 
 // LLF-split WENO derivative of field k plus its source hk (out of line: one
 // copy of the code for the five fields).
+// The planes hold half fluxes F/2, G/2, and ha, hb are half the split
+// speeds: fma(ha, w, F/2) is 0.5 fma(af, w, F) exactly (halving is exact),
+// one multiplication fewer per split flux.
 template <int ORDER>
-__device__ __noinline__ double weno_field64(const SAcc64P A, const RhsConst& P, int k, double af, double ag,
+__device__ __noinline__ double weno_field64(const SAcc64P A, const RhsConst& P, int k, double ha, double hb,
                                             double hk) {
   double fp[7], fm[7], gp[7], gm[7];
 #pragma unroll
   for (int q = 0; q < 7; ++q) {
     const double wx = A.w(k, q - 3, 0), wy = A.w(k, 0, q - 3);
-    const double F = A.fx(k, q - 3), G = A.gy(k, q - 3);
-    fp[q] = 0.5 * fma(af, wx, F);
-    fm[q] = 0.5 * fma(-af, wx, F);
-    gp[q] = 0.5 * fma(ag, wy, G);
-    gm[q] = 0.5 * fma(-ag, wy, G);
+    const double Fh = A.fx(k, q - 3), Gh = A.gy(k, q - 3);
+    fp[q] = fma(ha, wx, Fh);
+    fm[q] = fma(-ha, wx, Fh);
+    gp[q] = fma(hb, wy, Gh);
+    gm[q] = fma(-hb, wy, Gh);
   }
   double dfx, dgy;
   if (ORDER == 5) {
-    dfx = ((weno5r<true>(fp[0], fp[1], fp[2], fp[3], fp[4]) + weno5r<false>(fm[1], fm[2], fm[3], fm[4], fm[5])) -
-           weno5r<true>(fp[1], fp[2], fp[3], fp[4], fp[5])) -
-          weno5r<false>(fm[2], fm[3], fm[4], fm[5], fm[6]);
-    dgy = ((weno5r<true>(gp[0], gp[1], gp[2], gp[3], gp[4]) + weno5r<false>(gm[1], gm[2], gm[3], gm[4], gm[5])) -
-           weno5r<true>(gp[1], gp[2], gp[3], gp[4], gp[5])) -
-          weno5r<false>(gm[2], gm[3], gm[4], gm[5], gm[6]);
+    double fpl, fph, fml, fmh, gpl, gph, gml, gmh;
+    weno5_pair<true>(fp, fpl, fph);
+    weno5_pair<false>(fm + 1, fml, fmh);
+    weno5_pair<true>(gp, gpl, gph);
+    weno5_pair<false>(gm + 1, gml, gmh);
+    dfx = ((fpl + fml) - fph) - fmh;
+    dgy = ((gpl + gml) - gph) - gmh;
   } else {
     dfx = ((weno3r<true>(fp[1], fp[2], fp[3]) + weno3r<false>(fm[2], fm[3], fm[4])) -
            weno3r<true>(fp[2], fp[3], fp[4])) -
@@ -261,10 +295,11 @@ __device__ __forceinline__ void fluxes64(const SAcc64P& A, const RhsConst& P, in
     // Tam-Webb DRP, rhs_hybrid_high_llf.m4:258-268
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
+      // half fluxes in the planes: the coefficients are doubled (exactly)
       double fx = 0.0, gy = 0.0;
 #pragma unroll
       for (int m = 3; m >= 1; --m) {
-        const double a = m == 1 ? Lit::a1 : (m == 2 ? Lit::a2 : Lit::a3);
+        const double a = 2.0 * (m == 1 ? Lit::a1 : (m == 2 ? Lit::a2 : Lit::a3));
         fx = fma(a, A.fx(k, m) - A.fx(k, -m), fx);
         gy = fma(a, A.gy(k, m) - A.gy(k, -m), gy);
       }
@@ -279,23 +314,34 @@ __device__ __forceinline__ void fluxes64(const SAcc64P& A, const RhsConst& P, in
     double mx = 0.0;
 #pragma unroll
     for (int q = -qr; q <= qr; ++q) mx = fmax(mx, fabs(A.u(q, 0)));
-    const double hrow = P.ylo + P.dy * ((double)cj + 0.5);
-    af = (mx + P.c) + P.c_lr * hrow;
-    ag = 0.0;
+    if (P.c_lr == 0.0) {
+      // (x + c) + 0 h is x + c, and x + c rounds monotonically in x: the
+      // maximum of the sums is the sum with the maximum (same doubles)
+      af = mx + P.c;
+      double mv = 0.0;
 #pragma unroll
-    for (int q = -qr; q <= qr; ++q) {
-      const double h = P.ylo + P.dy * ((double)(cj + q) + 0.5);
-      ag = fmax(ag, (fabs(A.v(0, q)) + P.c) + P.c_lr * h);
+      for (int q = -qr; q <= qr; ++q) mv = fmax(mv, fabs(A.v(0, q)));
+      ag = mv + P.c;
+    } else {
+      const double hrow = P.ylo + P.dy * ((double)cj + 0.5);
+      af = (mx + P.c) + P.c_lr * hrow;
+      ag = 0.0;
+#pragma unroll
+      for (int q = -qr; q <= qr; ++q) {
+        const double h = P.ylo + P.dy * ((double)(cj + q) + 0.5);
+        ag = fmax(ag, (fabs(A.v(0, q)) + P.c) + P.c_lr * h);
+      }
     }
   } else {
     af = P.alpha;
     ag = P.alpha;
   }
-  KK[0] = weno_field64<ORDER>(A, P, 0, af, ag, H[0]);
-  KK[1] = weno_field64<ORDER>(A, P, 1, af, ag, H[1]);
-  KK[2] = weno_field64<ORDER>(A, P, 2, af, ag, H[2]);
-  KK[3] = weno_field64<ORDER>(A, P, 3, af, ag, H[3]);
-  KK[4] = weno_field64<ORDER>(A, P, 4, af, ag, H[4]);
+  const double ha = 0.5 * af, hb = 0.5 * ag;
+  KK[0] = weno_field64<ORDER>(A, P, 0, ha, hb, H[0]);
+  KK[1] = weno_field64<ORDER>(A, P, 1, ha, hb, H[1]);
+  KK[2] = weno_field64<ORDER>(A, P, 2, ha, hb, H[2]);
+  KK[3] = weno_field64<ORDER>(A, P, 3, ha, hb, H[3]);
+  KK[4] = weno_field64<ORDER>(A, P, 4, ha, hb, H[4]);
 }
 
 // Accessor of the learned switch's features on an FP64 tile: density and

@@ -254,7 +254,8 @@ struct StageArgs {
   FastConst F[kL];
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
   int uniform;              // uniform tiles reuse a computed cell (c_lr == 0 and not dense)
-  int finest_first;         // claim tiles from the end of the table (finest level first)
+  int tile_order;           // 0 finest level first (table from its end), 1 level 0
+                            // first, 2 the two ends alternately
   int chunk;                // a block claims runs of `chunk` consecutive tiles (>= 1)
   EosConst32 E32;  // FP32-storage epilogue
   EosConst64 E64;  // FP64 epilogue
@@ -497,7 +498,13 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     return atomicAdd(A.counter, A.chunk);
   };
   auto issue = [&](int t, int b) {
-    const int4 td = A.tiles[A.finest_first ? ntiles - 1 - t : t];
+    // claim order -> table index (the table runs level 0 to the finest);
+    // order 2 takes the two ends alternately, so that fine-level WENO tiles
+    // (FP64-bound) and level-0 tiles (memory-bound) run side by side
+    const int ti = A.tile_order == 1 ? t
+                   : A.tile_order == 2 ? ((t & 1) ? (t >> 1) : ntiles - 1 - (t >> 1))
+                                       : ntiles - 1 - t;
+    const int4 td = A.tiles[ti];
     s_td[b] = td;
     // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
     // doubles, a multiple of 4 for floats; set_patches only accepts such
@@ -670,25 +677,29 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
             }
           }
         } else {
-          // FP64: one seeded reciprocal of rho per halo position
+          // FP64: one seeded reciprocal of rho per halo position; the flux
+          // planes hold half fluxes, formed from u/2, v/2 and p/2 (halving
+          // is exact, so each is F/2 or G/2 of the same double)
           for (int e = 255 - tid; e < kPos64; e += 256) {
             const int row = e / kBW64, col = e - row * kBW64;
             const double ir = rcp64(tile[e]);
             const double u = tile[kPos64 + e] * ir, v = tile[2 * kPos64 + e] * ir;
-            const double pp = tile[5 * kPos64 + e];
+            const double hp = 0.5 * tile[5 * kPos64 + e];
             planes64[e] = u;
             planes64[kPl64OffV + e] = v;
             if (row >= 3 && row < 3 + kTH) {
+              const double hu = 0.5 * u;
 #pragma unroll
               for (int k = 0; k < 5; ++k)
                 planes64[kPl64OffF + k * kPl64F + (row - 3) * kBW64 + col] =
-                    k == 1 ? fma(u, tile[kPos64 + e], pp) : u * tile[k * kPos64 + e];
+                    k == 1 ? fma(hu, tile[kPos64 + e], hp) : hu * tile[k * kPos64 + e];
             }
             if (col >= 3 && col < 3 + kTW) {
+              const double hv = 0.5 * v;
 #pragma unroll
               for (int k = 0; k < 5; ++k)
                 planes64[kPl64OffG + k * kPl64G + row * kTW + (col - 3)] =
-                    k == 2 ? fma(v, tile[2 * kPos64 + e], pp) : v * tile[k * kPos64 + e];
+                    k == 2 ? fma(hv, tile[2 * kPos64 + e], hp) : hv * tile[k * kPos64 + e];
             }
           }
         }
@@ -2256,7 +2267,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.c_p = c.c_p;
   A.c_v = c.c_v;
   A.uniform = (!c.dense && c.c_lr == 0.0) ? 1 : 0;
-  A.finest_first = c.tile_order == 0 ? 1 : 0;
+  A.tile_order = c.tile_order;
   A.chunk = std::max(1, E->sched_chunk);
   A.R = c.R;
   A.ylo = c.xlo[1];
@@ -2630,7 +2641,7 @@ extern "C" {
 int enl_engine_create(const enl_engine_config* cfg, void** out) {
   if (!cfg || !out || cfg->nlevels < 1 || cfg->nlevels > kL || cfg->ratio < 2 || cfg->nx0 < 8 || cfg->ny0 < 8 ||
       cfg->variant < 0 || cfg->variant > 8 || cfg->precision < ENL_PREC_FP64 || cfg->precision > ENL_PREC_FP32_STATE ||
-      cfg->tile_order < 0 || cfg->tile_order > 1 ||
+      cfg->tile_order < 0 || cfg->tile_order > 2 ||
       (cfg->independent && (cfg->nlevels != 1 || cfg->bc[0] == kAbsorb || cfg->bc[1] == kAbsorb ||
                             cfg->bc[2] == kAbsorb || cfg->bc[3] == kAbsorb))) {
     set_error(ENL_ERR_ARG);
@@ -3514,14 +3525,15 @@ int enl_engine_mic_records(void* e, void* host, long long max, long long* n, lon
 // patches of all levels share one persistent grid, and what decides the
 // balance is how the grid's blocks take tiles.  A schedule is
 //   [0] resident blocks per SM of the persistent grid (0: occupancy limit),
-//   [1] tile order: 0 finest level first, 1 level 0 first,
+//   [1] tile order: 0 finest level first, 1 level 0 first, 2 the two ends
+//       of the tile table alternately,
 //   [2] uniform-tile reuse: 1 on (when the configuration allows it), 0 every
 //       tile computed cell by cell (results identical either way),
 //   [3] run length: a block claims this many consecutive tiles at a time
 //       (1, 2, 4: 32x8, 64x8, 128x8 cells of a patch row per claim).
 // ---------------------------------------------------------------------------
 static int apply_schedule(Engine* E, const int* v) {
-  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 1 || v[2] < 0 || v[2] > 1 || v[3] < 1 ||
+  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 2 || v[2] < 0 || v[2] > 1 || v[3] < 1 ||
       v[3] > 16)
     return ENL_ERR_ARG;
   E->sched_bps = v[0];
@@ -3633,12 +3645,12 @@ int enl_engine_autotune(void* e, double dt, int steps, int cap, int* tried, floa
   int current[4];
   get_schedule(E, current);
   save_restore(true);
-  // candidates: the upper half of the occupancy range, both orders, reuse on
+  // candidates: the upper half of the occupancy range, the three orders, reuse on
   // and off (when the configuration allows reuse), runs of 1, 2, 4 tiles
   std::vector<std::array<int, 4>> cand;
   const bool reuse_ok = E->cfg.c_lr == 0.0;
   for (int bps = (E->max_blocks_per_sm + 1) / 2; bps <= E->max_blocks_per_sm; ++bps)
-    for (int order = 0; order <= 1; ++order)
+    for (int order = 0; order <= 2; ++order)
       for (int reuse = reuse_ok ? 1 : 0; reuse >= 0; --reuse)
         for (int chunk : {1, 2, 4}) cand.push_back({bps, order, reuse, chunk});
   std::vector<float> best(cand.size(), 1e30f);
