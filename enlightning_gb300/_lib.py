@@ -77,6 +77,7 @@ ENGINE_SIGNATURES = {
     "enl_engine_packed_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "enl_engine_storage": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "enl_engine_graph_valid": (C.c_int, [C.c_void_p]),
+    "enl_engine_set_level_order": (C.c_int, [C.c_void_p, C.c_int]),
     "enl_engine_set_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int]),
     "enl_engine_get_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int]),
     "enl_engine_autotune": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int),

@@ -254,6 +254,7 @@ struct StageArgs {
   FastConst F[kL];
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
   int uniform;              // uniform tiles reuse a computed cell (c_lr == 0 and not dense)
+  const int* tile_base;     // first table entry of the launch's tiles (null: 0)
   int tile_order;           // 0 finest level first (table from its end), 1 level 0
                             // first, 2 the two ends alternately
   int chunk;                // a block claims runs of `chunk` consecutive tiles (>= 1)
@@ -490,6 +491,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   __shared__ S s_wl[8][6];  // per warp: u^n (5 fields) and H0 of its first cell
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ntiles = *A.ntiles;
+  const int tbase = A.tile_base ? *A.tile_base : 0;
   // the block's next tile: the rest of its run of A.chunk consecutive tiles
   // (neighbours in the table: the next tile to the right in a patch row),
   // then a new run from the counter
@@ -504,7 +506,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     const int ti = A.tile_order == 1 ? t
                    : A.tile_order == 2 ? ((t & 1) ? (t >> 1) : ntiles - 1 - (t >> 1))
                                        : ntiles - 1 - t;
-    const int4 td = A.tiles[ti];
+    const int4 td = A.tiles[tbase + ti];
     s_td[b] = td;
     // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
     // doubles, a multiple of 4 for floats; set_patches only accepts such
@@ -1493,16 +1495,25 @@ struct SpeedArgs {
 
 // max(|rho u|, |rho v|) / |rho| is max(|u|, |v|) bit for bit (a correctly
 // rounded division is monotonic), with one division instead of two.  With
-// perturbation storage the speed is formed in single precision.
+// perturbation storage the speed is formed in single precision.  With FP64
+// storage a cell divides in FP64 only when its single-precision estimate
+// says it may hold the block's maximum (FP64 division costs about nine
+// fused multiply-adds on this GPU); the maximum is the same double.
 // Each block takes kSpeedTiles tiles per pass with all their loads in flight
 // together (the pass is a chain of dependent loads: descriptor, then fields).
 constexpr int kSpeedTiles = 4;
 template <typename S>
 __global__ void speed_kernel(SpeedArgs<S> A) {
   __shared__ double s_w[8];
+  __shared__ float s_e[8];
   const int n = *A.ntiles;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   double m = 0.0;
+  float m64est = 0.f;  // FP64 storage: the largest quotient estimate of the pass
+  float cand_q[kSpeedTiles];
+  double av[kSpeedTiles], bv[kSpeedTiles];
+#pragma unroll
+  for (int u = 0; u < kSpeedTiles; ++u) cand_q[u] = -1.f;
   for (int t0 = blockIdx.x; t0 < n; t0 += kSpeedTiles * gridDim.x) {
     int4 td[kSpeedTiles];
 #pragma unroll
@@ -1531,11 +1542,53 @@ __global__ void speed_kernel(SpeedArgs<S> A) {
       if constexpr (std::is_same<S, float>::value) {
         const float rr = (float)A.rho_off + r[u];
         s = (double)(fmaxf(fabsf(mu[u]), fabsf(mv[u])) / fabsf(rr) + (float)A.c);
+        if (!(s == s)) s = 1e300;  // NaN state: force a tiny dt, health check reports it
+        m = fmax(m, s);
       } else {
-        s = fmax(fabs(mu[u]), fabs(mv[u])) / fabs(r[u]) + A.c;
+        // FP64: the quotient max(|rho u|, |rho v|) / |rho| is divided exactly
+        // only where it can be the largest of the block (below); here its
+        // single-precision estimate
+        const double a = fmax(fabs(mu[u]), fabs(mv[u])), b = fabs(r[u]);
+        const float qe = __fdividef((float)a, (float)b);
+        // cells whose estimate proves nothing: zero numerator (exact 0),
+        // values outside the float range, NaN, zero density
+        const bool odd = !(qe > 0.f && qe < 1e30f) || !(b > 0.0);
+        if (a == 0.0 && b > 0.0) {
+          m = fmax(m, A.c);  // quotient exactly 0: the speed is c
+        } else if (odd) {
+          double q = a / b;
+          if (!(q == q)) q = 1e300;  // NaN state: force a tiny dt, health check reports it
+          m = fmax(m, q + A.c);
+        } else {
+          cand_q[u] = qe;
+          m64est = fmaxf(m64est, qe);
+        }
+        av[u] = a;
+        bv[u] = b;
       }
-      if (!(s == s)) s = 1e300;  // NaN state: force a tiny dt, health check reports it
-      m = fmax(m, s);
+    }
+    if constexpr (!std::is_same<S, float>::value) {
+      // the block's largest estimate; a cell can hold the largest exact
+      // quotient only if its estimate is within the estimates' relative error
+      // (2^-21 from the two roundings to float and the approximate division,
+      // taken here as 1e-5) of that maximum: only those divide in FP64, so
+      // the maximum is the same double as dividing everywhere
+      float bm = m64est;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+      if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = bm;
+      __syncthreads();
+      bm = s_e[0];
+#pragma unroll
+      for (int w = 1; w < 8; ++w) bm = fmaxf(bm, s_e[w]);
+      __syncthreads();
+      const float thr = bm * (1.0f - 1e-5f);
+#pragma unroll
+      for (int u = 0; u < kSpeedTiles; ++u) {
+        if (cand_q[u] >= 0.f && cand_q[u] >= thr) m = fmax(m, av[u] / bv[u] + A.c);
+        cand_q[u] = -1.f;
+      }
+      m64est = 0.f;
     }
   }
 #pragma unroll
@@ -1809,7 +1862,9 @@ enum {
   M_CT_CNT = 1 + 3 * kL,
   M_PATCH_OFF = 1 + 4 * kL,  // kL + 1 entries: first patch-table index of each level, then the total
   M_HALO_NCELL = 2 + 5 * kL,  // +level: halo cells to interpolate
-  M_SIZE = 2 + 6 * kL
+  M_TILE_OFF = 2 + 6 * kL,    // +level: first stage tile of the level
+  M_TILE_CNT = 2 + 7 * kL,    // +level: stage tiles of the level
+  M_SIZE = 2 + 8 * kL
 };
 
 template <typename T>
@@ -1921,6 +1976,7 @@ struct Engine {
   // stage-kernel schedule (enl_engine_set_schedule / enl_engine_autotune):
   // resident blocks per SM of the persistent grid (the occupancy limit by
   // default) and the length of the tile runs a block claims
+  int samrai_order = 0;  // enl_engine_set_level_order
   int max_blocks_per_sm = 1;
   int sched_bps = 0;  // 0: max_blocks_per_sm
   int sched_chunk = 1;
@@ -2096,6 +2152,10 @@ static int rebuild_tables(Engine* E) {
     E->h_meta[M_CT_CNT + l] = (int)E->h_ctiles.size() - E->h_meta[M_CT_OFF + l];
   }
   E->h_meta[M_NTILES] = (int)E->h_tiles.size();
+  for (int l = 0; l < kL; ++l) {
+    E->h_meta[M_TILE_OFF + l] = l < nl ? E->tile_off[l] : (int)E->h_tiles.size();
+    E->h_meta[M_TILE_CNT + l] = l < nl ? E->tile_cnt[l] : 0;
+  }
   for (int l = 0; l < kL; ++l) E->h_meta[M_PATCH_OFF + l] = l < nl ? E->patch_off[l] : (int)E->h_patchtab.size();
   E->h_meta[M_PATCH_OFF + kL] = (int)E->h_patchtab.size();
   E->h_tileoff.resize(E->h_tiles.size());
@@ -2210,7 +2270,9 @@ static EosConst64 eos_const64(const enl_engine_config& c) {
                     1.0 / c.c_p, 1.0 / c.c_v};
 }
 
-static StageArgs stage_args(Engine* E, int stage, double dt) {
+// level < 0: the launch covers every tile of every level; otherwise the
+// tiles of that level only (the per-level stage order)
+static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   StageArgs A;
   memset(&A, 0, sizeof(A));
   const auto& c = E->cfg;
@@ -2288,8 +2350,9 @@ static StageArgs stage_args(Engine* E, int stage, double dt) {
   A.any_absorb = any_absorb(E);
   A.patchtab = E->d_patchtab.p;
   A.tiles = E->d_tiles.p;
-  A.ntiles = E->d_meta + M_NTILES;
-  A.counter = E->d_counters + stage;
+  A.ntiles = E->d_meta + (level < 0 ? M_NTILES : M_TILE_CNT + level);
+  A.tile_base = level < 0 ? nullptr : E->d_meta + M_TILE_OFF + level;
+  A.counter = E->d_counters + (level < 0 ? stage : 3 * (1 + level) + stage);
   A.health = E->d_health;
   A.stats = E->d_stats;
   A.mlp = E->cfg.learned ? E->d_mlp : nullptr;  // null until set_mlp
@@ -2324,12 +2387,15 @@ static StageFn pick_stage(int precision, int variant) {
 }
 
 template <typename S>
-static int fill_level(Engine* E, int l, int which, bool skip_unread) {
+static int fill_level(Engine* E, int l, int which, bool skip_unread, int src_which = -1) {
   cudaStream_t s = stream();
   const auto& c = E->cfg;
   Level& L = E->lev[l];
   if (l > 0) {
-    interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(which), c.ratio,
+    // coarse-fine ghosts from buffer src_which of the coarser level (the
+    // same buffer unless given)
+    const int src = src_which < 0 ? which : src_which;
+    interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(src), c.ratio,
                                                 E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l,
                                                 M_HALO_NCELL + l, kNF);
   }
@@ -2507,12 +2573,35 @@ static void record_mics(Engine* E) {
 
 static int step_fused(Engine* E, double dt) {
   cudaStream_t s = stream();
-  cudaMemsetAsync(E->d_counters, 0, 3 * sizeof(int), s);
+  cudaMemsetAsync(E->d_counters, 0, 3 * (1 + kL) * sizeof(int), s);
   adaptive_dt(E, dt);
   StageFn fn = pick_stage(E->cfg.precision, E->cfg.variant);
   for (int st = 0; st < 3; ++st) {
     int in = st == 0 ? 0 : st;
     int out = st == 2 ? 0 : st + 1;
+    if (E->samrai_order) {
+      // SAMRAI's MethodOfLinesIntegrator order (main.C:448): per stage the
+      // levels coarsest first, each filling its ghosts -- coarse-fine ones
+      // from the coarser level already advanced in this stage -- and then
+      // advancing; one launch per level
+      if (E->profile) cudaEventRecord(E->pev[2 * st], s);
+      for (int l = 0; l < E->cfg.nlevels; ++l) {
+        if (l > 0) {
+          // the coarser level's ghosts in its advanced buffer, as SAMRAI's
+          // refine schedule rebuilds them (from the levels below, already
+          // advanced, and the physical boundary) before interpolating
+          if (E->f32s) fill_level<float>(E, l - 1, out, false);
+          else fill_level<double>(E, l - 1, out, false);
+        }
+        if (E->f32s) fill_level<float>(E, l, in, true, out);
+        else fill_level<double>(E, l, in, true, out);
+        StageArgs A = stage_args(E, st, dt, l);
+        void* args[] = {&A};
+        cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
+      }
+      if (E->profile) cudaEventRecord(E->pev[2 * st + 1], s);
+      continue;
+    }
     fill_all(E, in, kL, true);
     StageArgs A = stage_args(E, st, dt);
     void* args[] = {&A};
@@ -2699,7 +2788,7 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   }
   cudaMalloc(&E->d_meta, sizeof(E->h_meta));
   cudaMemset(E->d_meta, 0, sizeof(E->h_meta));
-  cudaMalloc(&E->d_counters, 4 * sizeof(int));
+  cudaMalloc(&E->d_counters, 3 * (1 + kL) * sizeof(int));
   cudaMalloc(&E->d_health, sizeof(int));
   cudaMemset(E->d_health, 0, sizeof(int));
   cudaMalloc(&E->d_stats, 4 * kL * sizeof(unsigned long long));
@@ -3054,7 +3143,11 @@ int enl_engine_launches_per_step(void* e, int plain) {
   if (!plain) {
     int bands = 0;
     for (int l = 0; l < nl; ++l) bands += (c.independent || E->bc_read[l] != 0) ? 1 : 0;
-    return 3 * (bands + (nl - 1) + 1) + (nl - 1) + dt;
+    // SAMRAI order: one stage launch per level, and the coarser level's
+    // ghosts rebuilt before each finer level (a band fill, and an
+    // interpolation below level 1)
+    const int refresh = E->samrai_order ? (nl - 1) + (nl > 2 ? nl - 2 : 0) : 0;
+    return 3 * (bands + (nl - 1) + (E->samrai_order ? nl : 1) + refresh) + (nl - 1) + dt;
   }
   const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;
@@ -3701,6 +3794,17 @@ int enl_engine_autotune(void* e, double dt, int steps, int cap, int* tried, floa
   release();
   if (rc != ENL_OK) return rc;
   return check_launch("engine autotune");
+}
+
+int enl_engine_set_level_order(void* e, int samrai) {
+  Engine* E = (Engine*)e;
+  if (!E || samrai < 0 || samrai > 1) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  E->samrai_order = samrai;
+  E->graph_valid = false;  // the step's launches change
+  return ENL_OK;
 }
 
 int enl_engine_set_adaptive_dt(void* e, int on, double cfl) {

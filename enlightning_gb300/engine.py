@@ -132,6 +132,12 @@ class Engine:
     def cells(self):
         return sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1) for lv in self.patches for b in lv)
 
+    def set_level_order(self, samrai=True):
+        """Stage order across levels: SAMRAI's (each level filled from the
+        coarser level already advanced in the same stage) or the default
+        (every level from the same stage input, one launch per stage)."""
+        _lib.check(self.L.enl_engine_set_level_order(self.h, int(bool(samrai))), "enl_engine_set_level_order")
+
     # -- schedule and autotuner ---------------------------------------------
     SCHEDULE_KEYS = ("blocks_per_sm", "tile_order", "reuse", "run")
 

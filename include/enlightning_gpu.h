@@ -317,6 +317,15 @@ int enl_engine_sync(void* engine);
 int enl_engine_profile(void* engine, int on, double* ms_total,
                        long long* launches, long long* cells);
 
+/* Stage order across levels.  samrai = 0 (default): in every RK stage all
+ * levels fill their ghosts from the same stage input and advance in one
+ * launch.  samrai = 1: the order of SAMRAI's MethodOfLinesIntegrator, which
+ * the reference drives (main.C:448): per stage the levels go coarsest first,
+ * each filling its ghosts (coarse-fine ones interpolated from the coarser
+ * level after that level's update in the same stage) and then advancing, one
+ * launch per level.  Invalidates a captured graph. */
+int enl_engine_set_level_order(void* engine, int samrai);
+
 /* Stage-kernel schedule.  Replaces SAMRAI's patch-to-rank load balancing
  * (main.C:268-301): every patch of every level shares one persistent grid,
  * and the schedule decides how its blocks take the tiles.

@@ -16,6 +16,12 @@ CPU with the oracle's restated Fortran for every per-patch call:
   runge_kutta, update_state and the absorbing envelope on every patch
   (enlightning.C:459-583); copy scratch -> current; average fine cells onto
   the coarse cells under them, finest level first.
+* order="samrai": the stage order of SAMRAI's MethodOfLinesIntegrator, which
+  main.C:448 drives: per stage the levels go coarsest first, each filling
+  its ghosts and then advancing its patches, so that a level's coarse-fine
+  ghosts are interpolated from the coarser level's data after that level's
+  update in the same stage (with the coarser level's own ghosts rebuilt
+  around that data first, as SAMRAI's refine schedule does).
 """
 from __future__ import annotations
 
@@ -99,8 +105,8 @@ class OracleAMR:
                     v[2] = -v[2]
                 a[:, rows, cols] = v[:, None, None]
 
-    def fill(self, bufs):
-        for l in range(self.nl):
+    def fill(self, bufs, levels=None):
+        for l in (range(self.nl) if levels is None else levels):
             if l > 0:
                 jj, ii = np.nonzero(self.halo_mask(l))
                 self.interp_cells(bufs[l], bufs[l - 1], l, jj, ii)
@@ -110,43 +116,57 @@ class OracleAMR:
     def _patch_view(self, a, b):
         return a[:, b[2]:b[3] + 1 + 2 * G, b[0]:b[1] + 1 + 2 * G]
 
-    def step(self, dt):
-        prm = self.prm
+    def step(self, dt, order="engine"):
         for l in range(self.nl):
             for b in self.patches[l]:
                 self._patch_view(self.scr[l], b)[:, G:-G, G:-G] = self._patch_view(self.cur[l], b)[:, G:-G, G:-G]
         for s in range(3):
-            self.fill(self.scr)
-            KK = {}
-            for l in range(self.nl):
-                for n, b in enumerate(self.patches[l]):
-                    v = self._patch_view(self.scr[l], b)
-                    w = np.ascontiguousarray(v[0:5])
-                    p = np.ascontiguousarray(v[5])
-                    t = np.ascontiguousarray(v[6])
-                    nx, ny = b[1] - b[0] + 1, b[3] - b[2] + 1
-                    xlo = (self.xlo[0] + self.dx[l][0] * b[0], self.xlo[1] + self.dx[l][1] * b[2])
-                    KK[(l, n)] = ora.rhs(self.variant, b, (G, G), xlo, self.dx[l], w, np.zeros((ny, nx)), p, t,
-                                         prm, l)
-            for l in range(self.nl):
-                for n, b in enumerate(self.patches[l]):
-                    v = self._patch_view(self.scr[l], b)
-                    w = np.ascontiguousarray(v[0:5])
-                    p = np.ascontiguousarray(v[5])
-                    t = np.ascontiguousarray(v[6])
-                    ww = np.ascontiguousarray(self._patch_view(self.cur[l], b)[0:5, G:-G, G:-G])
-                    ora.runge_kutta(b, (G, G), dt, RK[0][s], RK[1][s], RK[2][s], w, ww, KK[(l, n)])
-                    xlo = (self.xlo[0] + self.dx[l][0] * b[0], self.xlo[1] + self.dx[l][1] * b[2])
-                    ora.update_state(self.dx[l], xlo, b, (G, G), w, p, t, prm)
-                    ora.absorb(b, (G, G), xlo, self.dx[l], self.xlo, self.level_hi(l), self.bc,
-                               prm["bc_absorb_width"], prm, w, p, t)
-                    v[0:5, G:-G, G:-G] = w[:, G:-G, G:-G]
-                    v[5, G:-G, G:-G] = p[G:-G, G:-G]
-                    v[6, G:-G, G:-G] = t[G:-G, G:-G]
+            if order == "samrai":
+                for l in range(self.nl):
+                    if l > 0:
+                        # the coarser level's ghosts again, around its
+                        # advanced data (SAMRAI's refine schedule rebuilds
+                        # the coarse data it interpolates from)
+                        self.fill(self.scr, levels=[l - 1])
+                    self.fill(self.scr, levels=[l])
+                    self._stage(dt, s, [l])
+            else:
+                self.fill(self.scr)
+                self._stage(dt, s, range(self.nl))
         for l in range(self.nl):
             for b in self.patches[l]:
                 self._patch_view(self.cur[l], b)[:, G:-G, G:-G] = self._patch_view(self.scr[l], b)[:, G:-G, G:-G]
         self.coarsen()
+
+    def _stage(self, dt, s, levels):
+        """Stage s on the patches of `levels`: rhs on every patch first, then
+        runge_kutta, update_state and the envelope, in place in the scratch data."""
+        prm = self.prm
+        KK = {}
+        for l in levels:
+            for n, b in enumerate(self.patches[l]):
+                v = self._patch_view(self.scr[l], b)
+                w = np.ascontiguousarray(v[0:5])
+                p = np.ascontiguousarray(v[5])
+                t = np.ascontiguousarray(v[6])
+                nx, ny = b[1] - b[0] + 1, b[3] - b[2] + 1
+                xlo = (self.xlo[0] + self.dx[l][0] * b[0], self.xlo[1] + self.dx[l][1] * b[2])
+                KK[(l, n)] = ora.rhs(self.variant, b, (G, G), xlo, self.dx[l], w, np.zeros((ny, nx)), p, t, prm, l)
+        for l in levels:
+            for n, b in enumerate(self.patches[l]):
+                v = self._patch_view(self.scr[l], b)
+                w = np.ascontiguousarray(v[0:5])
+                p = np.ascontiguousarray(v[5])
+                t = np.ascontiguousarray(v[6])
+                ww = np.ascontiguousarray(self._patch_view(self.cur[l], b)[0:5, G:-G, G:-G])
+                ora.runge_kutta(b, (G, G), dt, RK[0][s], RK[1][s], RK[2][s], w, ww, KK[(l, n)])
+                xlo = (self.xlo[0] + self.dx[l][0] * b[0], self.xlo[1] + self.dx[l][1] * b[2])
+                ora.update_state(self.dx[l], xlo, b, (G, G), w, p, t, prm)
+                ora.absorb(b, (G, G), xlo, self.dx[l], self.xlo, self.level_hi(l), self.bc,
+                           prm["bc_absorb_width"], prm, w, p, t)
+                v[0:5, G:-G, G:-G] = w[:, G:-G, G:-G]
+                v[5, G:-G, G:-G] = p[G:-G, G:-G]
+                v[6, G:-G, G:-G] = t[G:-G, G:-G]
 
     def level_hi(self, l):
         nx, ny = self.shape[l]

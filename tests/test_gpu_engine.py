@@ -762,3 +762,85 @@ def test_independent_problems_fp32_state_within_budget(ora):
         sl = (slice(bx[2], bx[3] + 1), slice(bx[0], bx[1] + 1))
         assert relL2(a[0][sl] - prm["rho0"], b[0][sl] - prm["rho0"]) <= 1e-3
         assert relL2(a[1][sl], b[1][sl]) <= 1e-3
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_samrai_level_order_matches_oracle(ora, precision):
+    """SAMRAI's stage order (each level's coarse-fine ghosts from the coarser
+    level already advanced in the same stage, main.C:448) against the
+    oracle's restatement of it: FP64 within 1e-12, FP32 storage within 1e-3;
+    graph replay bit-identical to direct steps; and the order matters (the
+    default order gives other states)."""
+    prm = default_params(bc_absorb_width=0.5)
+    nx, ny = 48, 40
+    fine = FINE_SETS["inside"]
+    levels = [[(0, 23, 0, 39), (24, 47, 0, 39)], fine]
+    bc = (ABSORB, REFLECT, REFLECT, ABSORB)
+    dt = workloads.pulse_dt(prm, (0.05, 0.05))
+    E, O = make_pair(prm, nx, ny, (0.1, 0.1), 2, levels, bc, "hybrid_high_llf", precision=precision)
+    E.set_level_order(True)
+    for _ in range(5):
+        E.step(dt)
+        O.step(dt, order="samrai")
+    torch.cuda.synchronize()
+    assert E.health() == 0
+    tol = 1e-12 if precision == PREC_FP64 else 1e-3
+    compare(E, O, 0, tol)
+    compare(E, O, 1, tol)
+    if precision != PREC_FP64:
+        return
+    # graph replay of the per-level launches equals direct steps
+    E2, _ = make_pair(prm, nx, ny, (0.1, 0.1), 2, levels, bc, "hybrid_high_llf", precision=precision)
+    E2.set_level_order(True)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        E2.L.enl_set_stream(__import__("ctypes").c_void_p(s.cuda_stream))
+        E2.capture(dt)
+        E2.replay(5)
+    torch.cuda.synchronize()
+    for l in range(2):
+        assert np.array_equal(E2.level_state(l).cpu().numpy(), E.level_state(l).cpu().numpy())
+    # the default order differs from SAMRAI's
+    E3, O3 = make_pair(prm, nx, ny, (0.1, 0.1), 2, levels, bc, "hybrid_high_llf", precision=precision)
+    for _ in range(5):
+        E3.step(dt)
+    torch.cuda.synchronize()
+    a, b = E3.level_state(1).cpu().numpy(), E.level_state(1).cpu().numpy()
+    assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) > 1e-10
+
+
+def test_cfl_speed_reduction_is_exact():
+    """The FP64 CFL reduction divides only where a single-precision estimate
+    allows the block maximum; dt must still be the double that dividing every
+    cell gives: quotients tied to within 1e-9 at the top, zero velocities,
+    and both signs, on two levels."""
+    prm = default_params()
+    nx, ny = 160, 96
+    rng = np.random.default_rng(11)
+    E = Engine(prm, nx, ny, (0.1, 0.1), nlevels=2, bc=(REFLECT,) * 4, precision=PREC_FP64)
+    rho = prm["rho0"] * (1.0 + 0.05 * rng.uniform(-1, 1, (ny, nx)))
+    u = 40.0 * (1.0 + 1e-9 * rng.uniform(-1, 1, (ny, nx))) * rng.choice([-1.0, 1.0], (ny, nx))
+    v = 39.99999 * rng.uniform(-1, 1, (ny, nx))
+    u[:, : nx // 3] = 0.0
+    v[:, : nx // 3] = 0.0
+    w = np.stack([rho, rho * u, rho * v, np.zeros_like(rho), rho * prm["T0"]])
+    p = np.full_like(rho, prm["p0"])
+    T = np.full_like(rho, prm["T0"])
+    E.set_level_state(0, w, p, T)
+    E.set_patches(0, [(0, 79, 0, 95), (80, 159, 0, 95)])
+    fine = [(64, 191, 32, 127)]
+    E.set_patches(1, fine)
+    E.refine_init(1, fine)
+    torch.cuda.synchronize()
+    smax = 0.0
+    for l in range(2):
+        st = E.level_state(l).cpu().numpy()
+        for b in E.patches[l]:
+            sl = (slice(b[2], b[3] + 1), slice(b[0], b[1] + 1))
+            q = np.maximum(np.abs(st[1][sl]), np.abs(st[2][sl])) / np.abs(st[0][sl])
+            smax = max(smax, float((q + prm["c"]).max()))
+    E.set_adaptive_dt(True, 0.5)
+    E.step(1.0)
+    dt, _ = E.time()
+    assert dt == (0.5 * 0.05) / smax
+    E.close()
