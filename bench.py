@@ -818,6 +818,79 @@ def run_stats_only(args):
                       "uniform_cells": int(st[:, 3].sum())}), flush=True)
 
 
+def extra_records(args, fpk):
+    """Short runs of the other workloads, reported beside the line source:
+    the 64 independent pulses and the Mach-1.5 shock (FP64 batched engine
+    with the metric's switch, against the plain per-patch FP64 arm from the
+    same state) and the single 512x512 pulse through the drop-in entry
+    points.  Each: rate over `steps` graph-replayed steps, the stage kernel's
+    FP64 roofline, and the relative L2 difference from the plain arm after
+    a few matched steps (the full-horizon parity of these workloads is in the
+    GPU tests)."""
+    import torch
+    out = {}
+    f_weno, f_drp = fp64_flops_per_cell()
+    steps, ncmp = 10, 4
+    for name in ("pulses64", "mach"):
+        t0 = time.perf_counter()
+        wl = WORKLOADS[name](learned=args.learned, precision=0)
+        tune = tune_schedule(wl, args.schedule_cache)
+        wl.advance("fast", ncmp, use_graph=True)
+        wl.advance("plain", ncmp)
+        torch.cuda.synchronize()
+        err = wl.compare()
+        wl.advance("fast", 3, use_graph=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        cu = wl.advance("fast", steps, use_graph=True)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        kms, kcells, kst, nl = stage_timing(wl)
+        dense = float(kst[:, 1].sum() - kst[:, 3].sum()) / nl
+        weno = float(kst[:, 0].sum()) / nl
+        flops = weno * f_weno + max(0.0, dense - weno) * f_drp if f_weno else None
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record()
+        cup = wl.advance("plain", 2)
+        p1.record()
+        torch.cuda.synchronize()
+        st_w = kst[:, 0].sum() / max(1, kst[:, 1].sum())
+        out[name] = {"workload": wl.name, "dtype": "f64", "value": cu / (ms * 1e-3), "unit": UNIT,
+                     "ms_per_step": ms / steps, "steps": steps, "cells_per_step": cu / steps,
+                     "plain_value": cup / (p0.elapsed_time(p1) * 1e-3),
+                     "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp,
+                     "weno_fraction": float(st_w), "schedule": tune["chosen"],
+                     "stage_kernel_ms": kms,
+                     "fp64_roofline": {"achieved": None if flops is None else flops / (kms * 1e-3) / 1e12,
+                                       "peak": fpk["fp64_fma_tflops"], "unit": "TFLOP/s",
+                                       "frac": None if flops is None else flops / (kms * 1e-3) / 1e12
+                                       / fpk["fp64_fma_tflops"]},
+                     "wall_s": time.perf_counter() - t0}
+        wl.fast.close()
+        wl.plain.close()
+        del wl
+    # the single pulse through the drop-in rhs_ / runge_kutta_ / update_state_
+    wl = Pulse512Plain()
+    for _ in range(3):
+        wl.step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        wl.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out["pulse512"] = {"workload": wl.name, "dtype": "f64", "path": "drop-in F77 entry points, per patch",
+                       "value": wl.cells * steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / steps,
+                       "steps": steps,
+                       "parity": "200 steps within 1e-12 of the oracle (rho s within ten times the oracle's own "
+                                 "one-ulp sensitivity), tests/test_gpu_configs.py"}
+    return out
+
+
 def tune_schedule(wl, cache):
     """Autotune the stage kernel's schedule of a workload's fast engine
     (cached by workload signature); returns what the bench line reports."""
@@ -1041,6 +1114,16 @@ def run_linesource(args):
         else:
             cb = cpu_baseline_with_single_core(wl)
     dt_last, sim_t = wl.fast.time()
+    sched_info = tune or wl.fast.schedule()
+    extra = None
+    if not args.no_extra and args.workload == "linesource" and ws == 1:
+        for w_ in (wl32,):
+            if w_ is not None:
+                w_.fast.close()
+        wl.fast.close()
+        if wl.plain is not None:
+            wl.plain.close()
+        extra = extra_records(args, fpk)
     path = ("batched: persistent fused stage kernel over all levels, " + PREC_PATH[args.precision]
             + ", CUDA graph" + (", learned sensor" if wl.learned else ", plain sensor")
             + ("" if args.dense else ", uniform tiles reuse a block-cached cell result"))
@@ -1058,10 +1141,11 @@ def run_linesource(args):
                    "plain_path": "per-patch FP64 rhs / runge_kutta / update_state launches, plain sensor",
                    "speedup_vs_plain": (value / plain_value) if plain_value else None,
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
-                   "uniform_tile_fraction": uniform_frac, "schedule": tune or wl.fast.schedule(),
+                   "uniform_tile_fraction": uniform_frac, "schedule": sched_info,
                    "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "fp_peaks": fpk},
         "fp32_state": secondary,
+        "other_workloads": extra,
         "roofline": roof,
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
@@ -1101,6 +1185,8 @@ def main():
     ap.add_argument("--stats-only", action="store_true",
                     help="run --steps direct steps of the batched engine and print its counters (profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default stage-kernel schedule")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the short runs of the pulse batch, the Mach shock and the single pulse")
     ap.add_argument("--schedule-cache", default=os.path.join(tempfile.gettempdir(), "enlightning_gb300_schedules.json"),
                     help="JSON file of tuned schedules by workload signature")
     ap.add_argument("--no-secondary", action="store_true",
