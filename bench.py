@@ -775,12 +775,18 @@ def fp_peaks():
     return {"fp64_fma_tflops": o[0], "fp64_div_per_s": o[1] * 1e9, "fp32_fma_tflops": o[2]}
 
 
-def fp64_flops_per_cell():
-    """FP64 flops (2 per FMA, 1 per add or multiply) of one dense stage-kernel
-    cell by branch, from the ncu instruction counts in profiles/."""
+def fp64_flops_per_cell(kind="algorithmic"):
+    """FP64 operations per computed cell and stage by branch (WENO, DRP):
+    "algorithmic" = the reference algorithm's operations (oracle-counted
+    rhs plus runge_kutta and update_state, one per + - * /); "implementation"
+    = what the stage kernel issues (ncu: 2 per FMA, 1 per add or multiply).
+    From profiles/stage_fp64_flops.json."""
     try:
         with open(os.path.join(ROOT, "profiles", "stage_fp64_flops.json")) as f:
             d = json.load(f)
+        if kind == "algorithmic":
+            a = d["algorithmic"]
+            return float(a["weno_ops_per_cell"]), float(a["drp_ops_per_cell"])
         return float(d["weno_flops_per_cell"]), float(d["drp_flops_per_cell"])
     except Exception:
         return None, None
@@ -829,7 +835,7 @@ def extra_records(args, fpk):
     GPU tests)."""
     import torch
     out = {}
-    f_weno, f_drp = fp64_flops_per_cell()
+    f_weno, f_drp = fp64_flops_per_cell("algorithmic")
     steps, ncmp = 10, 4
     for name in ("pulses64", "mach"):
         t0 = time.perf_counter()
@@ -1022,10 +1028,12 @@ def run_linesource(args):
     roof = {"kernel": "stage_kernel (" + PREC_NAMES[args.precision] + ")", "kernel_ms": per_launch_ms,
             "cells_per_launch": cells_per_launch}
     if args.precision == 0:
-        f_weno, f_drp = fp64_flops_per_cell()
+        f_weno, f_drp = fp64_flops_per_cell("algorithmic")
+        i_weno, i_drp = fp64_flops_per_cell("implementation")
         dense_cells = float(kst[:, 1].sum() - kst[:, 3].sum()) / nl
         weno_cells = float(kst[:, 0].sum()) / nl
         flops = None if f_weno is None else weno_cells * f_weno + max(0.0, dense_cells - weno_cells) * f_drp
+        iflops = None if i_weno is None else weno_cells * i_weno + max(0.0, dense_cells - weno_cells) * i_drp
         fp64_achieved = None if flops is None else flops / (per_launch_ms * 1e-3) / 1e12
         fp64_peak = fpk["fp64_fma_tflops"]
         roof.update({"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
@@ -1035,7 +1043,16 @@ def run_linesource(args):
                      "flops_per_launch": flops, "dense_cells_per_launch": dense_cells,
                      "weno_cells_per_launch": weno_cells,
                      "flops_per_cell": {"weno": f_weno, "drp": f_drp,
-                                        "source": "profiles/stage_fp64_flops.json (ncu FP64 instruction counts)"},
+                                        "counting": "algorithmic: the reference algorithm's FP64 operations per "
+                                                    "computed cell (oracle-counted rhs, runge_kutta, update_state; "
+                                                    "profiles/stage_fp64_flops.json); cells of uniform tiles, whose "
+                                                    "shared result is computed once per block, are not counted"},
+                     "implementation": {"flops_per_cell": {"weno": i_weno, "drp": i_drp},
+                                        "achieved": None if iflops is None else iflops / (per_launch_ms * 1e-3) / 1e12,
+                                        "frac": None if iflops is None else iflops / (per_launch_ms * 1e-3) / 1e12
+                                        / fp64_peak,
+                                        "counting": "FP64 instructions the kernel issues (ncu: 2 per FMA, 1 per "
+                                                    "add or multiply)"},
                      "hbm": hbm})
     else:
         roof.update({"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -1081,6 +1098,24 @@ def run_linesource(args):
     cue = E.cells() * ke
     e2e_value = aggregate_rate(cue, ws, e2e_ms)
     nbytes = int(n * esize)
+    # the same engine with every tile computed cell by cell (no uniform-tile
+    # reuse; identical states), a few steps after the e2e leg: what the reuse
+    # is worth
+    dense_value, dense_steps = None, max(2, min(args.steps, 6))
+    if not args.dense:
+        keep = wl.fast.schedule()
+        wl.fast.set_schedule(keep["blocks_per_sm"], keep["tile_order"], 0, keep["run"])
+        wl.graph_ok = False
+        wl.advance("fast", 1, use_graph=True)
+        barrier()
+        d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d0.record()
+        cud = wl.advance("fast", dense_steps, use_graph=True)
+        d1.record()
+        barrier()
+        dense_value = aggregate_rate(cud, ws, max_over_ranks(d0.elapsed_time(d1), ws))
+        wl.fast.set_schedule(keep["blocks_per_sm"], keep["tile_order"], keep["reuse"], keep["run"])
+        wl.graph_ok = False
     # the FP32-storage engine: its own timed region (graph replay, regrids)
     secondary = None
     if wl32 is not None:
@@ -1125,7 +1160,8 @@ def run_linesource(args):
             wl.plain.close()
         extra = extra_records(args, fpk)
     path = ("batched: persistent fused stage kernel over all levels, " + PREC_PATH[args.precision]
-            + ", CUDA graph" + (", learned sensor" if wl.learned else ", plain sensor")
+            + ", CUDA graph" + ((", learned sensor on every level" if wl.learned == 2 else ", learned sensor on level 0")
+                                if wl.learned else ", plain sensor")
             + ("" if args.dense else ", uniform tiles reuse a block-cached cell result"))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -1142,6 +1178,11 @@ def run_linesource(args):
                    "speedup_vs_plain": (value / plain_value) if plain_value else None,
                    "rel_l2_vs_plain_fp64": err, "compare_steps": ncmp, "weno_fraction": weno_frac,
                    "uniform_tile_fraction": uniform_frac, "schedule": sched_info,
+                   "dense_value": dense_value, "dense_steps": dense_steps if dense_value else None,
+                   "dense_note": "the same engine and schedule with every tile computed cell by cell "
+                                 "(uniform-tile reuse off; identical states): every cell's update is "
+                                 "computed and stored in both, the reuse computes a bitwise-uniform "
+                                 "tile's shared result once per block",
                    "health": health, "build_s": t_build, "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "fp_peaks": fpk},
         "fp32_state": secondary,
@@ -1168,8 +1209,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="linesource", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--learned", type=int, default=-1,
-                    help="learned switch: 1 on, 0 off, -1 on when the trained network is present (default)")
+    ap.add_argument("--learned", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="learned switch: 1 on level 0, 2 on every level, 0 off, -1 (default) as the trained "
+                         "network was made for, when it is present")
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--compare-steps", type=int, default=20)
     ap.add_argument("--scale", type=int, default=1, help="shrink the line-source base grid (profiling)")
@@ -1193,7 +1235,8 @@ def main():
                     help="skip the FP32-storage engine reported beside the FP64 line")
     args = ap.parse_args()
     if args.learned < 0:  # the metric's configuration: batched + learned switch
-        args.learned = int(os.path.exists(os.path.join(ROOT, "enlightning_gb300", "learned_sensor.npz")))
+        from enlightning_gb300 import sensor
+        args.learned = sensor.weights_levels() if os.path.exists(sensor.WEIGHTS) else 0
     if args.stats_only:
         run_stats_only(args)
     elif args.impl == "reference":

@@ -255,6 +255,7 @@ struct StageArgs {
   double rho0, p0, T0, c, c_lr, gm1_over_2rho0, c_p, c_v, R, ylo, dy[kL];
   int uniform;              // uniform tiles reuse a computed cell (c_lr == 0 and not dense)
   const int* tile_base;     // first table entry of the launch's tiles (null: 0)
+  int learned_levels;       // levels whose plain-WENO cells the network reviews
   int tile_order;           // 0 finest level first (table from its end), 1 level 0
                             // first, 2 the two ends alternately
   int chunk;                // a block claims runs of `chunk` consecutive tiles (>= 1)
@@ -706,9 +707,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
           }
         }
       };
-      // the learned review (level 0 tiles with WENO cells) keeps its features
-      // where the planes are and rebuilds them after it
-      const bool review = learned && lvl == 0;
+      // the learned review (tiles with WENO cells on level 0, or on every
+      // level: on the fine levels the plain decision is WENO for every cell)
+      // keeps its features where the planes are and rebuilds them after it
+      const bool review = learned && lvl < A.learned_levels;
       build_planes();
       // compaction counts: DRP cells first, then WENO cells, each in tile order
       int nd = 0, nw = 0, od = 0, ow = 0;
@@ -2356,6 +2358,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   A.health = E->d_health;
   A.stats = E->d_stats;
   A.mlp = E->cfg.learned ? E->d_mlp : nullptr;  // null until set_mlp
+  A.learned_levels = E->cfg.learned == 2 ? kL : 1;
   A.margin = E->margin;
   A.feat_eps = (float)A.P[0].sensor_eps;
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
@@ -2730,7 +2733,7 @@ extern "C" {
 int enl_engine_create(const enl_engine_config* cfg, void** out) {
   if (!cfg || !out || cfg->nlevels < 1 || cfg->nlevels > kL || cfg->ratio < 2 || cfg->nx0 < 8 || cfg->ny0 < 8 ||
       cfg->variant < 0 || cfg->variant > 8 || cfg->precision < ENL_PREC_FP64 || cfg->precision > ENL_PREC_FP32_STATE ||
-      cfg->tile_order < 0 || cfg->tile_order > 2 ||
+      cfg->tile_order < 0 || cfg->tile_order > 2 || cfg->learned < 0 || cfg->learned > 2 ||
       (cfg->independent && (cfg->nlevels != 1 || cfg->bc[0] == kAbsorb || cfg->bc[1] == kAbsorb ||
                             cfg->bc[2] == kAbsorb || cfg->bc[3] == kAbsorb))) {
     set_error(ENL_ERR_ARG);

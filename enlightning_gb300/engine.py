@@ -51,7 +51,10 @@ class Engine:
         cfg.dx0[:] = list(dx0)
         cfg.bc[:] = list(bc)
         cfg.variant = VARIANTS.index(variant) if isinstance(variant, str) else int(variant)
-        cfg.precision, cfg.learned = int(precision), int(bool(learned))
+        # learned: False/0 off, True/1 the learned switch on level 0, 2 or
+        # "all" on every level
+        lv = 2 if learned in (2, "all") else int(bool(learned))
+        cfg.precision, cfg.learned = int(precision), lv
         for k in ("weno_alpha", "kappa", "mu", "muB", "R", "T_star_n", "tau_n", "c", "c_lr", "rho0", "gamma1",
                   "c_p", "p0", "T0", "c_v"):
             setattr(cfg, k, float(p[k]))
@@ -66,7 +69,7 @@ class Engine:
         self.cfg = cfg
         self.params = dict(p)
         self._init_args = dict(nx0=nx0, ny0=ny0, dx0=tuple(dx0), nlevels=nlevels, ratio=ratio, xlo=tuple(xlo),
-                               bc=tuple(bc), variant=variant, precision=int(precision), learned=bool(learned),
+                               bc=tuple(bc), variant=variant, precision=int(precision), learned=lv,
                                independent=bool(independent), dense=bool(dense), tile_order=int(tile_order))
         self.nlevels, self.ratio = nlevels, ratio
         self.dx0 = tuple(dx0)

@@ -3,26 +3,28 @@
 The reference's hybrid switch (fortran/rhs_hybrid_high_llf.m4:239-256) sends
 a level-0 cell to WENO when any of six density-ratio tests falls below
 0.9999; with the test's small epsilon it does so for almost every cell that a
-wave of any amplitude has reached.  The learned switch predicts, from 40
-stencil features, whether WENO actually changes the right-hand side there:
+wave of any amplitude has reached.  On the finer levels the reference runs
+WENO on every cell.  The learned switch predicts, from 40 stencil features,
+whether WENO actually changes the right-hand side there:
 
-  label y = 1  iff  the plain switch says WENO  and
+  label y = 1  iff  the plain decision is WENO  and
                     err = max_k dt |KK_drp,k - KK_weno,k| / scale_k > tau
-
-scale_k is the perturbation of field k that an acoustic wave with the run's
-RMS pressure perturbation carries (run_scales), so one threshold means the
-same on a weak pulse, a Mach shock and a line source.
-
-The network only reviews cells the plain switch puts on WENO (it can send
-them back to DRP), so the harvest keeps those cells.
 
 where KK_drp and KK_weno are the two right-hand sides of the same cell in
 FP64 (harvested by enl_engine_harvest from trajectories of the batched
-engine).  Training runs entirely on the GPU with the library's BF16
+engine) and scale_k is the perturbation of field k that an acoustic wave
+with the run's RMS pressure perturbation carries (run_scales), so one
+threshold means the same on a weak pulse, a Mach shock and a line source.
+
+The network only reviews cells whose plain decision is WENO (it can send them
+back to DRP), on level 0 (engine learned = 1, the default) or on every level
+(learned = 2, --levels 2), so the harvest keeps those cells: the plain
+switch's WENO cells of level 0, and with --levels 2 every cell of the finer
+levels.  Training runs entirely on the GPU with the library's BF16
 tensor-core forward/backward kernels (enl_mlp_grad) and Adam (enl_mlp_adam).
-At run time the plain switch still decides every cell whose logit lies within
-+-margin of 0, and it remains the reference the learned run is measured
-against.
+At run time the plain decision stands for every cell whose logit lies within
++-margin of 0, and the plain run remains the reference the learned run is
+measured against.
 """
 from __future__ import annotations
 
@@ -45,14 +47,23 @@ NF = 40
 # to the run's acoustic amplitude) and the largest relative L2
 # difference from the plain switch that a network may cause on the held-out
 # runs, each at its workload's full horizon: half of the 1e-3 accuracy bound
-TAUS = (1e-5, 1e-4, 1e-3, 1e-2)
+TAUS = (1e-5, 1e-4, 3e-4, 1e-3, 3e-3, 1e-2)
 ERR_BUDGET = 5e-4
-# rows harvested: the plain switch's WENO cells of level 0 (the only ones the
-# network reviews), about 50 million from seeds 0-9 of the Mach-shock and
-# line-source workloads and from batches of independent pulses with seeds
+# rows harvested: the plain switch's WENO cells (the only ones the network
+# reviews) of every level, about 50 million from seeds 0-9 of the Mach-shock
+# and line-source workloads and from batches of independent pulses with seeds
 # 10-19 (the pulse batch of the evaluation is seed 7)
 HARVEST_ROWS = 50_000_000
 PULSE_SEEDS = range(10, 20)
+# shares of the harvest buffer per source and level, for a network that
+# reviews level 0 (engine learned = 1, the default) or every level (learned =
+# 2; on the fine levels the reference always uses WENO, so every cell there
+# is a row)
+HARVEST_SHARES = {
+    1: {"pulses": 0.54, "line L0": 0.22, "line L1": 0.0, "line L2": 0.0, "mach L0": 0.24, "mach L1": 0.0},
+    2: {"pulses": 0.16, "line L0": 0.10, "line L1": 0.16, "line L2": 0.24, "mach L0": 0.18, "mach L1": 0.16},
+}
+LEARNED_LEVELS = 1
 
 
 def nparams():
@@ -62,6 +73,13 @@ def nparams():
 def load_weights(path=WEIGHTS):
     d = np.load(path)
     return d["params"].astype(np.float32), float(d["margin"])
+
+
+def weights_levels(path=WEIGHTS):
+    """The engine's learned setting the stored network was trained and
+    evaluated for: 1 (level 0) or 2 (every level)."""
+    d = np.load(path)
+    return int(d["levels"]) if "levels" in d.files else 1
 
 
 def init_params(seed=0):
@@ -175,54 +193,85 @@ def logits(X, params):
     return out
 
 
-def harvest_line_source(H, seeds, steps=100, every=10, keep0=0.0, prm=None, log=None, **kw):
+class Quota:
+    """Rows harvested per (source, level), each up to its share of the buffer."""
+
+    def __init__(self, H, shares):
+        self.H, self.share, self.got = H, dict(shares), {k: 0 for k in shares}
+
+    def take(self, key, engine, level, dt, prm, keep0, seed):
+        if self.got[key] >= self.share[key]:
+            return False
+        before = int(self.H.count.item())
+        self.H.take(engine, level, dt, prm, keep0, seed)
+        self.got[key] += int(self.H.count.item()) - before
+        return True
+
+    def full(self, *keys):
+        return all(self.got[k] >= self.share[k] for k in keys)
+
+
+def harvest_line_source(Q, seeds, steps=300, every=(10, 50, 50), keep0=0.0, prm=None, log=None, **kw):
+    """Line-source runs: level-0 rows (plain-switch WENO cells) every
+    every[0] steps and fine-level rows (every cell: the reference always
+    uses WENO there) every every[l] steps."""
     from . import workloads
     from .engine import PREC_FP32_STATE
     prm = prm or default_params()
+    keys = [f"line L{l}" for l in range(3)]
     for sd in seeds:
+        if Q.full(*keys):
+            break
         E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32_STATE, **kw)
         for s in range(steps):
             if s and s % 10 == 0:
                 Hy.regrid()
             E.step(1.0)
-            if (s + 1) % every == 0:
-                dt, _ = E.time()
-                H.take(E, 0, dt, prm, keep0, sd * 1000 + s)
+            for l in range(E.nlevels):
+                if every[l] and (s + 1) % every[l] == 0:
+                    dt, _ = E.time()
+                    Q.take(keys[l], E, l, dt, prm, keep0, sd * 1000 + s + 100000 * l)
         if log:
-            log(f"line source seed {sd}: {int(H.count.item())} rows")
+            log(f"line source seed {sd}: " + ", ".join(f"{k} {Q.got[k]}" for k in keys))
         E.close()
 
 
-def harvest_shock(H, seeds, steps=400, every=25, keep0=0.0, prm=None, log=None, **kw):
+def harvest_shock(Q, seeds, steps=400, every=(50, 100), keep0=0.0, prm=None, log=None, **kw):
     from . import workloads
     from .engine import PREC_FP32_STATE
     prm = prm or default_params()
+    keys = ["mach L0", "mach L1"]
     for sd in seeds:
+        if Q.full(*keys):
+            break
         E, Hy = workloads.mach_shock(prm, seed=sd, precision=PREC_FP32_STATE, **kw)
         for s in range(steps):
             if s and s % 10 == 0:
                 Hy.regrid()
             E.step(1.0)
-            if (s + 1) % every == 0:
-                dt, _ = E.time()
-                H.take(E, 0, dt, prm, keep0, 77 + sd * 1000 + s)
+            for l in range(E.nlevels):
+                if every[l] and (s + 1) % every[l] == 0:
+                    dt, _ = E.time()
+                    Q.take(keys[l], E, l, dt, prm, keep0, 77 + sd * 1000 + s + 100000 * l)
         if log:
-            log(f"shock seed {sd}: {int(H.count.item())} rows")
+            log(f"shock seed {sd}: " + ", ".join(f"{k} {Q.got[k]}" for k in keys))
         E.close()
 
 
-def harvest_pulses(H, seeds, steps=500, every=25, keep0=0.0, prm=None, log=None):
+def harvest_pulses(Q, seeds, steps=500, every=25, keep0=0.0, prm=None, log=None):
     from . import workloads
     from .engine import PREC_FP32_STATE
     prm = prm or default_params()
     for sd in seeds:
+        if Q.full("pulses"):
+            break
         E, _, info = workloads.pulse_batch(prm, seed=sd, n=64, precision=PREC_FP32_STATE)
         for s in range(steps):
             E.step(info["dt"])
             if (s + 1) % every == 0:
-                H.take(E, 0, info["dt"], prm, keep0, 151 + sd * 1000 + s)
+                Q.take("pulses", E, 0, info["dt"], prm, keep0, 151 + sd * 1000 + s)
         if log:
-            log(f"pulses seed {sd}: {int(H.count.item())} rows")
+            log(f"pulses seed {sd}: {Q.got['pulses']} rows")
         E.close()
 
 
@@ -237,7 +286,7 @@ def _rel_errors(a, b, prm, mask=None):
     return err
 
 
-def _held_out_runs(prm, quick):
+def _held_out_runs(prm, quick, levels=LEARNED_LEVELS):
     """(name, builder(learned) -> (engine, hierarchy or None, dt, mask), steps) of the held-out evaluation:
     line source seeds 100-104 (1000 steps), the Mach shock seed 100 (400 steps), the 64 pulses (500 steps)."""
     from . import workloads
@@ -245,16 +294,19 @@ def _held_out_runs(prm, quick):
 
     def line(sd):
         def b(learned):
-            E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32_STATE, learned=learned)
+            E, Hy, _ = workloads.line_source(prm, seed=sd, precision=PREC_FP32_STATE,
+                                             learned=levels if learned else False)
             return E, Hy, 1.0, None
         return b
 
     def mach(learned):
-        E, Hy = workloads.mach_shock(prm, seed=100, precision=PREC_FP32_STATE, learned=learned)
+        E, Hy = workloads.mach_shock(prm, seed=100, precision=PREC_FP32_STATE,
+                                     learned=levels if learned else False)
         return E, Hy, 1.0, None
 
     def pulses(learned):
-        E, boxes, info = workloads.pulse_batch(prm, seed=7, n=64, precision=PREC_FP32_STATE, learned=learned)
+        E, boxes, info = workloads.pulse_batch(prm, seed=7, n=64, precision=PREC_FP32_STATE,
+                                               learned=levels if learned else False)
         ny, nx = E.level_shape(0)[1], E.level_shape(0)[0]
         mask = np.zeros((ny, nx), bool)
         for bx in boxes:
@@ -267,14 +319,14 @@ def _held_out_runs(prm, quick):
             + [("mach shock 100", mach, 400), ("pulses64", pulses, 500)])
 
 
-def evaluate(params, margin, prm=None, log=None, quick=False):
+def evaluate(params, margin, prm=None, log=None, quick=False, levels=LEARNED_LEVELS):
     """Learned vs plain-switch runs of the FP32 engine on the held-out runs at
     their full horizons: WENO fractions (level 0 and all levels), fallback
     fraction, run times and the relative L2 difference of the final level-0
     states."""
     prm = prm or default_params()
     rows = []
-    for name, build, steps in _held_out_runs(prm, quick):
+    for name, build, steps in _held_out_runs(prm, quick, levels):
         res = {}
         for learned in (False, True):
             E, Hy, dt, mask = build(learned)
@@ -307,7 +359,7 @@ def evaluate(params, margin, prm=None, log=None, quick=False):
     return rows
 
 
-def main(out_dir="sensor_out", quick=False):
+def main(out_dir="sensor_out", quick=False, levels=LEARNED_LEVELS):
     torch.cuda.set_device(0)
     torch.cuda.set_stream(torch.cuda.Stream())
     prm = default_params()
@@ -319,13 +371,13 @@ def main(out_dir="sensor_out", quick=False):
         logf.flush()
 
     H = Harvest(HARVEST_ROWS if not quick else 400_000)
+    Q = Quota(H, {k: int(v * H.cap) for k, v in HARVEST_SHARES[levels].items()})
     seeds = range(10) if not quick else range(2)
     t0 = time.perf_counter()
-    # the Mach shock flags ~6 M level-0 cells per seed and step window; it is
-    # harvested last, so the buffer's limit cuts it and not the others
-    harvest_pulses(H, PULSE_SEEDS if not quick else range(10, 11), steps=500 if not quick else 40, log=log)
-    harvest_line_source(H, seeds, steps=300 if not quick else 20, log=log)
-    harvest_shock(H, seeds, steps=400 if not quick else 40, every=50, log=log)
+    harvest_pulses(Q, PULSE_SEEDS if not quick else range(10, 11), steps=500 if not quick else 40, log=log)
+    harvest_line_source(Q, seeds, steps=300 if not quick else 20, log=log)
+    harvest_shock(Q, seeds, steps=400 if not quick else 40, log=log)
+    log("rows per source: " + json.dumps(Q.got))
     X, lab = H.rows()
     log(f"harvested {X.shape[0]} rows in {time.perf_counter() - t0:.1f} s (capacity {H.cap})")
     err = lab[:, 1]
@@ -356,15 +408,17 @@ def main(out_dir="sensor_out", quick=False):
             fp = int((pred & sure & (yv < 0.5)).sum())
             log(f"margin {mg}: decided {float(sure.float().mean()):.3f}, false-DRP {fn}, false-WENO {fp}, "
                 f"positives {int(yv.sum())}")
-        rows = evaluate(P, margin, prm=prm, log=log, quick=quick)
+        rows = evaluate(P, margin, prm=prm, log=log, quick=quick, levels=levels)
         worst = max(r["worst"] for r in rows)
-        shock = [r for r in rows if r["run"].startswith("mach")][0]
-        gain = shock["weno0_plain"] / max(1e-30, shock["weno0_learned"])
+        lines = [r for r in rows if r["run"].startswith("line")]
+        gain = float(np.mean([r["weno_plain"] / max(1e-30, r["weno_learned"]) for r in lines]))
         ok = worst <= ERR_BUDGET and all(r["health"] == (0, 0) for r in rows)
-        log(f"tau {tau}: worst rel L2 {worst:.3e}, shock level-0 WENO reduction x{gain:.3f}, accepted {ok}")
+        log(f"tau {tau}: worst rel L2 {worst:.3e}, line-source WENO work (all levels) reduction x{gain:.3f}, "
+            f"accepted {ok}")
         results.append(dict(tau=tau, margin=margin, loss=hist, eval=rows, worst=worst, gain=gain, ok=ok, P=P))
-    # the largest reduction of the shock's level-0 WENO work whose error stays
-    # inside the budget on every held-out run (none accepted: no network)
+    # the largest reduction of the line source's WENO work (all levels) whose
+    # error stays inside the budget on every held-out run (none accepted: no
+    # network)
     good = [r for r in results if r["ok"]]
     with open(os.path.join(out_dir, "sensor_report.json"), "w") as f:
         json.dump(dict(chosen_tau=(max(good, key=lambda r: r["gain"])["tau"] if good else None),
@@ -373,7 +427,7 @@ def main(out_dir="sensor_out", quick=False):
     if good:
         best = max(good, key=lambda r: r["gain"])
         np.savez(os.path.join(out_dir, "learned_sensor.npz"), params=best["P"], margin=np.float32(best["margin"]),
-                 tau=np.float64(best["tau"]), loss=np.array(best["loss"]))
+                 tau=np.float64(best["tau"]), loss=np.array(best["loss"]), levels=np.int32(levels))
         log(f"chosen tau {best['tau']}")
     else:
         log("no threshold kept every held-out run inside the budget")
@@ -386,6 +440,8 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser(description="harvest, train and evaluate the learned switch on the GPU")
     ap.add_argument("--out", default="sensor_out", help="directory for the network, log and report")
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--levels", type=int, default=LEARNED_LEVELS, choices=[1, 2],
+                    help="levels the network reviews: 1 level 0 (default), 2 every level")
     a = ap.parse_args()
     os.makedirs(a.out, exist_ok=True)
-    main(out_dir=a.out, quick=a.quick)
+    main(out_dir=a.out, quick=a.quick, levels=a.levels)

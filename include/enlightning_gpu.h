@@ -190,7 +190,10 @@ typedef struct {
   int bc[4];              /* L, R, B, T: 10 = REFLECT, 20 = ABSORB           */
   int variant;            /* ENL_* scheme id                                 */
   int precision;          /* ENL_PREC_FP64, ENL_PREC_FP32, ENL_PREC_FP32_STATE */
-  int learned;            /* 1: learned switch on level 0                    */
+  int learned;            /* 1: learned switch on level 0 (reviews the plain
+                             switch's WENO cells); 2: on every level (on the
+                             fine levels, where the reference always uses
+                             WENO, it reviews every cell); 0: off          */
   double weno_alpha, kappa, mu, muB, R, T_star_n, tau_n, c, c_lr;
   double tol[3];
   double rho0, gamma1, c_p, p0, T0, c_v;

@@ -133,8 +133,9 @@ def test_config5_pulses_500_steps_learned_and_fp32_storage_within_budget():
     prm = default_params()
     net = sensor.load_weights()
     states, mask = {}, None
-    for key, prec, learned in (("plain", PREC_FP64, False), ("learned", PREC_FP64, True),
-                               ("fp32", PREC_FP32_STATE, True)):
+    lv = sensor.weights_levels()
+    for key, prec, learned in (("plain", PREC_FP64, False), ("learned", PREC_FP64, lv),
+                               ("fp32", PREC_FP32_STATE, lv)):
         E, boxes, info = workloads.pulse_batch(prm, seed=7, n=64, precision=prec, learned=learned)
         if learned:
             E.set_mlp(*net)
@@ -155,8 +156,9 @@ def test_config3_line_source_1000_steps_learned_and_fp32_storage_within_budget()
     prm = default_params()
     net = sensor.load_weights()
     states = {}
-    for key, prec, learned in (("plain", PREC_FP64, False), ("learned", PREC_FP64, True),
-                               ("fp32", PREC_FP32_STATE, True)):
+    lv = sensor.weights_levels()
+    for key, prec, learned in (("plain", PREC_FP64, False), ("learned", PREC_FP64, lv),
+                               ("fp32", PREC_FP32_STATE, lv)):
         E, H, _ = workloads.line_source(prm, precision=prec, learned=learned)
         if learned:
             E.set_mlp(*net)

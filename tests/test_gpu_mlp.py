@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 from enlightning_gb300 import _lib, sensor, workloads  # noqa: E402
 from enlightning_gb300.constants import default_params  # noqa: E402
-from enlightning_gb300.engine import PREC_FP32, PREC_FP32_STATE  # noqa: E402
+from enlightning_gb300.engine import PREC_FP32, PREC_FP32_STATE, PREC_FP64  # noqa: E402
 
 
 def relL2(a, b):
@@ -112,13 +112,28 @@ def test_learned_with_full_margin_equals_plain(precision):
     assert np.array_equal(sa[:, :2], sb[:, :2])
 
 
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_learned_on_every_level_with_full_margin_equals_plain(precision):
+    """Review on every level (learned = 2): on the fine levels every cell's
+    plain decision is WENO and goes to the network; with a margin covering
+    every logit all of them keep it, bit for bit."""
+    prm = default_params()
+    P = sensor.init_params(0)
+    a, sa = _run(prm, False, precision=precision)
+    b, sb = _run(prm, 2, P, margin=1e30, precision=precision)
+    for l in range(2):
+        assert np.array_equal(a[l], b[l])
+    assert sb[1, 2] == sb[1, 0] == sb[1, 1] > 0  # every level-1 cell reviewed and deferred
+    assert sb[0, 2] == sb[0, 0] > 0
+
+
 @pytest.mark.skipif(not os.path.exists(sensor.WEIGHTS), reason="no trained network committed")
 @pytest.mark.parametrize("precision", [PREC_FP32, PREC_FP32_STATE])
 def test_trained_network_stays_within_budget_of_plain_switch(precision):
     prm = default_params()
     P, margin = sensor.load_weights()
     a, sa = _run(prm, False, steps=20, seed=101, precision=precision)
-    b, sb = _run(prm, True, P, margin=margin, steps=20, seed=101, precision=precision)
+    b, sb = _run(prm, sensor.weights_levels(), P, margin=margin, steps=20, seed=101, precision=precision)
     weno_plain = sa[0, 0] / max(1, sa[0, 1])
     weno_learned = sb[0, 0] / max(1, sb[0, 1])
     assert weno_learned <= weno_plain

@@ -172,3 +172,27 @@ def test_reference_build_matches_oracle_on_fresh_cases(ora):
         a = mk.run(R, "ref", kind, args, arrays)
         b = mk.run(L, "ora", kind, args, arrays)
         assert mk.digest(a) == mk.digest(b), (k, kind, args)
+
+
+def test_fp64_roofline_operation_counts_match_the_oracle(golden, ora):
+    """The FP64 roofline counts the reference algorithm's operations per cell
+    (profiles/stage_fp64_flops.json, "algorithmic"): the rhs part must be
+    what the oracle's instrumented restatement counts on WENO and DRP cells."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.dirname(__file__)), "profiles", "stage_fp64_flops.json")) as f:
+        alg = json.load(f)["algorithmic"]
+    seen = {0: set(), 1: set()}
+    for case in ("shock", "smooth", "random"):
+        c = _case(golden, case)
+        prm = _prm(c["c_lr"])
+        H0 = np.ascontiguousarray(c["H0g"][G:-G, G:-G])
+        _, flags, oc = ora.rhs("hybrid_high_llf", c["box"], (G, G), c["xlo"], c["dx"], c["w"], H0, c["pres"],
+                               c["temp"], prm, 0, flags=True, opcounts=True)
+        flags = np.asarray(flags).reshape(oc.shape[0], oc.shape[1])
+        for f in (0, 1):
+            for v in oc[flags == f]:
+                seen[f].add(int(v[0] + v[1] + v[2]))
+    assert seen[1] == {alg["rhs_weno"]} and seen[0] == {alg["rhs_drp"]}, seen
+    assert alg["weno_ops_per_cell"] == alg["rhs_weno"] + alg["runge_kutta"] + alg["update_state"]
+    assert alg["drp_ops_per_cell"] == alg["rhs_drp"] + alg["runge_kutta"] + alg["update_state"]
