@@ -7,8 +7,9 @@
   restated, all host cores): relative L2 <= 1e-12 per conserved field and on
   rho - rho0 and rho T_n - rho0 T0, or ten times the oracle's own
   sensitivity to a one-ulp change of its initial state where that is larger.
-* The 64 independent pulses (500 steps) and the 3-level line source (4096 x
-  2048 base, 1000 steps, regrid every 10 steps): the FP64 engine with the
+* The 64 independent pulses (500 steps), the Mach-1.5 shock (2 levels, 400
+  steps) and the 3-level line source (4096 x 2048 base, 1000 steps, regrid
+  every 10 steps): the FP64 engine with the
   learned switch, and the FP32-perturbation-storage engine with the learned
   switch, against the FP64 engine with the reference's switch on the same
   cadence: relative L2 <= 1e-3 per field and on the perturbation fields.
@@ -168,4 +169,25 @@ def test_config3_line_source_1000_steps_learned_and_fp32_storage_within_budget()
     for key in ("learned", "fp32"):
         errs = field_errors(states[key], states["plain"], prm)
         print("config 3, 1000 steps,", key, "vs FP64 reference switch:", errs)
+        assert max(errs.values()) <= BUDGET, (key, errs)
+
+
+def test_config2_mach_shock_400_steps_learned_and_fp32_storage_within_budget():
+    """The Mach-1.5 shock into 1 % density noise (1024x512 base, 2 levels,
+    regrid every 10 steps, device CFL time step) for its 400 steps."""
+    prm = default_params()
+    net = sensor.load_weights()
+    lv = sensor.weights_levels()
+    states = {}
+    for key, prec, learned in (("plain", PREC_FP64, False), ("learned", PREC_FP64, lv),
+                               ("fp32", PREC_FP32_STATE, lv)):
+        E, H = workloads.mach_shock(prm, seed=0, precision=prec, learned=learned)
+        if learned:
+            E.set_mlp(*net)
+        _run(E, H, 400, 1.0, 10)
+        states[key] = E.level_state(0).cpu().numpy()
+        E.close()
+    for key in ("learned", "fp32"):
+        errs = field_errors(states[key], states["plain"], prm)
+        print("config 2, 400 steps,", key, "vs FP64 reference switch:", errs)
         assert max(errs.values()) <= BUDGET, (key, errs)
