@@ -1218,8 +1218,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm (profiling)")
     ap.add_argument("--regrid-every", type=int, default=None,
                     help="regrid interval of the multi-level workloads (default: the workload's, 10)")
-    ap.add_argument("--tile-order", type=int, default=0, choices=[0, 1, 2],
-                    help="stage-kernel tile order: 0 finest level first, 1 level 0 first, 2 alternately")
+    ap.add_argument("--tile-order", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="stage-kernel tile order: 0 finest level first, 1 level 0 first, 2 alternately, "
+                         "3 two streams by block")
     ap.add_argument("--dense", action="store_true",
                     help="compute every stage tile cell by cell (no uniform-tile reuse; same states)")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2],

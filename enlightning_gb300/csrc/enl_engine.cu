@@ -268,6 +268,8 @@ struct StageArgs {
   const int4* tiles;
   const int* ntiles;
   int* counter;
+  unsigned long long* counter64;  // tile order 3: packed level-0 / finest-end claims
+  int nsm;                        // SMs (the grid's first wave of blocks)
   int* health;
   unsigned long long* stats;  // [level][4]: weno cells, cells, cells decided by the plain-sensor fallback,
                               // cells of uniform tiles stored from the cache
@@ -497,6 +499,20 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   // (neighbours in the table: the next tile to the right in a patch row),
   // then a new run from the counter
   auto claim_next = [&](int cur) -> int {
+    if (A.tile_order == 3) {
+      // two streams on one packed counter (level-0 claims in the low half,
+      // finest-end claims in the high half): the first wave of blocks (one
+      // per SM) takes tiles from the finest end of the table, the second
+      // from level 0, so an SM keeps an FP64-heavy block while fine tiles
+      // remain; a claim is valid while the streams have not met (each side's
+      // indices are distinct, and an index claimed by one side after the
+      // other claimed it would see the sum reach ntiles)
+      const bool from_end = ((blockIdx.x / A.nsm) & 1) == 0;
+      const unsigned long long old = atomicAdd(A.counter64, from_end ? (1ull << 32) : 1ull);
+      const unsigned long long f = old & 0xffffffffull, bk = old >> 32;
+      if (f + bk >= (unsigned long long)ntiles) return ntiles;
+      return from_end ? ntiles - 1 - (int)bk : (int)f;
+    }
     if (cur >= 0 && (cur + 1) % A.chunk != 0 && cur + 1 < ntiles) return cur + 1;
     return atomicAdd(A.counter, A.chunk);
   };
@@ -504,7 +520,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     // claim order -> table index (the table runs level 0 to the finest);
     // order 2 takes the two ends alternately, so that fine-level WENO tiles
     // (FP64-bound) and level-0 tiles (memory-bound) run side by side
-    const int ti = A.tile_order == 1 ? t
+    const int ti = (A.tile_order == 1 || A.tile_order == 3) ? t  // order 3 claims table indices
                    : A.tile_order == 2 ? ((t & 1) ? (t >> 1) : ntiles - 1 - (t >> 1))
                                        : ntiles - 1 - t;
     const int4 td = A.tiles[tbase + ti];
@@ -1919,7 +1935,8 @@ struct Engine {
   size_t rbox_cap = 0;
   cudaEvent_t rbox_ev = nullptr;
   int* d_meta = nullptr;
-  int* d_counters = nullptr;   // 3 stage counters
+  int* d_counters = nullptr;   // stage counters: 3 for the all-level launches, 3 per level
+  unsigned long long* d_counters64 = nullptr;  // the same, packed two-stream claims (tile order 3)
   int* d_health = nullptr;
   unsigned long long* d_stats = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -2355,6 +2372,8 @@ static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   A.ntiles = E->d_meta + (level < 0 ? M_NTILES : M_TILE_CNT + level);
   A.tile_base = level < 0 ? nullptr : E->d_meta + M_TILE_OFF + level;
   A.counter = E->d_counters + (level < 0 ? stage : 3 * (1 + level) + stage);
+  A.counter64 = E->d_counters64 + (level < 0 ? stage : 3 * (1 + level) + stage);
+  A.nsm = E->nsm;
   A.health = E->d_health;
   A.stats = E->d_stats;
   A.mlp = E->cfg.learned ? E->d_mlp : nullptr;  // null until set_mlp
@@ -2577,6 +2596,7 @@ static void record_mics(Engine* E) {
 static int step_fused(Engine* E, double dt) {
   cudaStream_t s = stream();
   cudaMemsetAsync(E->d_counters, 0, 3 * (1 + kL) * sizeof(int), s);
+  cudaMemsetAsync(E->d_counters64, 0, 3 * (1 + kL) * sizeof(unsigned long long), s);
   adaptive_dt(E, dt);
   StageFn fn = pick_stage(E->cfg.precision, E->cfg.variant);
   for (int st = 0; st < 3; ++st) {
@@ -2733,7 +2753,7 @@ extern "C" {
 int enl_engine_create(const enl_engine_config* cfg, void** out) {
   if (!cfg || !out || cfg->nlevels < 1 || cfg->nlevels > kL || cfg->ratio < 2 || cfg->nx0 < 8 || cfg->ny0 < 8 ||
       cfg->variant < 0 || cfg->variant > 8 || cfg->precision < ENL_PREC_FP64 || cfg->precision > ENL_PREC_FP32_STATE ||
-      cfg->tile_order < 0 || cfg->tile_order > 2 || cfg->learned < 0 || cfg->learned > 2 ||
+      cfg->tile_order < 0 || cfg->tile_order > 3 || cfg->learned < 0 || cfg->learned > 2 ||
       (cfg->independent && (cfg->nlevels != 1 || cfg->bc[0] == kAbsorb || cfg->bc[1] == kAbsorb ||
                             cfg->bc[2] == kAbsorb || cfg->bc[3] == kAbsorb))) {
     set_error(ENL_ERR_ARG);
@@ -2792,6 +2812,7 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMalloc(&E->d_meta, sizeof(E->h_meta));
   cudaMemset(E->d_meta, 0, sizeof(E->h_meta));
   cudaMalloc(&E->d_counters, 3 * (1 + kL) * sizeof(int));
+  cudaMalloc(&E->d_counters64, 3 * (1 + kL) * sizeof(unsigned long long));
   cudaMalloc(&E->d_health, sizeof(int));
   cudaMemset(E->d_health, 0, sizeof(int));
   cudaMalloc(&E->d_stats, 4 * kL * sizeof(unsigned long long));
@@ -2839,6 +2860,7 @@ int enl_engine_destroy(void* e) {
     }
   if (E->d_meta) cudaFree(E->d_meta);
   if (E->d_counters) cudaFree(E->d_counters);
+  if (E->d_counters64) cudaFree(E->d_counters64);
   if (E->d_health) cudaFree(E->d_health);
   if (E->d_stats) cudaFree(E->d_stats);
   for (int l = 0; l < kL; ++l)
@@ -3622,14 +3644,15 @@ int enl_engine_mic_records(void* e, void* host, long long max, long long* n, lon
 // balance is how the grid's blocks take tiles.  A schedule is
 //   [0] resident blocks per SM of the persistent grid (0: occupancy limit),
 //   [1] tile order: 0 finest level first, 1 level 0 first, 2 the two ends
-//       of the tile table alternately,
+//       of the tile table alternately, 3 two streams (each SM's first block
+//       from the finest end, its second from level 0),
 //   [2] uniform-tile reuse: 1 on (when the configuration allows it), 0 every
 //       tile computed cell by cell (results identical either way),
 //   [3] run length: a block claims this many consecutive tiles at a time
 //       (1, 2, 4: 32x8, 64x8, 128x8 cells of a patch row per claim).
 // ---------------------------------------------------------------------------
 static int apply_schedule(Engine* E, const int* v) {
-  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 2 || v[2] < 0 || v[2] > 1 || v[3] < 1 ||
+  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 3 || v[2] < 0 || v[2] > 1 || v[3] < 1 ||
       v[3] > 16)
     return ENL_ERR_ARG;
   E->sched_bps = v[0];
@@ -3746,9 +3769,11 @@ int enl_engine_autotune(void* e, double dt, int steps, int cap, int* tried, floa
   std::vector<std::array<int, 4>> cand;
   const bool reuse_ok = E->cfg.c_lr == 0.0;
   for (int bps = (E->max_blocks_per_sm + 1) / 2; bps <= E->max_blocks_per_sm; ++bps)
-    for (int order = 0; order <= 2; ++order)
+    for (int order = 0; order <= 3; ++order)
       for (int reuse = reuse_ok ? 1 : 0; reuse >= 0; --reuse)
-        for (int chunk : {1, 2, 4}) cand.push_back({bps, order, reuse, chunk});
+        for (int chunk : {1, 2, 4})
+          if (order != 3 || chunk == 1)  // the two-stream order claims single tiles
+            cand.push_back({bps, order, reuse, chunk});
   std::vector<float> best(cand.size(), 1e30f);
   int rc = ENL_OK;
   auto time_one = [&](size_t k) -> float {

@@ -215,7 +215,9 @@ typedef struct {
                              tiles: 0 (default) finest level first (the WENO
                              tiles of the fine levels start first and the
                              cheaper coarse tiles balance the end), 1 level 0
-                             first, 2 finest and level-0 tiles alternately.
+                             first, 2 finest and level-0 tiles alternately,
+                             3 two streams: each SM's first block takes tiles
+                             from the finest end, its second from level 0.
                              Every order gives the same states.            */
 } enl_engine_config;
 
@@ -344,7 +346,7 @@ int enl_engine_set_level_order(void* engine, int samrai);
 int enl_engine_set_schedule(void* engine, const int* sched, int n);
 int enl_engine_get_schedule(void* engine, int* sched, int n);
 /* Autotuner: times candidate schedules (blocks per SM in the upper half of
- * the occupancy range x the three tile orders x reuse on/off x runs of 1, 2, 4
+ * the occupancy range x the four tile orders x reuse on/off x runs of 1, 2, 4
  * tiles) on the current hierarchy and state, `steps` timed steps each after
  * one untimed step, with CUDA events on the library stream; the three
  * fastest and the schedule in force are timed again and the fastest is

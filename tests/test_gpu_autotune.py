@@ -39,7 +39,8 @@ def test_every_schedule_gives_the_same_states(precision):
     results = {}
     scheds = [None, dict(blocks_per_sm=1, tile_order=1, reuse=0, run=4), dict(blocks_per_sm=0, tile_order=0, reuse=1, run=2),
               dict(blocks_per_sm=0, tile_order=1, reuse=1, run=3), dict(blocks_per_sm=0, tile_order=2, reuse=1, run=1),
-              dict(blocks_per_sm=0, tile_order=2, reuse=0, run=4)]
+              dict(blocks_per_sm=0, tile_order=2, reuse=0, run=4), dict(blocks_per_sm=0, tile_order=3, reuse=1, run=1),
+              dict(blocks_per_sm=1, tile_order=3, reuse=0, run=1)]
     for k, sc in enumerate(scheds):
         E, H, _ = small_line_source(precision)
         if sc is not None:
