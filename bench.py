@@ -792,16 +792,43 @@ def fp64_flops_per_cell(kind="algorithmic"):
         return None, None
 
 
+KERNEL_NOTES = {
+    "interp": "coarse-fine halo interpolation (bilinear, 7 fields): halo cells written + distinct coarse "
+              "cells under their 2x2 stencils read",
+    "physbc": "physical ghost band fill (sides a stencil reads): one read and one write per band cell",
+    "coarsen": "fine-to-coarse averaging: ratio^2 fine reads + one coarse write per covered coarse cell",
+    "cfl": "CFL maximum (speed_kernel + dt_kernel): rho, rho u, rho v of every patch cell read",
+}
+
+
+def other_kernels(cls, steps, hbm_peak, peak_kind):
+    """Roofline of every other kernel class of the step from profile mode 2:
+    algorithmic bytes per launch over its event-timed duration."""
+    out = {}
+    for k, (ms, by, n) in cls.items():
+        if n == 0:
+            continue
+        gbs = by / (ms * 1e-3) / 1e9 if ms > 0 else None
+        out[k] = {"launches_per_step": n / steps, "ms_per_step": ms / steps, "ms_per_launch": ms / n,
+                  "bytes_per_launch": by / n, "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                  "frac": None if gbs is None else gbs / hbm_peak, "bound": "hbm", "peak_kind": peak_kind,
+                  "bytes": KERNEL_NOTES[k]}
+    return out
+
+
 def stage_timing(wl, which="fast", steps=3):
     """Stage-kernel launches of `steps` direct steps timed with CUDA events on
-    the engine's stream: (ms per launch, cells per launch, counters)."""
+    the engine's stream: (ms per launch, cells per launch, counters,
+    launches, {kernel class: (ms, algorithmic bytes, launches)} of the other
+    kernels of those steps)."""
     E = wl.fast if which == "fast" else wl.plain
     E.stats()
-    E.profile(True)
+    E.profile(2)
     wl.advance(which, steps, use_graph=False)
+    cls = E.profile_kernels()
     kms, kl, kcells = E.profile(False)
     st = E.stats()
-    return kms / max(1, kl), kcells / max(1, kl), st, max(1, kl)
+    return kms / max(1, kl), kcells / max(1, kl), st, max(1, kl), cls
 
 
 def run_stats_only(args):
@@ -853,7 +880,7 @@ def extra_records(args, fpk):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        kms, kcells, kst, nl = stage_timing(wl)
+        kms, kcells, kst, nl, _ = stage_timing(wl)
         dense = float(kst[:, 1].sum() - kst[:, 3].sum()) / nl
         weno = float(kst[:, 0].sum()) / nl
         flops = weno * f_weno + max(0.0, dense - weno) * f_drp if f_weno else None
@@ -1007,7 +1034,7 @@ def run_linesource(args):
         barrier()
         plain_value = cup / (p0.elapsed_time(p1) * 1e-3)
     # dominant kernel: the stage kernel, timed with events around each launch
-    per_launch_ms, cells_per_launch, kst, nl = stage_timing(wl)
+    per_launch_ms, cells_per_launch, kst, nl, kcls = stage_timing(wl)
     # 320 B per RK3 cell-update of 5 FP64 fields (106.7 B per stage launch);
     # FP32 storage moves half of it
     bytes_per_cell_launch = STEP_BYTES_PER_CELL / 3.0 * esize / 8.0
@@ -1127,6 +1154,9 @@ def run_linesource(args):
         dense_value = aggregate_rate(cud, ws, max_over_ranks(d0.elapsed_time(d1), ws))
         wl.fast.set_schedule(keep["blocks_per_sm"], keep["tile_order"], keep["reuse"], keep["run"])
         wl.graph_ok = False
+    # the step's other kernels, timed with events around each launch over the
+    # same three direct steps
+    roof["other_kernels"] = other_kernels(kcls, 3, hbm_peak, peak_kind)
     # the FP32-storage engine: its own timed region (graph replay, regrids)
     secondary = None
     if wl32 is not None:
@@ -1138,14 +1168,15 @@ def run_linesource(args):
         s1.record()
         barrier()
         ms32 = s0.elapsed_time(s1)
-        k32, c32, _, _ = stage_timing(wl32)
+        k32, c32, _, _, kcls32 = stage_timing(wl32)
         a32 = c32 * (STEP_BYTES_PER_CELL / 6.0) / (k32 * 1e-3) / 1e9
         secondary = {"dtype": "f32 (perturbation state and rhs)", "value": aggregate_rate(cu32, ws, ms32),
                      "ms_per_step": ms32 / args.steps,
                      "rel_l2_vs_plain_fp64": err32, "rel_l2_vs_fp64_same_switch": err32_fp64,
                      "compare_steps": ncmp, "stage_kernel_ms": k32, "schedule": tune32,
                      "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm_peak, "unit": "GB/s",
-                                  "frac": a32 / hbm_peak, "bytes_per_cell_launch": STEP_BYTES_PER_CELL / 6.0}}
+                                  "frac": a32 / hbm_peak, "bytes_per_cell_launch": STEP_BYTES_PER_CELL / 6.0},
+                     "other_kernels": other_kernels(kcls32, 3, hbm_peak, peak_kind)}
     if rank != 0:
         return
     health = wl.fast.health()

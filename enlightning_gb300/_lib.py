@@ -103,6 +103,8 @@ ENGINE_SIGNATURES = {
                                      C.c_void_p, C.c_void_p, C.c_long, C.c_void_p]),
     "enl_engine_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_longlong)]),
+    "enl_engine_profile_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                             C.POINTER(C.c_longlong)]),
     "enl_engine_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     "enl_engine_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     "enl_engine_download_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),

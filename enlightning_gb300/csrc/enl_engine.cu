@@ -1954,10 +1954,24 @@ struct Engine {
   int adaptive = 0;          // device-computed dt
   double cfl = 0.5;
   double* d_dt = nullptr;    // [0] = dt of the current step, [1] = simulated time
-  int profile = 0;            // time each stage-kernel launch with events
+  int profile = 0;            // 1: time each stage-kernel launch with events; 2: also the other kernels
   cudaEvent_t pev[6] = {};
   double prof_ms = 0.0;
   long long prof_launches = 0, prof_cells = 0;
+  // per-class timing of the step's other kernels (profile 2): 0 interp,
+  // 1 physical band fill, 2 coarsen, 3 CFL maximum (speed + dt)
+  static constexpr int kKev = 128;
+  cudaEvent_t kev[2 * kKev] = {};
+  int kev_cls[kKev] = {};
+  int kev_n = 0;
+  double kev_bytes[kKev] = {};
+  double kcls_ms[4] = {0, 0, 0, 0};
+  double kcls_bytes[4] = {0, 0, 0, 0};
+  long long kcls_n[4] = {0, 0, 0, 0};
+  // per level, from the tables: distinct coarse cells the halo interpolation
+  // reads, coarse cells the coarsening writes, band cells of the per-patch
+  // fill, patch cells
+  long long n_halo_coarse[kL] = {}, n_ccells[kL] = {}, n_pband[kL] = {}, n_cells[kL] = {};
   DevArray<long long> d_tileoff;
   std::vector<long long> h_tileoff;
   // host exchange (upload/download): two device staging slots per direction,
@@ -2117,6 +2131,62 @@ static void halo_segments(const std::vector<int4>& P, int nx, int ny, std::vecto
   }
 }
 
+// Coarse index of the lower of the two coarse cells a fine cell
+// interpolates from: floor((I + 1/2)/r - 1/2), as refine_weights.
+static int coarse_lo(int I, int r) {
+  const int n = 2 * I + 1 - r, d = 2 * r;
+  return n >= 0 ? n / d : -((-n + d - 1) / d);
+}
+
+// Sizes the profile mode's byte counts use, for level l of the tables.
+static void level_counts(Engine* E, int l) {
+  const int r = E->cfg.ratio;
+  long long hc = 0;
+  if (l > 0) {
+    // distinct coarse cells under the halo's 2 x 2 stencils: row intervals
+    // per coarse row, merged
+    std::vector<int3> iv;
+    const int off = E->h_meta[M_HALO_OFF + l], cnt = E->h_meta[M_HALO_CNT + l];
+    iv.reserve(2 * (size_t)cnt);
+    for (int q = off; q < off + cnt; ++q) {
+      const int4 sg = E->h_halo[q];
+      const int jc = coarse_lo(sg.x, r), a = coarse_lo(sg.y, r), b = coarse_lo(sg.z, r) + 1;
+      iv.push_back(make_int3(jc, a, b));
+      iv.push_back(make_int3(jc + 1, a, b));
+    }
+    std::sort(iv.begin(), iv.end(), [](const int3& u, const int3& v) { return u.x != v.x ? u.x < v.x : u.y < v.y; });
+    for (size_t k = 0; k < iv.size();) {
+      int row = iv[k].x, lo = iv[k].y, hi = iv[k].z;
+      for (++k; k < iv.size() && iv[k].x == row && iv[k].y <= hi + 1; ++k) hi = std::max(hi, iv[k].z);
+      hc += hi - lo + 1;
+    }
+  }
+  E->n_halo_coarse[l] = hc;
+  long long cc = 0;
+  for (int q = E->h_meta[M_CT_OFF + l]; q < E->h_meta[M_CT_OFF + l] + E->h_meta[M_CT_CNT + l]; ++q)
+    cc += (long long)((E->h_ctiles[q].z >> 8) & 0xff) * ((E->h_ctiles[q].z >> 16) & 0xff);
+  E->n_ccells[l] = cc;
+  long long pb = 0, pc = 0;
+  for (const int4& b : E->lev[l].patches) {
+    const long long w = b.y - b.x + 1, h = b.w - b.z + 1;
+    pb += 6 * (w + h) + 36;
+    pc += w * h;
+  }
+  E->n_pband[l] = pb;
+  E->n_cells[l] = pc;
+}
+
+// Band cells physbc_kernel fills on a level for a mask of sides.
+static long long band_cells(int nx, int ny, int sides) {
+  long long n = 0;
+  for (int side = 0; side < 4; ++side)
+    if (sides & (1 << side)) n += 3LL * (side < 2 ? ny : nx);
+  for (int xs = 0; xs < 2; ++xs)
+    for (int ys = 0; ys < 2; ++ys)
+      if ((sides & (1 << xs)) && (sides & (4 << ys))) n += 9;
+  return n;
+}
+
 // Host and device patch, tile, halo and coarsen tables.  Levels below
 // E->tables_from are unchanged since the last rebuild: their entries (at the
 // front of every table) are kept on the host and, unless a device table was
@@ -2169,6 +2239,7 @@ static int rebuild_tables(Engine* E) {
       }
     }
     E->h_meta[M_CT_CNT + l] = (int)E->h_ctiles.size() - E->h_meta[M_CT_OFF + l];
+    level_counts(E, l);
   }
   E->h_meta[M_NTILES] = (int)E->h_tiles.size();
   for (int l = 0; l < kL; ++l) {
@@ -2408,6 +2479,36 @@ static StageFn pick_stage(int precision, int variant) {
   return pick_stage_t<false, double>(variant);
 }
 
+// Events around one launch of a kernel class (profile mode 2, direct steps),
+// with the launch's algorithmic bytes (each cell value read or written once).
+static int kt_begin(Engine* E, int cls, double bytes) {
+  if (E->profile < 2 || E->kev_n >= Engine::kKev) return -1;
+  const int q = E->kev_n++;
+  if (!E->kev[2 * q] && (cudaEventCreate(&E->kev[2 * q]) != cudaSuccess ||
+                         cudaEventCreate(&E->kev[2 * q + 1]) != cudaSuccess)) {
+    E->kev_n = q;
+    return -1;
+  }
+  E->kev_cls[q] = cls;
+  E->kev_bytes[q] = bytes;
+  cudaEventRecord(E->kev[2 * q], stream());
+  return q;
+}
+static void kt_end(Engine* E, int q) {
+  if (q >= 0) cudaEventRecord(E->kev[2 * q + 1], stream());
+}
+static void kt_collect(Engine* E) {
+  for (int q = 0; q < E->kev_n; ++q) {
+    float ms = 0.f;
+    cudaEventSynchronize(E->kev[2 * q + 1]);
+    cudaEventElapsedTime(&ms, E->kev[2 * q], E->kev[2 * q + 1]);
+    E->kcls_ms[E->kev_cls[q]] += ms;
+    E->kcls_bytes[E->kev_cls[q]] += E->kev_bytes[q];
+    E->kcls_n[E->kev_cls[q]] += 1;
+  }
+  E->kev_n = 0;
+}
+
 template <typename S>
 static int fill_level(Engine* E, int l, int which, bool skip_unread, int src_which = -1) {
   cudaStream_t s = stream();
@@ -2417,17 +2518,26 @@ static int fill_level(Engine* E, int l, int which, bool skip_unread, int src_whi
     // coarse-fine ghosts from buffer src_which of the coarser level (the
     // same buffer unless given)
     const int src = src_which < 0 ? which : src_which;
+    // writes the halo cells, reads the coarse cells under their stencils
+    const int q = kt_begin(E, 0, (double)kNF * sizeof(S) * (E->h_meta[M_HALO_NCELL + l] + E->n_halo_coarse[l]));
     interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(src), c.ratio,
                                                 E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l,
                                                 M_HALO_NCELL + l, kNF);
+    kt_end(E, q);
   }
   if (c.independent) {
-    if (E->patch_cnt[l])
+    if (E->patch_cnt[l]) {
+      // each band cell: one source value read, one ghost written
+      const int q = kt_begin(E, 1, 2.0 * kNF * sizeof(S) * E->n_pband[l]);
       physbc_patches_kernel<S><<<dim3(kBandBlocksPerPatch, std::min(E->patch_cnt[l], 65535)), 256, 0, s>>>(
           L.view<S>(which), E->d_patchtab.p, E->patch_off[l], E->patch_cnt[l], c.bc[0], c.bc[1], c.bc[2], c.bc[3]);
+      kt_end(E, q);
+    }
   } else if (!skip_unread || E->bc_read[l]) {
+    const int q = kt_begin(E, 1, 2.0 * kNF * sizeof(S) * band_cells(L.nx, L.ny, skip_unread ? E->bc_read[l] : 15));
     physbc_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), kNF, c.bc[0], c.bc[1], c.bc[2], c.bc[3],
                                                 skip_unread ? E->bc_read[l] : 15);
+    kt_end(E, q);
   }
   return ENL_OK;
 }
@@ -2525,9 +2635,13 @@ static int absorb_all(Engine* E, int which) {
 
 template <typename S>
 static void coarsen_all_t(Engine* E) {
-  for (int l = E->cfg.nlevels - 1; l > 0; --l)
+  for (int l = E->cfg.nlevels - 1; l > 0; --l) {
+    // reads ratio^2 fine values per coarse value written
+    const int q = kt_begin(E, 2, (double)kNF * sizeof(S) * (E->cfg.ratio * E->cfg.ratio + 1) * E->n_ccells[l]);
     coarsen_kernel<S><<<E->nsm * 4, 256, 0, stream()>>>(E->lev[l - 1].view<S>(0), E->lev[l].view<S>(0), E->cfg.ratio,
                                                        E->d_ctiles.p, E->d_meta, M_CT_OFF + l, M_CT_CNT + l);
+    kt_end(E, q);
+  }
 }
 
 static int coarsen_all(Engine* E) {
@@ -2556,9 +2670,14 @@ static void speed_t(Engine* E) {
 
 static void adaptive_dt(Engine* E, double dt_max) {
   if (!E->adaptive) return;
+  // reads rho, rho u, rho v of every patch cell
+  long long cells = 0;
+  for (int l = 0; l < E->cfg.nlevels; ++l) cells += E->n_cells[l];
+  const int q = kt_begin(E, 3, 3.0 * (E->f32s ? 4 : 8) * cells);
   if (E->f32s) speed_t<float>(E);
   else speed_t<double>(E);
   dt_kernel<<<1, 1, 0, stream()>>>(E->d_smax, E->d_dt, E->d_dt + 1, reinterpret_cast<float*>(E->d_dt + 2), E->cfl * finest_dx(E), dt_max);
+  kt_end(E, q);
 }
 
 template <typename S>
@@ -2636,6 +2755,7 @@ static int step_fused(Engine* E, double dt) {
   coarsen_all(E);
   record_mics(E);
   if (E->profile) {
+    kt_collect(E);
     cudaEventSynchronize(E->pev[5]);
     long long cells = 0;
     for (auto& td : E->h_tiles) cells += (long long)((td.z >> 8) & 0xff) * ((td.z >> 16) & 0xff);
@@ -2891,6 +3011,8 @@ int enl_engine_destroy(void* e) {
   if (E->s_out) cudaStreamDestroy(E->s_out);
   for (int q = 0; q < 6; ++q)
     if (E->pev[q]) cudaEventDestroy(E->pev[q]);
+  for (int q = 0; q < 2 * Engine::kKev; ++q)
+    if (E->kev[q]) cudaEventDestroy(E->kev[q]);
   if (E->d_smax) cudaFree(E->d_smax);
   if (E->rbox_ev) {
     cudaEventSynchronize(E->rbox_ev);
@@ -3058,7 +3180,10 @@ int enl_engine_graph_capture(void* e, double dt) {
     set_error(ENL_ERR_CUDA);
     return ENL_ERR_CUDA;
   }
+  const int profile = E->profile;  // event timing waits on the host: not in a graph
+  E->profile = 0;
   step_fused(E, dt);
+  E->profile = profile;
   if (cudaStreamEndCapture(s, &g) != cudaSuccess) {
     set_error(ENL_ERR_CUDA);
     return ENL_ERR_CUDA;
@@ -4074,10 +4199,25 @@ int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, l
   E->prof_ms = 0.0;
   E->prof_launches = 0;
   E->prof_cells = 0;
+  for (int k = 0; k < 4; ++k) {
+    E->kcls_ms[k] = E->kcls_bytes[k] = 0.0;
+    E->kcls_n[k] = 0;
+  }
   if (on && !E->pev[0])
     for (int q = 0; q < 6; ++q) cudaEventCreate(&E->pev[q]);
-  E->profile = on ? 1 : 0;
+  E->profile = on <= 0 ? 0 : on >= 2 ? 2 : 1;
   return check_launch("engine profile");
+}
+
+int enl_engine_profile_kernels(void* e, double* ms, double* bytes, long long* launches) {
+  Engine* E = (Engine*)e;
+  if (!E) return ENL_ERR_ARG;
+  for (int k = 0; k < 4; ++k) {
+    if (ms) ms[k] = E->kcls_ms[k];
+    if (bytes) bytes[k] = E->kcls_bytes[k];
+    if (launches) launches[k] = E->kcls_n[k];
+  }
+  return ENL_OK;
 }
 
 int enl_engine_set_mlp(void* e, const float* params_host, float margin) {

@@ -252,11 +252,22 @@ class Engine:
                    "enl_engine_set_mlp")
 
     def profile(self, on=True):
-        """Switch stage-kernel event timing; returns (ms, launches, cells) since the last call."""
+        """Switch event timing (True or 1: stage kernels; 2: also the other
+        kernels of the step); returns (ms, launches, cells) of the stage
+        kernels since the last call and resets every profile figure."""
         ms, n, c = C.c_double(), C.c_longlong(), C.c_longlong()
         _lib.check(self.L.enl_engine_profile(self.h, int(on), C.byref(ms), C.byref(n), C.byref(c)),
                    "enl_engine_profile")
         return ms.value, n.value, c.value
+
+    KERNEL_CLASSES = ("interp", "physbc", "coarsen", "cfl")
+
+    def profile_kernels(self):
+        """{class: (ms, algorithmic bytes, launches)} of the step's other
+        kernels under profile(2), since the last profile() call."""
+        ms, by, n = (C.c_double * 4)(), (C.c_double * 4)(), (C.c_longlong * 4)()
+        _lib.check(self.L.enl_engine_profile_kernels(self.h, ms, by, n), "enl_engine_profile_kernels")
+        return {k: (ms[i], by[i], n[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 
     def packed_size(self):
         n = C.c_longlong()

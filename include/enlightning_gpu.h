@@ -316,11 +316,24 @@ int enl_engine_upload_state(void* engine, const void* host, long long host_bytes
 int enl_engine_sync(void* engine);
 
 /* Stage-kernel timing: with on = 1 every direct (not graph) enl_engine_step
- * brackets its three stage-kernel launches with CUDA events on the stream.
- * Returns (and resets) the accumulated kernel milliseconds, launches and
- * cells advanced by them since the previous call. */
+ * brackets its three stage-kernel launches with CUDA events on the stream;
+ * on = 2 also brackets every launch of the step's other kernels.  Returns
+ * (and resets, with the per-class figures below) the accumulated
+ * stage-kernel milliseconds, launches and cells advanced by them since the
+ * previous call. */
 int enl_engine_profile(void* engine, int on, double* ms_total,
                        long long* launches, long long* cells);
+
+/* Per-class figures of profile mode 2 since the last enl_engine_profile
+ * call, four entries each: 0 coarse-fine halo interpolation, 1 physical
+ * band fill, 2 coarsening, 3 CFL maximum (speed + dt kernels).  bytes are
+ * algorithmic: every cell value the launch must read or write, once
+ * (interpolation: the halo cells written and the distinct coarse cells
+ * under their 2 x 2 stencils; band fill: one read and one write per band
+ * cell; coarsening: ratio^2 fine reads and one write per coarse cell; CFL:
+ * rho, rho u, rho v of every patch cell), 7 fields of the storage type. */
+int enl_engine_profile_kernels(void* engine, double* ms, double* bytes,
+                               long long* launches);
 
 /* Stage order across levels.  samrai = 0 (default): in every RK stage all
  * levels fill their ghosts from the same stage input and advance in one

@@ -844,3 +844,40 @@ def test_cfl_speed_reduction_is_exact():
     dt, _ = E.time()
     assert dt == (0.5 * 0.05) / smax
     E.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_kernel_class_profile(precision):
+    """Profile mode 2 times every other kernel of the step by class and
+    leaves the results bit for bit as an untimed run; its algorithmic bytes
+    follow the hierarchy (coarsening: 7 fields x (4 reads + 1 write) per
+    covered coarse cell; CFL maximum: 3 fields per patch cell)."""
+    prm = default_params()
+    runs = {}
+    for mode in (0, 2):
+        E, H, _ = workloads.line_source(prm, nx0=256, ny0=128, dx0=0.5, nlevels=3, nseg=20, precision=precision,
+                                        base_patch=64)
+        E.profile(mode)
+        for _ in range(3):
+            E.step(1.0)
+        torch.cuda.synchronize()
+        cls = E.profile_kernels()
+        E.profile(False)
+        assert E.health() == 0
+        runs[mode] = ([E.canvas_state(l) for l in range(3)], cls, [list(p) for p in E.patches],
+                      4 if E.dtype == torch.float32 else 8)
+        E.close()
+    for a, b in zip(runs[0][0], runs[2][0]):
+        assert np.array_equal(a, b)
+    cls, patches, es = runs[2][1], runs[2][2], runs[2][3]
+    assert all(v == (0.0, 0.0, 0) for v in runs[0][1].values())
+    cells = [sum((b[1] - b[0] + 1) * (b[3] - b[2] + 1) for b in lv) for lv in patches]
+    assert cls["interp"][2] == 3 * 3 * 2 and cls["coarsen"][2] == 3 * 2 and cls["cfl"][2] == 3
+    assert cls["physbc"][2] >= 3 * 3
+    assert cls["coarsen"][1] == 3 * 7 * es * 5 * (cells[1] + cells[2]) // 4
+    assert cls["cfl"][1] == 3 * 3 * es * sum(cells)
+    # level 0 covers the domain: its whole band is filled every stage
+    assert cls["physbc"][1] >= 3 * 3 * 2 * 7 * es * (6 * (256 + 128) + 36)
+    assert cls["interp"][1] > 0
+    for k, (ms, by, n) in cls.items():
+        assert ms > 0, k
