@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -986,38 +987,40 @@ using CanvasView = CanvasT<double>;
 // filled when both of its sides are.
 template <typename S>
 __global__ void physbc_kernel(CanvasT<S> V, int nfields, int bcL, int bcR, int bcB, int bcT, int sides = 15) {
+  // 32-bit index arithmetic: a band holds 6 (nx + ny) + 36 cells, far below
+  // 2^31 / 7 for any canvas the engine allocates
   const int nx = V.nx, ny = V.ny;
-  const long nedge_x = 3L * ny, nedge_y = 3L * nx;
-  const long nband = 2 * nedge_x + 2 * nedge_y + 36;
-  const long total = nband * nfields;
+  const int nedge_x = 3 * ny, nedge_y = 3 * nx;
+  const int nband = 2 * nedge_x + 2 * nedge_y + 36;
+  const int total = nband * nfields;
   // field-major: neighbouring threads fill neighbouring band cells of one field
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    int k = (int)(t / nband);
-    long r = t - (long)k * nband;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int k = t / nband;
+    int r = t - k * nband;
     int i, j, si, sj;
     bool negu = false, negv = false;
     if (r < 2 * nedge_x) {
-      int side = (int)(r / nedge_x);
-      long q = r % nedge_x;
-      j = (int)(q / 3);
-      int d = (int)(q % 3);
+      int side = r >= nedge_x ? 1 : 0;
+      int q = r - side * nedge_x;
+      j = q / 3;
+      int d = q - 3 * j;
       sj = j;
       if (!(sides & (1 << side))) continue;
       if (side == 0) { i = -1 - d; si = 0; negu = bcL == kReflect; }
       else { i = nx + d; si = nx - 1; negu = bcR == kReflect; }
     } else if (r < 2 * nedge_x + 2 * nedge_y) {
       r -= 2 * nedge_x;
-      int side = (int)(r / nedge_y);
-      long q = r % nedge_y;
-      i = (int)(q / 3);
-      int d = (int)(q % 3);
+      int side = r >= nedge_y ? 1 : 0;
+      int q = r - side * nedge_y;
+      i = q / 3;
+      int d = q - 3 * i;
       si = i;
       if (!(sides & (4 << side))) continue;
       if (side == 0) { j = -1 - d; sj = 0; negv = bcB == kReflect; }
       else { j = ny + d; sj = ny - 1; negv = bcT == kReflect; }
     } else {
       r -= 2 * nedge_x + 2 * nedge_y;
-      int corner = (int)(r / 9), q = (int)(r % 9);
+      int corner = r / 9, q = r % 9;
       int dx = q % 3, dy = q / 3;
       int xs = corner & 1, ys = corner >> 1;
       if (!(sides & (1 << xs)) || !(sides & (4 << ys))) continue;
@@ -1091,30 +1094,28 @@ __global__ void physbc_patches_kernel(CanvasT<S> V, const int4* patches, int off
 // in float as well as in double (I < 2^22).
 template <typename S>
 __device__ __forceinline__ void refine_weights(int I, int r, int& ic, S& f) {
-  // fine cell centre in coarse index coordinates: (I + 0.5)/r - 0.5
-  S xc = ((S)I + (S)0.5) / (S)r - (S)0.5;
+  // fine cell centre in coarse index coordinates: (I + 0.5)/r - 0.5 (for a
+  // power-of-two ratio the product with 1/r is the same number, exactly)
+  S xc = ((r & (r - 1)) == 0 ? ((S)I + (S)0.5) * ((S)1 / (S)r) : ((S)I + (S)0.5) / (S)r) - (S)0.5;
   S fl = floor(xc);
   ic = (int)fl;
   f = xc - fl;
 }
 
-// One thread per halo cell: segment q of the level covers cells
-// [segs[q].w, segs[q].w + length) of the level's halo, found by binary
-// search, so short segments (the 3-cell rows beside a patch) keep every lane
-// busy and each thread has its 4 x nfields loads in flight together.
+// One warp per halo chunk (a row run of at most 32 cells of the level's halo,
+// the tables split longer runs), one lane per cell: a lane finds its cell
+// without a search and has its 4 x nfields loads in flight together.
+// Consecutive chunks go to different blocks, so a halo of a few hundred
+// chunks still spreads over every SM.
 template <typename S>
 __global__ void interp_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4* segs, const int* meta, int moff,
-                              int mcnt, int mncell, int nfields) {
-  const int off = meta[moff], cnt = meta[mcnt], ncell = meta[mncell];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += gridDim.x * blockDim.x) {
-    int lo = 0, hi = cnt - 1;  // last segment with .w <= t
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (segs[off + mid].w <= t) lo = mid;
-      else hi = mid - 1;
-    }
-    const int4 sg = segs[off + lo];
-    const int J = sg.x, I = sg.y + (t - sg.w);
+                              int mcnt, int nfields) {
+  const int off = meta[moff], cnt = meta[mcnt];
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int q = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; q < cnt; q += gridDim.x * wpb) {
+    const int4 sg = segs[off + q];
+    const int J = sg.x, I = sg.y + lane;
+    if (I > sg.z) continue;
     int jc, ic;
     S fy, fx;
     refine_weights(J, ratio, jc, fy);
@@ -1130,23 +1131,34 @@ __global__ void interp_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4*
 
 // Generic tile-list kernels: one block of 256 threads per 32x8 tile.
 // Coarsening: coarse cell = mean of its ratio x ratio fine cells (7 fields).
+// A block takes one field of one tile, so the few tiles a fine level covers
+// still spread over every SM; at ratio 2 a thread's four loads are issued
+// together (the sum keeps the row-major order of the general loop).
 template <typename S>
 __global__ void coarsen_kernel(CanvasT<S> C, CanvasT<S> F, int ratio, const int4* tiles, const int* meta, int moff,
                                int mcnt) {
   const int off = meta[moff], cnt = meta[mcnt];
-  for (int t = blockIdx.x; t < cnt; t += gridDim.x) {
-    int4 td = tiles[off + t];
-    int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
-    int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const S inv = (S)1 / (S)(ratio * ratio);
+  for (int t = blockIdx.x; t < cnt * kNF; t += gridDim.x) {
+    const int tile = t / kNF, k = t - tile * kNF;
+    const int4 td = tiles[off + tile];
+    const int w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     if (tx >= w || ty >= h) continue;
-    int I = td.x + tx, J = td.y + ty;
-    S inv = (S)1 / (S)(ratio * ratio);
-    for (int k = 0; k < kNF; ++k) {
-      S s = 0;
+    const int I = td.x + tx, J = td.y + ty;
+    S s = 0;
+    if (ratio == 2) {
+      const S f00 = F.at(k, 2 * I, 2 * J), f10 = F.at(k, 2 * I + 1, 2 * J);
+      const S f01 = F.at(k, 2 * I, 2 * J + 1), f11 = F.at(k, 2 * I + 1, 2 * J + 1);
+      s += f00;
+      s += f10;
+      s += f01;
+      s += f11;
+    } else {
       for (int b = 0; b < ratio; ++b)
         for (int a = 0; a < ratio; ++a) s += F.at(k, I * ratio + a, J * ratio + b);
-      C.at(k, I, J) = s * inv;
     }
+    C.at(k, I, J) = s * inv;
   }
 }
 
@@ -1507,6 +1519,7 @@ struct SpeedArgs {
   const int4* tiles;
   const int* ntiles;
   double c;
+  int ec;          // c >= 2^ec (binary exponent of c); -4096 when c is not a positive normal
   double rho_off;  // ambient density held out of the storage (0 for absolute)
   unsigned long long* smax_bits;
 };
@@ -1514,12 +1527,25 @@ struct SpeedArgs {
 // max(|rho u|, |rho v|) / |rho| is max(|u|, |v|) bit for bit (a correctly
 // rounded division is monotonic), with one division instead of two.  With
 // perturbation storage the speed is formed in single precision.  With FP64
-// storage a cell divides in FP64 only when its single-precision estimate
-// says it may hold the block's maximum (FP64 division costs about nine
-// fused multiply-adds on this GPU); the maximum is the same double.
+// storage the FP64 pipe (1/64 of the FP32 rate on this GPU, compares and
+// conversions included) is kept out of the per-cell work: magnitudes are
+// compared as integers, a quotient provably below a quarter unit in the last
+// place of c (exponents alone show it) contributes c exactly, and the rest
+// divide in FP64 only when a single-precision estimate, built from the
+// doubles' exponent and leading mantissa bits, says they may hold the block's
+// maximum (FP64 division costs about nine fused multiply-adds).  The maximum
+// is the same double as dividing every cell.
 // Each block takes kSpeedTiles tiles per pass with all their loads in flight
 // together (the pass is a chain of dependent loads: descriptor, then fields).
 constexpr int kSpeedTiles = 4;
+
+// Single-precision value of a non-negative double whose biased exponent e
+// lies in [1023 - 120, 1023 + 120]: exponent rebiased, mantissa truncated to
+// 23 bits (relative error below 2^-23, never above the double).
+__device__ __forceinline__ float f32_of_bits(unsigned long long u, int e) {
+  return __int_as_float(((e - 896) << 23) | (int)((u >> 29) & 0x7fffffu));
+}
+
 template <typename S>
 __global__ void speed_kernel(SpeedArgs<S> A) {
   __shared__ double s_w[8];
@@ -1527,7 +1553,11 @@ __global__ void speed_kernel(SpeedArgs<S> A) {
   const int n = *A.ntiles;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   double m = 0.0;
-  float m64est = 0.f;  // FP64 storage: the largest quotient estimate of the pass
+  float mf = 0.f;          // FP32 storage: the largest speed
+  bool nan_seen = false;   // FP32 storage: a NaN speed (forces a tiny dt)
+  bool zero_q = false;     // FP64 storage: a cell whose speed is exactly c
+  float m64est = 0.f;      // FP64 storage: the largest quotient estimate of the pass
+  const float roff = (float)A.rho_off, cf = (float)A.c;
   float cand_q[kSpeedTiles];
   double av[kSpeedTiles], bv[kSpeedTiles];
 #pragma unroll
@@ -1556,30 +1586,43 @@ __global__ void speed_kernel(SpeedArgs<S> A) {
 #pragma unroll
     for (int u = 0; u < kSpeedTiles; ++u) {
       if (!ok[u]) continue;
-      double s;
       if constexpr (std::is_same<S, float>::value) {
-        const float rr = (float)A.rho_off + r[u];
-        s = (double)(fmaxf(fabsf(mu[u]), fabsf(mv[u])) / fabsf(rr) + (float)A.c);
-        if (!(s == s)) s = 1e300;  // NaN state: force a tiny dt, health check reports it
-        m = fmax(m, s);
+        const float sf = fmaxf(fabsf(mu[u]), fabsf(mv[u])) / fabsf(roff + r[u]) + cf;
+        if (sf == sf) mf = fmaxf(mf, sf);
+        else nan_seen = true;
       } else {
-        // FP64: the quotient max(|rho u|, |rho v|) / |rho| is divided exactly
-        // only where it can be the largest of the block (below); here its
-        // single-precision estimate
-        const double a = fmax(fabs(mu[u]), fabs(mv[u])), b = fabs(r[u]);
-        const float qe = __fdividef((float)a, (float)b);
-        // cells whose estimate proves nothing: zero numerator (exact 0),
-        // values outside the float range, NaN, zero density
-        const bool odd = !(qe > 0.f && qe < 1e30f) || !(b > 0.0);
-        if (a == 0.0 && b > 0.0) {
-          m = fmax(m, A.c);  // quotient exactly 0: the speed is c
-        } else if (odd) {
+        constexpr unsigned long long kAbs = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
+        unsigned long long ua = (unsigned long long)__double_as_longlong(mu[u]) & kAbs;
+        unsigned long long uv = (unsigned long long)__double_as_longlong(mv[u]) & kAbs;
+        // fmax: a NaN operand yields the other one
+        if (ua > kInf) ua = uv;
+        else if (uv > kInf) uv = ua;
+        const unsigned long long qa = ua > uv ? ua : uv;
+        const unsigned long long qb = (unsigned long long)__double_as_longlong(r[u]) & kAbs;
+        const int ea = (int)(qa >> 52), eb = (int)(qb >> 52);
+        bool odd = true;
+        if (qb != 0 && qb <= kInf) {  // |rho| > 0, not NaN
+          // a < 2^(ea-1022) and b >= 2^(eb-1023) (b normal): the quotient is
+          // below 2^(ec-54), a quarter ulp of c, so q + c rounds to c
+          if (qa == 0 || (ea < 2047 && eb >= 1 && eb < 2047 && ea - eb <= A.ec - 55)) {
+            zero_q = true;
+            odd = false;
+          } else if (ea >= 903 && ea <= 1143 && eb >= 903 && eb <= 1143) {
+            const float qe = __fdividef(f32_of_bits(qa, ea), f32_of_bits(qb, eb));
+            if (qe > 0.f && qe < 1e30f) {
+              cand_q[u] = qe;
+              m64est = fmaxf(m64est, qe);
+              odd = false;
+            }
+          }
+        }
+        const double a = __longlong_as_double((long long)qa), b = __longlong_as_double((long long)qb);
+        if (odd) {
+          // outside the estimate's range: zero or subnormal density, infinite
+          // or NaN values, quotients beyond single precision
           double q = a / b;
           if (!(q == q)) q = 1e300;  // NaN state: force a tiny dt, health check reports it
           m = fmax(m, q + A.c);
-        } else {
-          cand_q[u] = qe;
-          m64est = fmaxf(m64est, qe);
         }
         av[u] = a;
         bv[u] = b;
@@ -1588,9 +1631,9 @@ __global__ void speed_kernel(SpeedArgs<S> A) {
     if constexpr (!std::is_same<S, float>::value) {
       // the block's largest estimate; a cell can hold the largest exact
       // quotient only if its estimate is within the estimates' relative error
-      // (2^-21 from the two roundings to float and the approximate division,
-      // taken here as 1e-5) of that maximum: only those divide in FP64, so
-      // the maximum is the same double as dividing everywhere
+      // (below 2^-21: two truncations to 23 mantissa bits and the approximate
+      // division; taken here as 1e-5) of that maximum: only those divide in
+      // FP64, so the maximum is the same double as dividing everywhere
       float bm = m64est;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
@@ -1608,6 +1651,12 @@ __global__ void speed_kernel(SpeedArgs<S> A) {
       }
       m64est = 0.f;
     }
+  }
+  if constexpr (std::is_same<S, float>::value) {
+    m = (double)mf;
+    if (nan_seen) m = fmax(m, 1e300);
+  } else if (zero_q) {
+    m = fmax(m, A.c);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -2222,9 +2271,15 @@ static int rebuild_tables(Engine* E) {
     E->tile_cnt[l] = (int)E->h_tiles.size() - E->tile_off[l];
     E->patch_cnt[l] = (int)E->h_patchtab.size() - E->patch_off[l];
     E->h_meta[M_HALO_OFF + l] = (int)E->h_halo.size();
-    if (l > 0) halo_segments(E->lev[l].patches, E->lev[l].nx, E->lev[l].ny, E->h_halo);
+    if (l > 0) {
+      // row runs, split into chunks of at most 32 cells (one warp each)
+      std::vector<int4> runs;
+      halo_segments(E->lev[l].patches, E->lev[l].nx, E->lev[l].ny, runs);
+      for (const int4& g : runs)
+        for (int a = g.y; a <= g.z; a += 32) E->h_halo.push_back(make_int4(g.x, a, std::min(g.z, a + 31), 0));
+    }
     E->h_meta[M_HALO_CNT + l] = (int)E->h_halo.size() - E->h_meta[M_HALO_OFF + l];
-    int ncell = 0;  // .w = halo cells of the level before this segment
+    int ncell = 0;  // .w = halo cells of the level before this chunk (for reading the tables)
     for (size_t q = E->h_meta[M_HALO_OFF + l]; q < E->h_halo.size(); ++q) {
       E->h_halo[q].w = ncell;
       ncell += E->h_halo[q].z - E->h_halo[q].y + 1;
@@ -2521,8 +2576,7 @@ static int fill_level(Engine* E, int l, int which, bool skip_unread, int src_whi
     // writes the halo cells, reads the coarse cells under their stencils
     const int q = kt_begin(E, 0, (double)kNF * sizeof(S) * (E->h_meta[M_HALO_NCELL + l] + E->n_halo_coarse[l]));
     interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(src), c.ratio,
-                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l,
-                                                M_HALO_NCELL + l, kNF);
+                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l, kNF);
     kt_end(E, q);
   }
   if (c.independent) {
@@ -2663,6 +2717,8 @@ static void speed_t(Engine* E) {
   A.tiles = E->d_tiles.p;
   A.ntiles = E->d_meta + M_NTILES;
   A.c = E->cfg.c;
+  int ec = 0;
+  A.ec = (std::isnormal(A.c) && A.c > 0.0) ? (std::frexp(A.c, &ec), ec - 1) : -4096;
   A.rho_off = E->off[0];
   A.smax_bits = E->d_smax;
   speed_kernel<S><<<E->nsm * 8, 256, 0, stream()>>>(A);

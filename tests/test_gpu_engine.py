@@ -809,20 +809,31 @@ def test_samrai_level_order_matches_oracle(ora, precision):
     assert relL2(a[0] - prm["rho0"], b[0] - prm["rho0"]) > 1e-10
 
 
-def test_cfl_speed_reduction_is_exact():
+@pytest.mark.parametrize("case", ["mixed", "tiny"])
+def test_cfl_speed_reduction_is_exact(case):
     """The FP64 CFL reduction divides only where a single-precision estimate
-    allows the block maximum; dt must still be the double that dividing every
-    cell gives: quotients tied to within 1e-9 at the top, zero velocities,
-    and both signs, on two levels."""
+    allows the block maximum, and takes c for quotients its exponents show to
+    be below a quarter ulp of c; dt must still be the double that dividing
+    every cell gives.  "mixed": quotients tied to within 1e-9 at the top,
+    zero, tiny and subnormal velocities, both signs; "tiny": every velocity
+    at most 1e-12 (zero, subnormal, and around the quarter-ulp bound), so
+    the maximum is c plus at most a few ulps.  Two levels each."""
     prm = default_params()
     nx, ny = 160, 96
     rng = np.random.default_rng(11)
     E = Engine(prm, nx, ny, (0.1, 0.1), nlevels=2, bc=(REFLECT,) * 4, precision=PREC_FP64)
     rho = prm["rho0"] * (1.0 + 0.05 * rng.uniform(-1, 1, (ny, nx)))
-    u = 40.0 * (1.0 + 1e-9 * rng.uniform(-1, 1, (ny, nx))) * rng.choice([-1.0, 1.0], (ny, nx))
-    v = 39.99999 * rng.uniform(-1, 1, (ny, nx))
-    u[:, : nx // 3] = 0.0
-    v[:, : nx // 3] = 0.0
+    tiny = np.array([0.0, 5e-324, 1e-310, 1e-300, 1e-40, 1e-20, 3e-15, 1e-14, 2e-14, 1e-13, 1e-12])
+    if case == "mixed":
+        u = 40.0 * (1.0 + 1e-9 * rng.uniform(-1, 1, (ny, nx))) * rng.choice([-1.0, 1.0], (ny, nx))
+        v = 39.99999 * rng.uniform(-1, 1, (ny, nx))
+        u[:, : nx // 3] = 0.0
+        v[:, : nx // 3] = 0.0
+        u[:, nx // 3: nx // 2] = rng.choice(tiny, (ny, nx // 2 - nx // 3)) * rng.choice([-1.0, 1.0], (ny, nx // 2 - nx // 3))
+        v[:, nx // 3: nx // 2] = rng.choice(tiny, (ny, nx // 2 - nx // 3))
+    else:
+        u = rng.choice(tiny, (ny, nx)) * rng.choice([-1.0, 1.0], (ny, nx)) * rng.uniform(0.5, 1.0, (ny, nx))
+        v = rng.choice(tiny, (ny, nx)) * rng.uniform(0.5, 1.0, (ny, nx))
     w = np.stack([rho, rho * u, rho * v, np.zeros_like(rho), rho * prm["T0"]])
     p = np.full_like(rho, prm["p0"])
     T = np.full_like(rho, prm["T0"])
