@@ -1106,10 +1106,12 @@ __device__ __forceinline__ void refine_weights(int I, int r, int& ic, S& f) {
 // the tables split longer runs), one lane per cell: a lane finds its cell
 // without a search and has its 4 x nfields loads in flight together.
 // Consecutive chunks go to different blocks, so a halo of a few hundred
-// chunks still spreads over every SM.
+// chunks still spreads over every SM.  All 4 x 7 coarse loads of a lane are
+// issued before its first store (a store could alias a later load, so the
+// compiler would not move those loads above it).
 template <typename S>
 __global__ void interp_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4* segs, const int* meta, int moff,
-                              int mcnt, int nfields) {
+                              int mcnt) {
   const int off = meta[moff], cnt = meta[mcnt];
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   for (int q = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; q < cnt; q += gridDim.x * wpb) {
@@ -1120,10 +1122,18 @@ __global__ void interp_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const int4*
     S fy, fx;
     refine_weights(J, ratio, jc, fy);
     refine_weights(I, ratio, ic, fx);
-    for (int k = 0; k < nfields; ++k) {
-      S c00 = C.at(k, ic, jc), c10 = C.at(k, ic + 1, jc), c01 = C.at(k, ic, jc + 1), c11 = C.at(k, ic + 1, jc + 1);
-      S lo_ = ((S)1 - fx) * c00 + fx * c10;
-      S hi_ = ((S)1 - fx) * c01 + fx * c11;
+    S c00[kNF], c10[kNF], c01[kNF], c11[kNF];
+#pragma unroll
+    for (int k = 0; k < kNF; ++k) {
+      c00[k] = C.at(k, ic, jc);
+      c10[k] = C.at(k, ic + 1, jc);
+      c01[k] = C.at(k, ic, jc + 1);
+      c11[k] = C.at(k, ic + 1, jc + 1);
+    }
+#pragma unroll
+    for (int k = 0; k < kNF; ++k) {
+      S lo_ = ((S)1 - fx) * c00[k] + fx * c10[k];
+      S hi_ = ((S)1 - fx) * c01[k] + fx * c11[k];
       F.at(k, I, J) = ((S)1 - fy) * lo_ + fy * hi_;
     }
   }
@@ -2576,7 +2586,7 @@ static int fill_level(Engine* E, int l, int which, bool skip_unread, int src_whi
     // writes the halo cells, reads the coarse cells under their stencils
     const int q = kt_begin(E, 0, (double)kNF * sizeof(S) * (E->h_meta[M_HALO_NCELL + l] + E->n_halo_coarse[l]));
     interp_kernel<S><<<E->nsm * 4, 256, 0, s>>>(L.view<S>(which), E->lev[l - 1].view<S>(src), c.ratio,
-                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l, kNF);
+                                                E->d_halo.p, E->d_meta, M_HALO_OFF + l, M_HALO_CNT + l);
     kt_end(E, q);
   }
   if (c.independent) {
