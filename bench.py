@@ -816,6 +816,40 @@ def other_kernels(cls, steps, hbm_peak, peak_kind):
     return out
 
 
+def host_copy_rates(nbytes, reps=3):
+    """GB/s of one pinned-host <-> device copy of `nbytes` on a side stream
+    (best of `reps`), each direction alone and both at once: what the e2e
+    leg's exchange has to hide behind the steps on this machine."""
+    import torch
+    h_in = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d_in = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d_out = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(h2d, d2h):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if h2d:
+                with torch.cuda.stream(s_up):
+                    d_in.copy_(h_in, non_blocking=True)
+            if d2h:
+                with torch.cuda.stream(s_down):
+                    h_out.copy_(d_out, non_blocking=True)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return best
+
+    out = {"bytes": nbytes, "h2d": nbytes / timed(True, False) / 1e9, "d2h": nbytes / timed(False, True) / 1e9}
+    both = timed(True, True)
+    out["both_directions_each"] = nbytes / both / 1e9
+    del h_in, h_out, d_in, d_out
+    return out
+
+
 def stage_timing(wl, which="fast", steps=3):
     """Stage-kernel launches of `steps` direct steps timed with CUDA events on
     the engine's stream: (ms per launch, cells per launch, counters,
@@ -1131,6 +1165,7 @@ def run_linesource(args):
     cue = E.cells() * ke
     e2e_value = aggregate_rate(cue, ws, e2e_ms)
     nbytes = int(n * esize)
+    copy_rates = host_copy_rates(nbytes)
     e2e5_ms, n5 = e2e_leg(E.state_host, E.download_state, E.upload_state, ke)
     e2e_conserved = {"value": aggregate_rate(cue, ws, e2e5_ms), "ms_per_step": e2e5_ms / ke,
                      "h2d_bytes_per_step": int(n5 * esize), "d2h_bytes_per_step": int(n5 * esize),
@@ -1237,7 +1272,7 @@ def run_linesource(args):
                            "interior) host->device, one RK3 step, result state device->host (pinned; two "
                            "alternating inputs and outputs; copies on the engine's copy streams overlap the "
                            "neighbouring steps; wall clock)",
-                "conserved_fields_only": e2e_conserved},
+                "conserved_fields_only": e2e_conserved, "host_copy_gbs": copy_rates},
         "clocks": clk.summary(), "gpu_launches": launches,
         "gpu_launches_counted": "kernels of the timed steps (graph replays); the regrids inside the timed "
                                 "region launch more (tagging, tag blocks, refine) and are not counted",
