@@ -1209,12 +1209,29 @@ __global__ void refine_box_kernel(CanvasT<S> F, CanvasT<S> C, int ratio, const i
 }
 
 // tag_cells.m4:58-108 over the tiles of one level, bit-exact.
+// Decided bit for bit as the reference's division would, with the estimate
+// of the hybrid switch (sensor_line_fast): two zero differences give the
+// ratio ep / ep, 1 or NaN, never below the threshold (most cells of a mostly
+// quiet level); otherwise, for a tolerance ep above 2^-1000 (num and den are
+// then normal, at least ep), an estimate num * rcp64(den) within 2^-50 of the
+// quotient decides unless it lies within 2^-44 of the threshold, and only
+// those ratios are divided.
 __device__ __forceinline__ bool ratio_below_e(double fm, double f0, double fp, double ep) {
-  double t1 = __dsub_rn(f0, fm);
-  double t2 = __dsub_rn(fp, f0);
-  double num = __dadd_rn(__dmul_rn(2.0, fabs(__dmul_rn(t1, t2))), ep);
-  double den = __dadd_rn(__dadd_rn(__dmul_rn(t1, t1), __dmul_rn(t2, t2)), ep);
-  return __ddiv_rn(num, den) < Lit::c0_9999;
+  constexpr double kLo = Lit::c0_9999 * (1.0 - 0x1p-44);
+  constexpr double kHi = Lit::c0_9999 * (1.0 + 0x1p-44);
+  const double t1 = __dsub_rn(f0, fm);
+  const double t2 = __dsub_rn(fp, f0);
+  const unsigned long long mag =
+      ((unsigned long long)__double_as_longlong(t1) | (unsigned long long)__double_as_longlong(t2)) << 1;
+  if (mag == 0ull) return false;
+  const double num = __dadd_rn(__dmul_rn(2.0, fabs(__dmul_rn(t1, t2))), ep);
+  const double den = __dadd_rn(__dadd_rn(__dmul_rn(t1, t1), __dmul_rn(t2, t2)), ep);
+  if (!(ep > 0x1p-1000)) return __ddiv_rn(num, den) < Lit::c0_9999;
+  // a positive quotient (or NaN, whose pattern is above kHi): its bit
+  // pattern orders as its value
+  const unsigned long long qb = (unsigned long long)__double_as_longlong(num * rcp64(den));
+  if (qb < (unsigned long long)__double_as_longlong(kLo)) return true;
+  return qb <= (unsigned long long)__double_as_longlong(kHi) && __ddiv_rn(num, den) < Lit::c0_9999;
 }
 
 // The same test in single precision for FP32 storage (FP64 division is slow

@@ -185,6 +185,63 @@ def test_engine_tag_bit_exact(ora):
     assert st.shape == (7, ny, nx)
 
 
+def test_engine_tag_bit_exact_near_threshold(ora):
+    """The regrid tagging decides each density ratio as the reference's
+    division would (tag_cells.m4:58-108) while dividing only ratios near the
+    0.9999 threshold: rows of sawtooth densities whose differences (t, k t)
+    put the ratio within a few 1e-14 of the threshold on both sides (the
+    estimate's window is 2^-44), random rows, and flat rows (zero
+    differences), against the oracle."""
+    prm = default_params()
+    nx, ny = 96, 48
+    f32 = lambda x: float(np.float32(x))
+    tol = prm["tol"]
+    c = f32(0.9999)
+    ep1 = ((f32(0.9) * tol[1]) * 1.0) / (1.0 - f32(0.9) * (tol[1] * tol[1]))
+
+    def ratio(t1, t2):
+        return (2.0 * abs(t1 * t2) + ep1) / ((t1 * t1 + t2 * t2) + ep1)
+
+    t = 0.05
+    lo, hi = 0.5, 1.0  # ratio(t, k t) rises to 1 at k = 1
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (mid, hi) if ratio(t, mid * t) < c else (lo, mid)
+    kstar = 0.5 * (lo + hi)
+    rng = np.random.default_rng(5)
+    rho = np.empty((ny, nx))
+    for j in range(ny):
+        if j < 36:
+            k = kstar * (1.0 + (j - 18) * 2e-15)
+            d = np.where(np.arange(nx) % 2 == 0, t, k * t)
+            rho[j] = prm["rho0"] + np.cumsum(d) - d.sum() / 2
+        elif j < 44:
+            rho[j] = prm["rho0"] * (1.0 + 0.01 * rng.normal(size=nx))
+        else:
+            rho[j] = prm["rho0"]
+    z = np.zeros_like(rho)
+    w = np.stack([rho, z, z, z, rho * prm["T0"]])
+    E = Engine(prm, nx, ny, (0.1, 0.1), nlevels=1, bc=(REFLECT,) * 4, precision=PREC_FP64)
+    E.set_level_state(0, w, np.full_like(rho, prm["p0"]), np.full_like(rho, prm["T0"]))
+    E.set_patches(0, [(0, nx - 1, 0, ny - 1)])
+    tags = E.tag(0).cpu().numpy()
+    buf = E.buffer(0, 0).cpu().numpy()
+    h0 = E.buffer(0, 3).cpu().numpy()[0]
+    E.close()
+    ref = ora.tag_cells((0, nx - 1, 0, ny - 1), (G, G), np.ascontiguousarray(buf[0:5]),
+                        np.ascontiguousarray(h0), prm["tol"])
+    assert np.array_equal(tags, ref)
+    # the rows straddle the threshold: ratios on both sides, many inside the
+    # window where only the division decides
+    r = buf[0, G:-G, :]
+    t1, t2 = r[:, 1:-1] - r[:, :-2], r[:, 2:] - r[:, 1:-1]
+    q = (2.0 * np.abs(t1 * t2) + ep1) / ((t1 * t1 + t2 * t2) + ep1)
+    near = np.abs(q[:36] / c - 1.0) < 2.0 ** -44
+    assert near.sum() > 100
+    assert (q[:36][near] < c).any() and (q[:36][near] >= c).any()
+    assert 0 < tags[:36].sum() < tags[:36].size
+
+
 def test_paint_source_matches_oracle(ora):
     """Device source painting (POINT, SINE, LIGHTNING, DRIVEN) vs the oracle
     restatement of enlightning.C:2140-2307."""
