@@ -971,7 +971,7 @@ def tune_schedule(wl, cache):
         out["candidates"] = len(ms)
         out["fastest_ms_per_step"] = ms[0][1]
         out["slowest_ms_per_step"] = ms[-1][1]
-        dflt = [t for sc, t in ms if sc["tile_order"] == 0 and sc["reuse"] == 1 and sc["run"] == 1
+        dflt = [t for sc, t in ms if sc["tile_order"] == 0 and sc["reuse"] == 2 and sc["run"] == 1
                 and sc["blocks_per_sm"] == res["schedule"]["max_blocks_per_sm"]]
         out["default_ms_per_step"] = dflt[0] if dflt else None
     return out

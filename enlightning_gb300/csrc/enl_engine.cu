@@ -280,6 +280,15 @@ struct StageArgs {
   const MlpSmem* mlp;         // learned-sensor network image (global memory) or null
   float margin;               // |p - 0.5| <= margin -> plain sensor decides
   float feat_eps, feat_eps_p, feat_inv_sqrt_eps;
+  // uniform-tile skipping (records of the current step, per table index;
+  // null when off): stage 1 writes rec_un_out and rec_out, stage 2 reads
+  // rec_in / rec_un_in and writes rec_out, stage 3 reads them; skip flags
+  // the tiles the records prove uniform (stages 2 and 3)
+  void* rec_out;
+  const void* rec_in;
+  void* rec_un_out;
+  const void* rec_un_in;
+  const unsigned char* skip;
 };
 
 // Shared-memory accessors centred on one cell of the staged halo tile.
@@ -345,6 +354,56 @@ __device__ __forceinline__ bool same_bits(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
 }
 __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
+
+// Records of one step for skipping uniform tiles.  Within a step nothing but
+// the stage kernels writes patch interiors (ghost fills write ghosts, the
+// coarsening follows the last stage), so what stage 1 and stage 2 record
+// about the tiles they wrote still holds when the next stage reads it:
+//   OutRec: the tile's stored outputs, when every cell of the tile holds the
+//           same 7 values (a uniform tile, from the cache or computed);
+//   UnRec:  the tile's u^n (5 fields) and H0, when uniform over its cells and
+//           the tile lies in no absorbing band (from stage 1's uniform test).
+// A tile of stage 2 or 3 whose own input record and its eight neighbours'
+// (all in its patch, each reaching at least 3 cells into the halo) hold the
+// same values has a uniform halo box with those values: with a matching
+// cache entry its outputs are the entry's, and the box is not loaded.
+template <typename S>
+struct alignas(16) OutRec {
+  S v[7];
+  int valid;
+};
+template <typename S>
+struct alignas(16) UnRec {
+  S v[6];  // u^n (5 fields), H0
+  int valid;
+};
+static_assert(sizeof(OutRec<double>) == 64 && sizeof(UnRec<double>) == 64, "FP64 records: 64 bytes");
+static_assert(sizeof(OutRec<float>) == 32 && sizeof(UnRec<float>) == 32, "FP32 records: 32 bytes");
+
+// Per tile: 1 when the stage's input records prove the tile's halo box
+// uniform (nbr[t] = tiles per row of its patch for a tile whose eight
+// neighbours lie in the patch, else 0).
+template <typename S>
+__global__ void skip_flags_kernel(const int* nbr, const int* ntiles, const OutRec<S>* rin, const UnRec<S>* run,
+                                  unsigned char* flag) {
+  const int n = *ntiles;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int nc = nbr[t];
+    bool ok = nc > 0 && run[t].valid != 0 && rin[t].valid != 0;
+    if (ok) {
+      const OutRec<S> c = rin[t];
+      const int q[8] = {t - nc - 1, t - nc, t - nc + 1, t - 1, t + 1, t + nc - 1, t + nc, t + nc + 1};
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const OutRec<S> r = rin[q[m]];
+        ok = ok && r.valid != 0;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) ok = ok && same_bits(r.v[k], c.v[k]);
+      }
+    }
+    flag[t] = ok ? 1 : 0;
+  }
+}
 // Input k of a uniform tile: the staged fields (0..6), u^n (7..11: the staged
 // fields 0..4 in stage 1, else the first cell's values) and H0 (12).
 template <typename S, int kPl>
@@ -455,6 +514,16 @@ __device__ __noinline__ void uniform_record(UniEntry<S>* U, const S* box, const 
   U->valid = 1;
 }
 
+// A computed uniform tile's record: the outputs of its first cell.
+template <typename S, typename W>
+__device__ __forceinline__ void record_out(OutRec<S>* ro, const W* wn, S pv, S tv) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) ro->v[k] = (S)wn[k];
+  ro->v[5] = pv;
+  ro->v[6] = tv;
+  ro->valid = 1;
+}
+
 // ---------------------------------------------------------------------------
 // Fused persistent stage kernel: per tile, TMA-stage the (32+6)x(8+6) halo box
 // of all 7 fields, decide WENO/DRP per cell, compact the cells so that each
@@ -487,6 +556,8 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_t[2];
   __shared__ int4 s_td[2];  // descriptors of the staged tiles
+  __shared__ int s_ti[2];   // their table indices
+  __shared__ int s_skip[2]; // 1: the records prove the tile uniform; its records are staged instead of its box
   __shared__ unsigned s_stats[4 * kL];
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
@@ -525,7 +596,10 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
                    : A.tile_order == 2 ? ((t & 1) ? (t >> 1) : ntiles - 1 - (t >> 1))
                                        : ntiles - 1 - t;
     const int4 td = A.tiles[tbase + ti];
+    const bool sk = A.skip != nullptr && A.skip[tbase + ti] != 0;
     s_td[b] = td;
+    s_ti[b] = tbase + ti;
+    s_skip[b] = sk ? 1 : 0;
     // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
     // doubles, a multiple of 4 for floats; set_patches only accepts such
     // patch origins and tiles are 32 wide
@@ -534,6 +608,15 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       return false;
     }
     fence_proxy_async_smem();
+    if (sk) {
+      // the tile's two records (16-byte aligned, 32 or 64 bytes each) in
+      // place of its halo box
+      constexpr uint32_t kRec = sizeof(OutRec<S>);
+      mbar_arrive_expect_tx(&mbar[b], 2 * kRec);
+      bulk_load(dst[b], static_cast<const OutRec<S>*>(A.rec_in) + tbase + ti, kRec, &mbar[b]);
+      bulk_load(dst[b] + kRec, static_cast<const UnRec<S>*>(A.rec_un_in) + tbase + ti, kRec, &mbar[b]);
+      return true;
+    }
     const int lv = td.z & 0xff;
     if constexpr (kF32S) {
       // halo box, and the interior rows of u^n (unless u^n is the input) and H0;
@@ -583,6 +666,8 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     const double* tile = reinterpret_cast<const double*>(dst[b]);  // FP64 storage
     float* tile32 = kF32S ? reinterpret_cast<float*>(dst[b]) : tile32_conv;
     const int4 td = s_td[b];
+    const int gti = s_ti[b];
+    const bool skipt = s_skip[b] != 0;
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     const int i0 = td.x, j0 = td.y;
     const int tx = lane, ty = warp;
@@ -590,7 +675,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     // u^n and H0 of this thread's cell, for the uniform-tile test: loaded
     // before the wait, so that their latency overlaps it
     S un_c[5] = {S(0), S(0), S(0), S(0), S(0)}, h0_c = S(0);
-    if (A.uniform && valid) {
+    if (A.uniform && valid && !skipt) {
       const long g = (long)(j0 + ty + 3) * A.pitch[lvl] + (i0 + tx + 3);
       h0_c = static_cast<const S*>(A.h0[lvl])[g];
       if (!A.un_is_in)
@@ -621,6 +706,66 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       break;
     }
     phase[b] ^= 1u;
+    if (skipt) {
+      // the staged records: the tile's key (its 7 input values, u^n, H0)
+      const OutRec<S>* ri = reinterpret_cast<const OutRec<S>*>(dst[b]);
+      const UnRec<S>* ru = reinterpret_cast<const UnRec<S>*>(dst[b] + sizeof(OutRec<S>));
+      S kv[13];
+#pragma unroll
+      for (int k = 0; k < 13; ++k) kv[k] = k < 7 ? ri->v[k] : ru->v[k - 7];
+      const UniEntry<S>& U = s_uc[lvl];
+      bool hit = U.valid != 0;
+#pragma unroll
+      for (int k = 0; k < 13; ++k) hit = hit && same_bits(kv[k], U.key[k]);
+      if (hit) {
+        // the block's cached outputs for this key, as uniform_hit stores them
+        if (valid) {
+          S* out = static_cast<S*>(A.out[lvl]);
+          const long fs = A.fstride[lvl];
+          const long gc = (long)(j0 + ty + 3) * A.pitch[lvl] + (i0 + tx + 3);
+#pragma unroll
+          for (int k = 0; k < kNF; ++k) out[k * fs + gc] = U.res[k];
+        }
+        if (tid == 0) {
+          s_stats[4 * lvl + 0] += U.weno ? (unsigned)(w * h) : 0u;
+          s_stats[4 * lvl + 1] += (unsigned)(w * h);
+          s_stats[4 * lvl + 3] += (unsigned)(w * h);
+          if (A.rec_out) {
+            OutRec<S>* ro = static_cast<OutRec<S>*>(A.rec_out) + gti;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) ro->v[k] = U.res[k];
+            ro->valid = 1;
+          }
+        }
+        __syncthreads();  // this staging buffer is refilled two tiles later
+        t = s_t[b ^ 1];
+        b ^= 1;
+        continue;
+      }
+      // not in the block's cache: build the box the records describe (one
+      // value per field; u^n and H0 where they are staged) and take the full
+      // path, which computes the tile and fills the cache entry
+      __syncthreads();  // every thread holds the key before the records are overwritten
+      S* box = reinterpret_cast<S*>(dst[b]);
+      constexpr int kPlB = kF32S ? kPlane32 : kBH * kBW;
+#pragma unroll
+      for (int k = 0; k < kNF; ++k)
+        for (int e = tid; e < kPlB; e += 256) box[k * kPlB + e] = kv[k];
+      if constexpr (kF32S && kUnTma) {
+        float* unb = reinterpret_cast<float*>(dst[b] + kTile32Bytes);
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+          for (int e = tid; e < kTH * kBW32; e += 256) unb[k * (kTH * kBW32) + e] = kv[7 + k];
+        float* h0b = reinterpret_cast<float*>(dst[b] + kTile32Bytes + kUnBytes);
+        for (int e = tid; e < kTH * kBW32; e += 256) h0b[e] = kv[12];
+      }
+      if (valid) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) un_c[k] = kv[7 + k];
+        h0_c = kv[12];
+      }
+      __syncthreads();
+    }
     // beta*dt of this stage (dt from the device CFL reduction when adaptive)
     const double bdt = kF32S ? 0.0 : (A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt);
     if (tid == 0) {
@@ -638,6 +783,22 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
                                                                  un_c[3], un_c[4], h0_c);
       const bool all = __syncthreads_and(ok) != 0;  // (also publishes s_tile and s_wl)
       if (all && s_tile.absorb == 0) ucode = uniform_hit<S, kPl>(A, box, s_uc, s_wl, s_stats, lvl, i0, j0, w, h);
+      // this step's records of the tile (a computed uniform tile, ucode 2,
+      // records its outputs where its first cell records the cache entry)
+      if (tid == 0 && A.rec_un_out) {
+        UnRec<S>* rn = static_cast<UnRec<S>*>(A.rec_un_out) + gti;
+        if (ucode != 0)
+#pragma unroll
+          for (int k = 0; k < 6; ++k) rn->v[k] = uni_key<S, kPl>(box, s_wl[0], A.un_is_in, 7 + k);
+        rn->valid = ucode != 0 ? 1 : 0;
+      }
+      if (tid == 0 && A.rec_out && ucode != 2) {
+        OutRec<S>* ro = static_cast<OutRec<S>*>(A.rec_out) + gti;
+        if (ucode == 1)
+#pragma unroll
+          for (int k = 0; k < 7; ++k) ro->v[k] = s_uc[lvl].res[k];
+        ro->valid = ucode == 1 ? 1 : 0;
+      }
     }
     // a uniform tile whose outputs came from the cache (ucode 1) goes to the
     // end of the tile; one missing from the cache (ucode 2) is computed in
@@ -884,9 +1045,11 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
           for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
           out[5 * fs + g] = pq;
           out[6 * fs + g] = tp;
-          if (record)
+          if (record) {
             uniform_record<S, kPl>(&s_uc[lvl], reinterpret_cast<const S*>(dst[b]), s_wl[0], A.un_is_in, wn[0], wn[1],
                                    wn[2], wn[3], wn[4], pq, tp, f);
+            if (A.rec_out) record_out<S>(static_cast<OutRec<S>*>(A.rec_out) + gti, wn, pq, tp);
+          }
           if (!(rho > 0.f) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
         } else {
           const double* un = static_cast<const double*>(A.un[lvl]);
@@ -948,9 +1111,11 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
           out[6 * fs + g] = tv;
 #pragma unroll
           for (int k = 0; k < 5; ++k) out[k * fs + g] = wn[k];
-          if (record)
+          if (record) {
             uniform_record<S, kPl>(&s_uc[lvl], reinterpret_cast<const S*>(dst[b]), s_wl[0], A.un_is_in, wn[0], wn[1],
                                    wn[2], wn[3], wn[4], pv, tv, f);
+            if (A.rec_out) record_out<S>(static_cast<OutRec<S>*>(A.rec_out) + gti, wn, pv, tv);
+          }
           if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4]))
             raise_health(A.health, ENL_ERR_NONFINITE);
         }
@@ -2089,6 +2254,13 @@ struct Engine {
   int max_blocks_per_sm = 1;
   int sched_bps = 0;  // 0: max_blocks_per_sm
   int sched_chunk = 1;
+  // uniform-tile skipping in stages 2 and 3 (with reuse): per tile the
+  // neighbour stride (tiles per row of its patch, 0 when a neighbour lies
+  // outside the patch), this step's records and the skip flags
+  int skip = 1;
+  DevArray<int> d_nbr;
+  std::vector<int> h_nbr;
+  DevArray<unsigned char> d_rec_o1, d_rec_o2, d_rec_un, d_skip;
   // storage: FP64 absolute values, or FP32 perturbations about the ambient
   // state (absolute = off[k] + stored)
   bool f32s = false;
@@ -2207,6 +2379,21 @@ static void halo_segments(const std::vector<int4>& P, int nx, int ny, std::vecto
   }
 }
 
+// Neighbour strides of the tiles tiles_of_box makes for box b, in its order:
+// the patch's tiles per row for a tile whose eight neighbours are tiles of
+// the same patch reaching at least 3 cells (the stencil) into its halo box,
+// else 0.
+static void nbr_of_box(int4 b, std::vector<int>& out) {
+  const int W = b.y - b.x + 1, H = b.w - b.z + 1;
+  const int nc = (W + kTW - 1) / kTW, nr = (H + kTH - 1) / kTH;
+  for (int r = 0; r < nr; ++r)
+    for (int c = 0; c < nc; ++c) {
+      const bool inner = c >= 1 && r >= 1 && c + 1 < nc && r + 1 < nr &&
+                         std::min(kTW, W - kTW * (c + 1)) >= 3 && std::min(kTH, H - kTH * (r + 1)) >= 3;
+      out.push_back(inner ? nc : 0);
+    }
+}
+
 // Coarse index of the lower of the two coarse cells a fine cell
 // interpolates from: floor((I + 1/2)/r - 1/2), as refine_weights.
 static int coarse_lo(int I, int r) {
@@ -2284,6 +2471,7 @@ static int rebuild_tables(Engine* E) {
   const size_t keep_ct = l0 < nl ? (size_t)E->h_meta[M_CT_OFF + l0] : E->h_ctiles.size();
   E->h_tiles.resize(keep_tiles);
   E->h_tileoff.resize(keep_tiles);
+  E->h_nbr.resize(keep_tiles);
   E->h_patchtab.resize(keep_pt);
   E->h_halo.resize(keep_halo);
   E->h_ctiles.resize(keep_ct);
@@ -2293,6 +2481,7 @@ static int rebuild_tables(Engine* E) {
     for (auto& b : E->lev[l].patches) {
       // tile .w = index of the patch in the all-level patch table
       tiles_of_box(b, l, (int)E->h_patchtab.size(), E->h_tiles);
+      nbr_of_box(b, E->h_nbr);
       E->h_patchtab.push_back(b);
     }
     E->tile_cnt[l] = (int)E->h_tiles.size() - E->tile_off[l];
@@ -2370,7 +2559,21 @@ static int rebuild_tables(Engine* E) {
   grew |= E->d_halo.ensure(std::max<size_t>(E->h_halo.size(), 1));
   grew |= E->d_ctiles.ensure(std::max<size_t>(E->h_ctiles.size(), 1));
   grew |= E->d_patchtab.ensure(std::max<size_t>(E->h_patchtab.size(), 1));
+  {
+    const size_t nt = std::max<size_t>(E->h_tiles.size(), 1), rb = E->f32s ? 32 : 64;
+    grew |= E->d_nbr.ensure(nt);
+    grew |= E->d_skip.ensure(nt);
+    grew |= E->d_rec_o1.ensure(nt * rb);
+    grew |= E->d_rec_o2.ensure(nt * rb);
+    grew |= E->d_rec_un.ensure(nt * rb);
+  }
   if (grew) E->graph_valid = false;
+  if (!E->d_nbr.p || !E->d_skip.p || !E->d_rec_o1.p || !E->d_rec_o2.p || !E->d_rec_un.p) {
+    E->tables_on_device = false;
+    E->graph_valid = false;
+    set_error(ENL_ERR_CUDA);
+    return ENL_ERR_CUDA;
+  }
   if (!E->d_tileoff.p || !E->d_tiles.p || !E->d_halo.p || !E->d_ctiles.p || !E->d_patchtab.p) {
     E->tables_on_device = false;
     E->graph_valid = false;
@@ -2384,11 +2587,12 @@ static int rebuild_tables(Engine* E) {
                k_ct = keep_dev ? keep_ct : 0, k_pt = keep_dev ? keep_pt : 0;
   // one pinned staging buffer for all tables, copied asynchronously; the
   // previous rebuild's copies must have left it before it is rewritten
+  const size_t b_nbr = (E->h_nbr.size() - k_tiles) * sizeof(int);
   const size_t b_off = (E->h_tileoff.size() - k_tiles) * sizeof(long long),
                b_tiles = (E->h_tiles.size() - k_tiles) * sizeof(int4),
                b_halo = (E->h_halo.size() - k_halo) * sizeof(int4), b_ct = (E->h_ctiles.size() - k_ct) * sizeof(int4),
                b_pt = (E->h_patchtab.size() - k_pt) * sizeof(int4), b_meta = sizeof(E->h_meta);
-  const size_t need = b_off + b_tiles + b_halo + b_ct + b_pt + b_meta;
+  const size_t need = b_nbr + b_off + b_tiles + b_halo + b_ct + b_pt + b_meta;
   if (E->stage_ev) cudaEventSynchronize(E->stage_ev);
   if (need > E->stage_cap) {
     if (E->stage_host) cudaFreeHost(E->stage_host);
@@ -2410,6 +2614,7 @@ static int rebuild_tables(Engine* E) {
     h += n;
   };
   put(E->d_tileoff.p + k_tiles, E->h_tileoff.data() + k_tiles, b_off);
+  put(E->d_nbr.p + k_tiles, E->h_nbr.data() + k_tiles, b_nbr);
   put(E->d_tiles.p + k_tiles, E->h_tiles.data() + k_tiles, b_tiles);
   put(E->d_halo.p + k_halo, E->h_halo.data() + k_halo, b_halo);
   put(E->d_ctiles.p + k_ct, E->h_ctiles.data() + k_ct, b_ct);
@@ -2444,6 +2649,10 @@ static EosConst64 eos_const64(const enl_engine_config& c) {
 
 // level < 0: the launch covers every tile of every level; otherwise the
 // tiles of that level only (the per-level stage order)
+// Uniform-tile skipping: with uniform-tile reuse (c_lr = 0, not dense) and
+// the schedule's skipping on.
+static bool skip_on(const Engine* E) { return E->skip && !E->cfg.dense && E->cfg.c_lr == 0.0; }
+
 static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   StageArgs A;
   memset(&A, 0, sizeof(A));
@@ -2535,7 +2744,34 @@ static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   A.feat_eps = (float)A.P[0].sensor_eps;
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
   A.feat_inv_sqrt_eps = (float)(1.0 / sqrt(A.P[0].sensor_eps));
+  if (skip_on(E)) {
+    // stage 1 records its outputs and u^n / H0; stage 2 reads stage 1's
+    // records and records its own; stage 3 reads stage 2's
+    if (stage == 0) {
+      A.rec_out = E->d_rec_o1.p;
+      A.rec_un_out = E->d_rec_un.p;
+    } else {
+      A.rec_in = stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p;
+      A.rec_un_in = E->d_rec_un.p;
+      A.rec_out = stage == 1 ? E->d_rec_o2.p : nullptr;
+      A.skip = E->d_skip.p;
+    }
+  }
   return A;
+}
+
+// The skip flags of stage `stage` (1 or 2) from the records of the previous
+// stage, for every tile of every level.
+static void skip_flags(Engine* E, int stage) {
+  const unsigned char* rin = stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p;
+  if (E->f32s)
+    skip_flags_kernel<float><<<E->nsm * 2, 256, 0, stream()>>>(
+        E->d_nbr.p, E->d_meta + M_NTILES, reinterpret_cast<const OutRec<float>*>(rin),
+        reinterpret_cast<const UnRec<float>*>(E->d_rec_un.p), E->d_skip.p);
+  else
+    skip_flags_kernel<double><<<E->nsm * 2, 256, 0, stream()>>>(
+        E->d_nbr.p, E->d_meta + M_NTILES, reinterpret_cast<const OutRec<double>*>(rin),
+        reinterpret_cast<const UnRec<double>*>(E->d_rec_un.p), E->d_skip.p);
 }
 
 typedef void (*StageFn)(StageArgs);
@@ -2804,6 +3040,7 @@ static int step_fused(Engine* E, double dt) {
   for (int st = 0; st < 3; ++st) {
     int in = st == 0 ? 0 : st;
     int out = st == 2 ? 0 : st + 1;
+    if (st > 0 && skip_on(E)) skip_flags(E, st);
     if (E->samrai_order) {
       // SAMRAI's MethodOfLinesIntegrator order (main.C:448): per stage the
       // levels coarsest first, each filling its ghosts -- coarse-fine ones
@@ -3354,6 +3591,22 @@ int enl_engine_stats(void* e, long long* counts) {
   return check_launch("engine stats");
 }
 
+int enl_engine_skipped_tiles(void* e, long long* flagged, long long* tiles) {
+  Engine* E = (Engine*)e;
+  if (!E || !flagged) return ENL_ERR_ARG;
+  const size_t n = E->h_tiles.size();
+  *flagged = 0;
+  if (tiles) *tiles = (long long)n;
+  if (!skip_on(E) || n == 0 || !E->d_skip.p) return ENL_OK;
+  std::vector<unsigned char> h(n);
+  cudaMemcpyAsync(h.data(), E->d_skip.p, n, cudaMemcpyDeviceToHost, stream());
+  cudaStreamSynchronize(stream());
+  long long c = 0;
+  for (unsigned char v : h) c += v ? 1 : 0;
+  *flagged = c;
+  return check_launch("engine skipped tiles");
+}
+
 int enl_engine_health(void* e) {
   Engine* E = (Engine*)e;
   if (!E) return ENL_ERR_ARG;
@@ -3380,7 +3633,8 @@ int enl_engine_launches_per_step(void* e, int plain) {
     // ghosts rebuilt before each finer level (a band fill, and an
     // interpolation below level 1)
     const int refresh = E->samrai_order ? (nl - 1) + (nl > 2 ? nl - 2 : 0) : 0;
-    return 3 * (bands + (nl - 1) + (E->samrai_order ? nl : 1) + refresh) + (nl - 1) + dt;
+    return 3 * (bands + (nl - 1) + (E->samrai_order ? nl : 1) + refresh) + (nl - 1) + dt +
+           (skip_on(E) ? 2 : 0);  // the skip flags of stages 2 and 3
   }
   const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;
@@ -3854,18 +4108,21 @@ int enl_engine_mic_records(void* e, void* host, long long max, long long* n, lon
 //   [1] tile order: 0 finest level first, 1 level 0 first, 2 the two ends
 //       of the tile table alternately, 3 two streams (each SM's first block
 //       from the finest end, its second from level 0),
-//   [2] uniform-tile reuse: 1 on (when the configuration allows it), 0 every
-//       tile computed cell by cell (results identical either way),
+//   [2] uniform-tile reuse: 2 on, with stages 2 and 3 skipping the halo box
+//       of tiles this step's records prove uniform; 1 on, every box loaded
+//       and tested; 0 every tile computed cell by cell (results identical
+//       in all three),
 //   [3] run length: a block claims this many consecutive tiles at a time
 //       (1, 2, 4: 32x8, 64x8, 128x8 cells of a patch row per claim).
 // ---------------------------------------------------------------------------
 static int apply_schedule(Engine* E, const int* v) {
-  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 3 || v[2] < 0 || v[2] > 1 || v[3] < 1 ||
+  if (v[0] < 0 || v[0] > E->max_blocks_per_sm || v[1] < 0 || v[1] > 3 || v[2] < 0 || v[2] > 2 || v[3] < 1 ||
       v[3] > 16)
     return ENL_ERR_ARG;
   E->sched_bps = v[0];
   E->cfg.tile_order = v[1];
   E->cfg.dense = v[2] ? 0 : 1;
+  E->skip = v[2] == 2 ? 1 : 0;
   E->sched_chunk = v[3];
   E->stage_blocks = E->nsm * (v[0] ? v[0] : E->max_blocks_per_sm);
   E->graph_valid = false;  // grid size and kernel arguments change
@@ -3875,7 +4132,7 @@ static int apply_schedule(Engine* E, const int* v) {
 static void get_schedule(const Engine* E, int* v) {
   v[0] = E->sched_bps ? E->sched_bps : E->max_blocks_per_sm;
   v[1] = E->cfg.tile_order;
-  v[2] = E->cfg.dense ? 0 : 1;
+  v[2] = E->cfg.dense ? 0 : (E->skip ? 2 : 1);
   v[3] = E->sched_chunk;
 }
 
@@ -3972,15 +4229,16 @@ int enl_engine_autotune(void* e, double dt, int steps, int cap, int* tried, floa
   int current[4];
   get_schedule(E, current);
   save_restore(true);
-  // candidates: the upper half of the occupancy range, the three orders, reuse on
-  // and off (when the configuration allows reuse), runs of 1, 2, 4 tiles
+  // candidates: the upper half of the occupancy range, the four orders, reuse
+  // with skipping and off (and reuse without skipping on single-tile runs)
+  // when the configuration allows reuse, runs of 1, 2, 4 tiles
   std::vector<std::array<int, 4>> cand;
   const bool reuse_ok = E->cfg.c_lr == 0.0;
   for (int bps = (E->max_blocks_per_sm + 1) / 2; bps <= E->max_blocks_per_sm; ++bps)
     for (int order = 0; order <= 3; ++order)
-      for (int reuse = reuse_ok ? 1 : 0; reuse >= 0; --reuse)
+      for (int reuse = reuse_ok ? 2 : 0; reuse >= 0; --reuse)
         for (int chunk : {1, 2, 4})
-          if (order != 3 || chunk == 1)  // the two-stream order claims single tiles
+          if ((order != 3 || chunk == 1) && (reuse != 1 || chunk == 1))  // the two-stream order claims single tiles
             cand.push_back({bps, order, reuse, chunk});
   std::vector<float> best(cand.size(), 1e30f);
   int rc = ENL_OK;

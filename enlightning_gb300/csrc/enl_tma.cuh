@@ -86,4 +86,14 @@ __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* m
       : "memory");
 }
 
+// Untiled bulk copy global -> shared (cp.async.bulk): both addresses 16-byte
+// aligned and bytes a multiple of 16; completion signalled on an mbarrier.
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(static_cast<uint64_t>(__cvta_generic_to_global(gsrc))), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 }  // namespace enl

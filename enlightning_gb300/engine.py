@@ -152,7 +152,7 @@ class Engine:
         out["max_blocks_per_sm"] = v[4]
         return out
 
-    def set_schedule(self, blocks_per_sm=0, tile_order=0, reuse=1, run=1):
+    def set_schedule(self, blocks_per_sm=0, tile_order=0, reuse=2, run=1):
         v = (C.c_int * 4)(int(blocks_per_sm), int(tile_order), int(reuse), int(run))
         _lib.check(self.L.enl_engine_set_schedule(self.h, v, 4), "enl_engine_set_schedule")
 
@@ -235,6 +235,12 @@ class Engine:
         _lib.check(self.L.enl_engine_stats(self.h, arr), "enl_engine_stats")
         a = np.array(arr[:], dtype=np.int64).reshape(MAX_LEVELS, 4)
         return a[: self.nlevels]
+
+    def skipped_tiles(self):
+        """(tiles the last step's stage 3 took without their halo box, tiles)."""
+        f, n = C.c_longlong(), C.c_longlong()
+        _lib.check(self.L.enl_engine_skipped_tiles(self.h, C.byref(f), C.byref(n)), "enl_engine_skipped_tiles")
+        return f.value, n.value
 
     def health(self):
         return int(self.L.enl_engine_health(self.h))

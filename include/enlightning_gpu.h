@@ -269,6 +269,11 @@ int enl_engine_tag(void* engine, int level, int* tags);
  * uniform tiles whose outputs came from the block's cache (host array of
  * 4*ENL_MAX_LEVELS long long), then reset. */
 int enl_engine_stats(void* engine, long long* counts);
+/* Tiles the last step's RK stage 3 took without loading their halo box
+ * (uniform-tile reuse 2: the records of stage 2 proved them uniform), and
+ * the tiles of the hierarchy (tiles may be NULL).  Synchronises the library
+ * stream.  0 when skipping is off. */
+int enl_engine_skipped_tiles(void* engine, long long* flagged, long long* tiles);
 /* Health word: 0, or the first code a kernel raised since the last call:
  * ENL_ERR_NONFINITE (rho <= 0 or non-finite state), ENL_ERR_TIMEOUT (a
  * bounded wait gave up), ENL_ERR_STATE (a TMA precondition failed and the
@@ -349,7 +354,11 @@ int enl_engine_set_level_order(void* engine, int samrai);
  * and the schedule decides how its blocks take the tiles.
  *   sched[0] resident blocks per SM (0 = the occupancy limit),
  *   sched[1] tile order (as enl_engine_config.tile_order),
- *   sched[2] uniform-tile reuse: 1 on, 0 off (as enl_engine_config.dense = 1),
+ *   sched[2] uniform-tile reuse: 2 on (the default), with RK stages 2 and 3
+ *            skipping the halo box of a tile whose own and neighbours'
+ *            records from the previous stage of the step prove it uniform;
+ *            1 on, every tile's box loaded and tested; 0 off (as
+ *            enl_engine_config.dense = 1),
  *   sched[3] run length: tiles a block claims at a time (1..16; consecutive
  *            tiles of a patch row, so 2 and 4 claim 64x8 and 128x8 cells).
  * Every schedule gives the same states.  Setting one invalidates a captured
@@ -359,8 +368,8 @@ int enl_engine_set_level_order(void* engine, int samrai);
 int enl_engine_set_schedule(void* engine, const int* sched, int n);
 int enl_engine_get_schedule(void* engine, int* sched, int n);
 /* Autotuner: times candidate schedules (blocks per SM in the upper half of
- * the occupancy range x the four tile orders x reuse on/off x runs of 1, 2, 4
- * tiles) on the current hierarchy and state, `steps` timed steps each after
+ * the occupancy range x the four tile orders x reuse 2 and 0 x runs of 1, 2, 4
+ * tiles, and reuse 1 with runs of 1) on the current hierarchy and state, `steps` timed steps each after
  * one untimed step, with CUDA events on the library stream; the three
  * fastest and the schedule in force are timed again and the fastest is
  * applied.  The current canvases, time step, simulated time, statistics and

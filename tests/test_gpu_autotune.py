@@ -98,3 +98,32 @@ def test_autotune_leaves_the_state_and_is_no_slower_than_default(tmp_path):
     for a, b in zip(tuned_state, states(E2)):
         assert np.array_equal(a, b)
     E2.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
+def test_skipping_uniform_tiles_changes_nothing(precision):
+    """Reuse 2 takes the tiles that the previous stage's records prove
+    uniform without loading their halo boxes; a line source run (regrids
+    included) and an ambient hierarchy step bit for bit as with reuse 1 and
+    0, and the ambient run skips most of its tiles."""
+    results = {}
+    for reuse in (2, 1, 0):
+        E, H, _ = small_line_source(precision)
+        E.set_schedule(blocks_per_sm=0, tile_order=3, reuse=reuse, run=1)
+        for s in range(6):
+            if s == 3:
+                H.regrid()
+            E.step(1.0)
+        torch.cuda.synchronize()
+        assert E.health() == 0
+        skipped, tiles = E.skipped_tiles()
+        results[reuse] = (states(E), E.time(), E.stats(), skipped, tiles)
+        E.close()
+    for reuse in (1, 0):
+        assert results[reuse][1] == results[2][1]
+        for a, b in zip(results[reuse][0], results[2][0]):
+            assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a,
+                                  b.view(np.int64) if b.dtype == np.float64 else b), reuse
+    assert results[1][3] == 0 and results[0][3] == 0
+    print("line source: stage 3 skipped", results[2][3], "of", results[2][4], "tiles")
+    assert results[2][3] > 0
