@@ -280,15 +280,16 @@ struct StageArgs {
   const MlpSmem* mlp;         // learned-sensor network image (global memory) or null
   float margin;               // |p - 0.5| <= margin -> plain sensor decides
   float feat_eps, feat_eps_p, feat_inv_sqrt_eps;
-  // uniform-tile skipping (records of the current step, per table index;
-  // null when off): stage 1 writes rec_un_out and rec_out, stage 2 reads
-  // rec_in / rec_un_in and writes rec_out, stage 3 reads them; skip flags
-  // the tiles the records prove uniform (stages 2 and 3)
+  // uniform-tile skipping (null when off).  Records of the current step,
+  // per table index: stage 1 writes rec_un_out and rec_out, stage 2 writes
+  // rec_out.  In stages 2 and 3 the launch runs over a list of tiles: tiles
+  // holds their descriptors, gti their table indices (null: the table
+  // itself), and the first uniform tile computed per level is published in
+  // gcache (GUni<S>[kL]) for the writer of the skipped tiles.
   void* rec_out;
-  const void* rec_in;
   void* rec_un_out;
-  const void* rec_un_in;
-  const unsigned char* skip;
+  const int* gti;
+  void* gcache;
 };
 
 // Shared-memory accessors centred on one cell of the staged halo tile.
@@ -382,14 +383,20 @@ static_assert(sizeof(OutRec<float>) == 32 && sizeof(UnRec<float>) == 32, "FP32 r
 
 // Per tile: 1 when the stage's input records prove the tile's halo box
 // uniform (nbr[t] = tiles per row of its patch for a tile whose eight
-// neighbours lie in the patch, else 0).
+// neighbours lie in the patch, else 0).  Block b takes tiles [256 b, 256 b +
+// 256) and writes its count of tiles to compute and to skip to bcnt[b].
+constexpr int kFlagThreads = 256;
 template <typename S>
-__global__ void skip_flags_kernel(const int* nbr, const int* ntiles, const OutRec<S>* rin, const UnRec<S>* run,
-                                  unsigned char* flag) {
+__global__ void __launch_bounds__(kFlagThreads) skip_flags_kernel(const int* nbr, const int* ntiles,
+                                                                  const OutRec<S>* rin, const UnRec<S>* run,
+                                                                  unsigned char* flag, int2* bcnt) {
   const int n = *ntiles;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+  const int t = blockIdx.x * kFlagThreads + threadIdx.x;
+  if (blockIdx.x * kFlagThreads >= n) return;  // (the whole block: no barrier below is left half-way)
+  bool ok = false;
+  if (t < n) {
     const int nc = nbr[t];
-    bool ok = nc > 0 && run[t].valid != 0 && rin[t].valid != 0;
+    ok = nc > 0 && run[t].valid != 0 && rin[t].valid != 0;
     if (ok) {
       const OutRec<S> c = rin[t];
       const int q[8] = {t - nc - 1, t - nc, t - nc + 1, t - 1, t + 1, t + nc - 1, t + nc, t + nc + 1};
@@ -403,7 +410,10 @@ __global__ void skip_flags_kernel(const int* nbr, const int* ntiles, const OutRe
     }
     flag[t] = ok ? 1 : 0;
   }
+  const int nskip = __syncthreads_count(ok);
+  if (threadIdx.x == 0) bcnt[blockIdx.x] = make_int2(min(kFlagThreads, n - blockIdx.x * kFlagThreads) - nskip, nskip);
 }
+
 // Input k of a uniform tile: the staged fields (0..6), u^n (7..11: the staged
 // fields 0..4 in stage 1, else the first cell's values) and H0 (12).
 template <typename S, int kPl>
@@ -514,6 +524,29 @@ __device__ __noinline__ void uniform_record(UniEntry<S>* U, const S* box, const 
   U->valid = 1;
 }
 
+// The first uniform tile a stage launch computes on a level publishes its
+// inputs and outputs (the block-cache entry it just filled) for the writer
+// of the skipped tiles, which runs after the launch: state 0 empty, 1 being
+// written, 2 complete.
+template <typename S>
+struct GUni {
+  S key[13];
+  S res[7];
+  int weno;
+  int state;
+};
+template <typename S>
+__device__ __forceinline__ void publish_uniform(GUni<S>* G, const UniEntry<S>& U) {
+  if (atomicCAS(&G->state, 0, 1) != 0) return;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) G->key[k] = U.key[k];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) G->res[k] = U.res[k];
+  G->weno = U.weno;
+  __threadfence();
+  atomicExch(&G->state, 2);
+}
+
 // A computed uniform tile's record: the outputs of its first cell.
 template <typename S, typename W>
 __device__ __forceinline__ void record_out(OutRec<S>* ro, const W* wn, S pv, S tv) {
@@ -557,7 +590,6 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   __shared__ int s_t[2];
   __shared__ int4 s_td[2];  // descriptors of the staged tiles
   __shared__ int s_ti[2];   // their table indices
-  __shared__ int s_skip[2]; // 1: the records prove the tile uniform; its records are staged instead of its box
   __shared__ unsigned s_stats[4 * kL];
   __shared__ int s_cnt[2][8];
   __shared__ int s_list[256];
@@ -596,10 +628,9 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
                    : A.tile_order == 2 ? ((t & 1) ? (t >> 1) : ntiles - 1 - (t >> 1))
                                        : ntiles - 1 - t;
     const int4 td = A.tiles[tbase + ti];
-    const bool sk = A.skip != nullptr && A.skip[tbase + ti] != 0;
+    const int gi = A.gti ? A.gti[tbase + ti] : tbase + ti;
     s_td[b] = td;
-    s_ti[b] = tbase + ti;
-    s_skip[b] = sk ? 1 : 0;
+    s_ti[b] = gi;
     // a tiled TMA copy needs x * sizeof(S) to be a multiple of 16: x even for
     // doubles, a multiple of 4 for floats; set_patches only accepts such
     // patch origins and tiles are 32 wide
@@ -608,15 +639,6 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       return false;
     }
     fence_proxy_async_smem();
-    if (sk) {
-      // the tile's two records (16-byte aligned, 32 or 64 bytes each) in
-      // place of its halo box
-      constexpr uint32_t kRec = sizeof(OutRec<S>);
-      mbar_arrive_expect_tx(&mbar[b], 2 * kRec);
-      bulk_load(dst[b], static_cast<const OutRec<S>*>(A.rec_in) + tbase + ti, kRec, &mbar[b]);
-      bulk_load(dst[b] + kRec, static_cast<const UnRec<S>*>(A.rec_un_in) + tbase + ti, kRec, &mbar[b]);
-      return true;
-    }
     const int lv = td.z & 0xff;
     if constexpr (kF32S) {
       // halo box, and the interior rows of u^n (unless u^n is the input) and H0;
@@ -667,7 +689,6 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     float* tile32 = kF32S ? reinterpret_cast<float*>(dst[b]) : tile32_conv;
     const int4 td = s_td[b];
     const int gti = s_ti[b];
-    const bool skipt = s_skip[b] != 0;
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
     const int i0 = td.x, j0 = td.y;
     const int tx = lane, ty = warp;
@@ -675,7 +696,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     // u^n and H0 of this thread's cell, for the uniform-tile test: loaded
     // before the wait, so that their latency overlaps it
     S un_c[5] = {S(0), S(0), S(0), S(0), S(0)}, h0_c = S(0);
-    if (A.uniform && valid && !skipt) {
+    if (A.uniform && valid) {
       const long g = (long)(j0 + ty + 3) * A.pitch[lvl] + (i0 + tx + 3);
       h0_c = static_cast<const S*>(A.h0[lvl])[g];
       if (!A.un_is_in)
@@ -706,66 +727,6 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
       break;
     }
     phase[b] ^= 1u;
-    if (skipt) {
-      // the staged records: the tile's key (its 7 input values, u^n, H0)
-      const OutRec<S>* ri = reinterpret_cast<const OutRec<S>*>(dst[b]);
-      const UnRec<S>* ru = reinterpret_cast<const UnRec<S>*>(dst[b] + sizeof(OutRec<S>));
-      S kv[13];
-#pragma unroll
-      for (int k = 0; k < 13; ++k) kv[k] = k < 7 ? ri->v[k] : ru->v[k - 7];
-      const UniEntry<S>& U = s_uc[lvl];
-      bool hit = U.valid != 0;
-#pragma unroll
-      for (int k = 0; k < 13; ++k) hit = hit && same_bits(kv[k], U.key[k]);
-      if (hit) {
-        // the block's cached outputs for this key, as uniform_hit stores them
-        if (valid) {
-          S* out = static_cast<S*>(A.out[lvl]);
-          const long fs = A.fstride[lvl];
-          const long gc = (long)(j0 + ty + 3) * A.pitch[lvl] + (i0 + tx + 3);
-#pragma unroll
-          for (int k = 0; k < kNF; ++k) out[k * fs + gc] = U.res[k];
-        }
-        if (tid == 0) {
-          s_stats[4 * lvl + 0] += U.weno ? (unsigned)(w * h) : 0u;
-          s_stats[4 * lvl + 1] += (unsigned)(w * h);
-          s_stats[4 * lvl + 3] += (unsigned)(w * h);
-          if (A.rec_out) {
-            OutRec<S>* ro = static_cast<OutRec<S>*>(A.rec_out) + gti;
-#pragma unroll
-            for (int k = 0; k < 7; ++k) ro->v[k] = U.res[k];
-            ro->valid = 1;
-          }
-        }
-        __syncthreads();  // this staging buffer is refilled two tiles later
-        t = s_t[b ^ 1];
-        b ^= 1;
-        continue;
-      }
-      // not in the block's cache: build the box the records describe (one
-      // value per field; u^n and H0 where they are staged) and take the full
-      // path, which computes the tile and fills the cache entry
-      __syncthreads();  // every thread holds the key before the records are overwritten
-      S* box = reinterpret_cast<S*>(dst[b]);
-      constexpr int kPlB = kF32S ? kPlane32 : kBH * kBW;
-#pragma unroll
-      for (int k = 0; k < kNF; ++k)
-        for (int e = tid; e < kPlB; e += 256) box[k * kPlB + e] = kv[k];
-      if constexpr (kF32S && kUnTma) {
-        float* unb = reinterpret_cast<float*>(dst[b] + kTile32Bytes);
-#pragma unroll
-        for (int k = 0; k < 5; ++k)
-          for (int e = tid; e < kTH * kBW32; e += 256) unb[k * (kTH * kBW32) + e] = kv[7 + k];
-        float* h0b = reinterpret_cast<float*>(dst[b] + kTile32Bytes + kUnBytes);
-        for (int e = tid; e < kTH * kBW32; e += 256) h0b[e] = kv[12];
-      }
-      if (valid) {
-#pragma unroll
-        for (int k = 0; k < 5; ++k) un_c[k] = kv[7 + k];
-        h0_c = kv[12];
-      }
-      __syncthreads();
-    }
     // beta*dt of this stage (dt from the device CFL reduction when adaptive)
     const double bdt = kF32S ? 0.0 : (A.dt_dev ? A.beta * (*A.dt_dev) : A.bdt);
     if (tid == 0) {
@@ -1049,6 +1010,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
             uniform_record<S, kPl>(&s_uc[lvl], reinterpret_cast<const S*>(dst[b]), s_wl[0], A.un_is_in, wn[0], wn[1],
                                    wn[2], wn[3], wn[4], pq, tp, f);
             if (A.rec_out) record_out<S>(static_cast<OutRec<S>*>(A.rec_out) + gti, wn, pq, tp);
+            if (A.gcache) publish_uniform<S>(static_cast<GUni<S>*>(A.gcache) + lvl, s_uc[lvl]);
           }
           if (!(rho > 0.f) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4])) raise_health(A.health, ENL_ERR_NONFINITE);
         } else {
@@ -1115,6 +1077,7 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
             uniform_record<S, kPl>(&s_uc[lvl], reinterpret_cast<const S*>(dst[b]), s_wl[0], A.un_is_in, wn[0], wn[1],
                                    wn[2], wn[3], wn[4], pv, tv, f);
             if (A.rec_out) record_out<S>(static_cast<OutRec<S>*>(A.rec_out) + gti, wn, pv, tv);
+            if (A.gcache) publish_uniform<S>(static_cast<GUni<S>*>(A.gcache) + lvl, s_uc[lvl]);
           }
           if (!(wn[0] > 0.0) || !isfinite(wn[0] + wn[1] + wn[2] + wn[3] + wn[4]))
             raise_health(A.health, ENL_ERR_NONFINITE);
@@ -1128,6 +1091,150 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
   if (tid == 0 && A.stats)
     for (int q = 0; q < 4 * kL; ++q)
       if (s_stats[q]) atomicAdd(&A.stats[q], (unsigned long long)s_stats[q]);
+}
+
+// ---------------------------------------------------------------------------
+// Uniform-tile skipping, stages 2 and 3: after skip_flags_kernel, one block
+// splits the tile table into the tiles to compute (their descriptors and
+// table indices, in table order, so the schedule's tile orders still apply)
+// and the tiles to skip; the stage launch computes the first list and
+// publishes its first uniform result per level; skip_write_kernel stores
+// that result into every skipped tile whose records carry the same key and
+// passes the others on to a second stage launch (usually empty).
+// counts: [0] tiles to compute, [1] tiles to skip, [2] passed on.
+// Block b (of the flag pass's blocks) writes the entries of its 256 tiles at
+// the offsets that the counts of the blocks before it give; block 0 also
+// writes the totals.
+__global__ void __launch_bounds__(kFlagThreads) skip_lists_kernel(const unsigned char* flag, const int* ntiles,
+                                                                  const int2* bcnt, const int4* tiles,
+                                                                  int4* full_td, int* full_gti, int* skip_gti,
+                                                                  int* counts) {
+  __shared__ int s_red[2][kFlagThreads / 32];
+  __shared__ int s_wf[kFlagThreads / 32], s_ws[kFlagThreads / 32];
+  const int n = *ntiles, nb = (n + kFlagThreads - 1) / kFlagThreads;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if ((int)blockIdx.x >= nb) return;
+  // offsets of this block: sums over the blocks before it (block 0 sums all
+  // of them for the totals)
+  const int upto = blockIdx.x == 0 ? nb : (int)blockIdx.x;
+  int of = 0, os = 0;
+  for (int q = tid; q < upto; q += kFlagThreads) {
+    const int2 c = bcnt[q];
+    of += c.x;
+    os += c.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    of += __shfl_xor_sync(0xffffffffu, of, o);
+    os += __shfl_xor_sync(0xffffffffu, os, o);
+  }
+  if (lane == 0) {
+    s_red[0][warp] = of;
+    s_red[1][warp] = os;
+  }
+  // this block's tiles: rank within the block by ballots
+  const int t = blockIdx.x * kFlagThreads + tid;
+  const bool in = t < n;
+  const bool sk = in && flag[t] != 0;
+  const unsigned bs = __ballot_sync(0xffffffffu, sk), bf = __ballot_sync(0xffffffffu, in && !sk);
+  if (lane == 0) {
+    s_wf[warp] = __popc(bf);
+    s_ws[warp] = __popc(bs);
+  }
+  __syncthreads();
+  of = 0;
+  os = 0;
+  int pf = 0, ps = 0;
+#pragma unroll
+  for (int q = 0; q < kFlagThreads / 32; ++q) {
+    of += s_red[0][q];
+    os += s_red[1][q];
+    if (q < warp) {
+      pf += s_wf[q];
+      ps += s_ws[q];
+    }
+  }
+  if (blockIdx.x == 0) {
+    if (tid == 0) {
+      counts[0] = of;
+      counts[1] = os;
+      counts[2] = 0;
+    }
+    of = os = 0;  // block 0 starts both lists
+  }
+  const unsigned lt = (1u << lane) - 1u;
+  if (sk) {
+    skip_gti[os + ps + __popc(bs & lt)] = t;
+  } else if (in) {
+    const int p = of + pf + __popc(bf & lt);
+    full_td[p] = tiles[t];
+    full_gti[p] = t;
+  }
+}
+
+template <typename S>
+struct SkipWriteArgs {
+  S* out[kL];
+  long pitch[kL], fstride[kL];
+  const int4* tiles;
+  const int* skip_gti;
+  int* counts;
+  const OutRec<S>* rin;
+  const UnRec<S>* run;
+  OutRec<S>* rout;  // stage 2: the output records (null in stage 3)
+  const GUni<S>* gcache;
+  int4* left_td;
+  int* left_gti;
+  unsigned long long* stats;
+};
+
+// One block per skipped tile: its key (input record, u^n / H0 record)
+// against the level's published uniform result; a match stores the result
+// into every cell (and the tile's output record), as a cache hit of the stage
+// kernel would; otherwise the tile goes to the list of the second launch.
+template <typename S>
+__global__ void skip_write_kernel(SkipWriteArgs<S> A) {
+  __shared__ unsigned long long s_st[4 * kL];
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  if (tid < 4 * kL) s_st[tid] = 0ull;
+  __syncthreads();
+  const int n = A.counts[1];
+  for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    const int gi = A.skip_gti[q];
+    const int4 td = A.tiles[gi];
+    const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
+    const GUni<S>& G = A.gcache[lvl];
+    const OutRec<S>& ri = A.rin[gi];
+    const UnRec<S>& ru = A.run[gi];
+    bool match = G.state == 2;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) match = match && same_bits(ri.v[k], G.key[k]);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) match = match && same_bits(ru.v[k], G.key[7 + k]);
+    if (match) {
+      if (tx < w && ty < h) {
+        const long g = (long)(td.y + ty + 3) * A.pitch[lvl] + (td.x + tx + 3);
+#pragma unroll
+        for (int k = 0; k < kNF; ++k) A.out[lvl][k * A.fstride[lvl] + g] = G.res[k];
+      }
+      if (tid == 0) {
+        s_st[4 * lvl + 0] += G.weno ? (unsigned long long)(w * h) : 0ull;
+        s_st[4 * lvl + 1] += (unsigned long long)(w * h);
+        s_st[4 * lvl + 3] += (unsigned long long)(w * h);
+        if (A.rout) {
+#pragma unroll
+          for (int k = 0; k < 7; ++k) A.rout[gi].v[k] = G.res[k];
+          A.rout[gi].valid = 1;
+        }
+      }
+    } else if (tid == 0) {
+      const int k = atomicAdd(&A.counts[2], 1);
+      A.left_td[k] = td;
+      A.left_gti[k] = gi;
+    }
+  }
+  __syncthreads();
+  if (tid < 4 * kL && s_st[tid] && A.stats) atomicAdd(&A.stats[tid], s_st[tid]);
 }
 
 // ---------------------------------------------------------------------------
@@ -2261,6 +2368,11 @@ struct Engine {
   DevArray<int> d_nbr;
   std::vector<int> h_nbr;
   DevArray<unsigned char> d_rec_o1, d_rec_o2, d_rec_un, d_skip;
+  DevArray<int2> d_bcnt;                       // per flag-pass block: tiles to compute, to skip
+  DevArray<int4> d_full_td, d_left_td;         // descriptors of the tiles to compute / passed on
+  DevArray<int> d_full_gti, d_skip_gti, d_left_gti;
+  int* d_skipcnt = nullptr;                    // [0] to compute, [1] to skip, [2] passed on
+  void* d_gcache = nullptr;                    // GUni<S>[kL]: published uniform results
   // storage: FP64 absolute values, or FP32 perturbations about the ambient
   // state (absolute = off[k] + stored)
   bool f32s = false;
@@ -2566,9 +2678,18 @@ static int rebuild_tables(Engine* E) {
     grew |= E->d_rec_o1.ensure(nt * rb);
     grew |= E->d_rec_o2.ensure(nt * rb);
     grew |= E->d_rec_un.ensure(nt * rb);
+    grew |= E->d_full_td.ensure(nt);
+    grew |= E->d_left_td.ensure(nt);
+    grew |= E->d_full_gti.ensure(nt);
+    grew |= E->d_skip_gti.ensure(nt);
+    grew |= E->d_left_gti.ensure(nt);
+    // one count per flag-pass block over the skip flags' capacity (the
+    // passes' grids, fixed while the arrays keep their size)
+    grew |= E->d_bcnt.ensure((E->d_skip.cap + kFlagThreads - 1) / kFlagThreads);
   }
   if (grew) E->graph_valid = false;
-  if (!E->d_nbr.p || !E->d_skip.p || !E->d_rec_o1.p || !E->d_rec_o2.p || !E->d_rec_un.p) {
+  if (!E->d_nbr.p || !E->d_skip.p || !E->d_rec_o1.p || !E->d_rec_o2.p || !E->d_rec_un.p || !E->d_full_td.p ||
+      !E->d_left_td.p || !E->d_full_gti.p || !E->d_skip_gti.p || !E->d_left_gti.p || !E->d_bcnt.p) {
     E->tables_on_device = false;
     E->graph_valid = false;
     set_error(ENL_ERR_CUDA);
@@ -2651,7 +2772,9 @@ static EosConst64 eos_const64(const enl_engine_config& c) {
 // tiles of that level only (the per-level stage order)
 // Uniform-tile skipping: with uniform-tile reuse (c_lr = 0, not dense) and
 // the schedule's skipping on.
-static bool skip_on(const Engine* E) { return E->skip && !E->cfg.dense && E->cfg.c_lr == 0.0; }
+static bool skip_on(const Engine* E) {
+  return E->skip && !E->cfg.dense && E->cfg.c_lr == 0.0 && !E->samrai_order && E->d_skipcnt && E->d_gcache;
+}
 
 static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   StageArgs A;
@@ -2745,33 +2868,21 @@ static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
   A.feat_inv_sqrt_eps = (float)(1.0 / sqrt(A.P[0].sensor_eps));
   if (skip_on(E)) {
-    // stage 1 records its outputs and u^n / H0; stage 2 reads stage 1's
-    // records and records its own; stage 3 reads stage 2's
+    // stage 1 records its outputs and u^n / H0, stage 2 its outputs; stages
+    // 2 and 3 run over the list of tiles to compute (skip_stage_t) and
+    // publish their uniform results for the writer of the skipped ones
     if (stage == 0) {
       A.rec_out = E->d_rec_o1.p;
       A.rec_un_out = E->d_rec_un.p;
     } else {
-      A.rec_in = stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p;
-      A.rec_un_in = E->d_rec_un.p;
       A.rec_out = stage == 1 ? E->d_rec_o2.p : nullptr;
-      A.skip = E->d_skip.p;
+      A.tiles = E->d_full_td.p;
+      A.gti = E->d_full_gti.p;
+      A.ntiles = E->d_skipcnt;
+      A.gcache = E->d_gcache;
     }
   }
   return A;
-}
-
-// The skip flags of stage `stage` (1 or 2) from the records of the previous
-// stage, for every tile of every level.
-static void skip_flags(Engine* E, int stage) {
-  const unsigned char* rin = stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p;
-  if (E->f32s)
-    skip_flags_kernel<float><<<E->nsm * 2, 256, 0, stream()>>>(
-        E->d_nbr.p, E->d_meta + M_NTILES, reinterpret_cast<const OutRec<float>*>(rin),
-        reinterpret_cast<const UnRec<float>*>(E->d_rec_un.p), E->d_skip.p);
-  else
-    skip_flags_kernel<double><<<E->nsm * 2, 256, 0, stream()>>>(
-        E->d_nbr.p, E->d_meta + M_NTILES, reinterpret_cast<const OutRec<double>*>(rin),
-        reinterpret_cast<const UnRec<double>*>(E->d_rec_un.p), E->d_skip.p);
 }
 
 typedef void (*StageFn)(StageArgs);
@@ -3031,6 +3142,53 @@ static void record_mics(Engine* E) {
   else mics_t<double>(E);
 }
 
+// Stage `stage` (1 or 2) with skipping: flags and lists from the previous
+// stage's records, the launch over the tiles to compute, the writer of the
+// skipped tiles, and a launch over the skipped tiles without a published
+// result (usually none).
+template <typename S>
+static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) {
+  cudaStream_t s = stream();
+  const OutRec<S>* rin = reinterpret_cast<const OutRec<S>*>(stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p);
+  const UnRec<S>* run = reinterpret_cast<const UnRec<S>*>(E->d_rec_un.p);
+  const int nbk = (int)E->d_bcnt.cap;
+  cudaMemsetAsync(E->d_gcache, 0, kL * sizeof(GUni<S>), s);
+  skip_flags_kernel<S><<<nbk, kFlagThreads, 0, s>>>(E->d_nbr.p, E->d_meta + M_NTILES, rin, run, E->d_skip.p,
+                                                     E->d_bcnt.p);
+  skip_lists_kernel<<<nbk, kFlagThreads, 0, s>>>(E->d_skip.p, E->d_meta + M_NTILES, E->d_bcnt.p, E->d_tiles.p,
+                                                 E->d_full_td.p, E->d_full_gti.p, E->d_skip_gti.p, E->d_skipcnt);
+  StageArgs A = A0;
+  void* args[] = {&A};
+  cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
+  SkipWriteArgs<S> W;
+  memset(&W, 0, sizeof(W));
+  for (int l = 0; l < E->cfg.nlevels; ++l) {
+    W.out[l] = static_cast<S*>(A0.out[l]);
+    W.pitch[l] = A0.pitch[l];
+    W.fstride[l] = A0.fstride[l];
+  }
+  W.tiles = E->d_tiles.p;
+  W.skip_gti = E->d_skip_gti.p;
+  W.counts = E->d_skipcnt;
+  W.rin = rin;
+  W.run = run;
+  W.rout = static_cast<OutRec<S>*>(A0.rec_out);
+  W.gcache = static_cast<const GUni<S>*>(E->d_gcache);
+  W.left_td = E->d_left_td.p;
+  W.left_gti = E->d_left_gti.p;
+  W.stats = E->d_stats;
+  skip_write_kernel<S><<<E->nsm * 4, 256, 0, s>>>(W);
+  StageArgs B = A0;
+  B.tiles = E->d_left_td.p;
+  B.gti = E->d_left_gti.p;
+  B.ntiles = E->d_skipcnt + 2;
+  B.counter = E->d_counters + 3 + stage;
+  B.counter64 = E->d_counters64 + 3 + stage;
+  B.gcache = nullptr;
+  void* bargs[] = {&B};
+  cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), bargs, E->smem_bytes, s);
+}
+
 static int step_fused(Engine* E, double dt) {
   cudaStream_t s = stream();
   cudaMemsetAsync(E->d_counters, 0, 3 * (1 + kL) * sizeof(int), s);
@@ -3040,7 +3198,6 @@ static int step_fused(Engine* E, double dt) {
   for (int st = 0; st < 3; ++st) {
     int in = st == 0 ? 0 : st;
     int out = st == 2 ? 0 : st + 1;
-    if (st > 0 && skip_on(E)) skip_flags(E, st);
     if (E->samrai_order) {
       // SAMRAI's MethodOfLinesIntegrator order (main.C:448): per stage the
       // levels coarsest first, each filling its ghosts -- coarse-fine ones
@@ -3068,7 +3225,12 @@ static int step_fused(Engine* E, double dt) {
     StageArgs A = stage_args(E, st, dt);
     void* args[] = {&A};
     if (E->profile) cudaEventRecord(E->pev[2 * st], s);
-    cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
+    if (st > 0 && skip_on(E)) {
+      if (E->f32s) skip_stage_t<float>(E, st, fn, A);
+      else skip_stage_t<double>(E, st, fn, A);
+    } else {
+      cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
+    }
     if (E->profile) cudaEventRecord(E->pev[2 * st + 1], s);
     (void)out;
   }
@@ -3253,6 +3415,9 @@ int enl_engine_create(const enl_engine_config* cfg, void** out) {
   cudaMemset(E->d_meta, 0, sizeof(E->h_meta));
   cudaMalloc(&E->d_counters, 3 * (1 + kL) * sizeof(int));
   cudaMalloc(&E->d_counters64, 3 * (1 + kL) * sizeof(unsigned long long));
+  if (cudaMalloc(&E->d_skipcnt, 4 * sizeof(int)) != cudaSuccess) E->d_skipcnt = nullptr;
+  if (cudaMalloc(&E->d_gcache, kL * sizeof(GUni<double>)) != cudaSuccess) E->d_gcache = nullptr;
+  cudaGetLastError();  // (skipping stays off without them)
   cudaMalloc(&E->d_health, sizeof(int));
   cudaMemset(E->d_health, 0, sizeof(int));
   cudaMalloc(&E->d_stats, 4 * kL * sizeof(unsigned long long));
@@ -3301,6 +3466,8 @@ int enl_engine_destroy(void* e) {
   if (E->d_meta) cudaFree(E->d_meta);
   if (E->d_counters) cudaFree(E->d_counters);
   if (E->d_counters64) cudaFree(E->d_counters64);
+  if (E->d_skipcnt) cudaFree(E->d_skipcnt);
+  if (E->d_gcache) cudaFree(E->d_gcache);
   if (E->d_health) cudaFree(E->d_health);
   if (E->d_stats) cudaFree(E->d_stats);
   for (int l = 0; l < kL; ++l)
@@ -3597,13 +3764,11 @@ int enl_engine_skipped_tiles(void* e, long long* flagged, long long* tiles) {
   const size_t n = E->h_tiles.size();
   *flagged = 0;
   if (tiles) *tiles = (long long)n;
-  if (!skip_on(E) || n == 0 || !E->d_skip.p) return ENL_OK;
-  std::vector<unsigned char> h(n);
-  cudaMemcpyAsync(h.data(), E->d_skip.p, n, cudaMemcpyDeviceToHost, stream());
+  if (!skip_on(E) || n == 0) return ENL_OK;
+  int h[3] = {0, 0, 0};
+  cudaMemcpyAsync(h, E->d_skipcnt, sizeof(h), cudaMemcpyDeviceToHost, stream());
   cudaStreamSynchronize(stream());
-  long long c = 0;
-  for (unsigned char v : h) c += v ? 1 : 0;
-  *flagged = c;
+  *flagged = (long long)h[1] - h[2];  // written from a published result
   return check_launch("engine skipped tiles");
 }
 
@@ -3634,7 +3799,7 @@ int enl_engine_launches_per_step(void* e, int plain) {
     // interpolation below level 1)
     const int refresh = E->samrai_order ? (nl - 1) + (nl > 2 ? nl - 2 : 0) : 0;
     return 3 * (bands + (nl - 1) + (E->samrai_order ? nl : 1) + refresh) + (nl - 1) + dt +
-           (skip_on(E) ? 2 : 0);  // the skip flags of stages 2 and 3
+           (skip_on(E) ? 8 : 0);  // stages 2 and 3: flags, lists, writer, second launch
   }
   const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;
