@@ -806,7 +806,7 @@ def other_kernels(cls, steps, hbm_peak, peak_kind):
     algorithmic bytes per launch over its event-timed duration."""
     out = {}
     for k, (ms, by, n) in cls.items():
-        if n == 0:
+        if n == 0 or k not in KERNEL_NOTES:
             continue
         gbs = by / (ms * 1e-3) / 1e9 if ms > 0 else None
         out[k] = {"launches_per_step": n / steps, "ms_per_step": ms / steps, "ms_per_launch": ms / n,
@@ -1192,6 +1192,8 @@ def run_linesource(args):
     # the step's other kernels, timed with events around each launch over the
     # same three direct steps
     roof["other_kernels"] = other_kernels(kcls, 3, hbm_peak, peak_kind)
+    roof["skip_kernels"] = {k: {"ms_per_step": kcls[k][0] / 3, "launches_per_step": kcls[k][2] / 3}
+                            for k in ("skip_lists", "skip_write", "stage_rest") if kcls.get(k, (0, 0, 0))[2]}
     # the FP32-storage engine: its own timed region (graph replay, regrids)
     secondary = None
     if wl32 is not None:

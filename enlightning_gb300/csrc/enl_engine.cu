@@ -2307,15 +2307,18 @@ struct Engine {
   double prof_ms = 0.0;
   long long prof_launches = 0, prof_cells = 0;
   // per-class timing of the step's other kernels (profile 2): 0 interp,
-  // 1 physical band fill, 2 coarsen, 3 CFL maximum (speed + dt)
+  // 1 physical band fill, 2 coarsen, 3 CFL maximum (speed + dt), and with
+  // uniform-tile skipping 4 the flag pass and lists, 5 the writer of the
+  // skipped tiles, 6 the second stage launch
   static constexpr int kKev = 128;
   cudaEvent_t kev[2 * kKev] = {};
   int kev_cls[kKev] = {};
   int kev_n = 0;
+  static constexpr int kCls = 7;
   double kev_bytes[kKev] = {};
-  double kcls_ms[4] = {0, 0, 0, 0};
-  double kcls_bytes[4] = {0, 0, 0, 0};
-  long long kcls_n[4] = {0, 0, 0, 0};
+  double kcls_ms[kCls] = {};
+  double kcls_bytes[kCls] = {};
+  long long kcls_n[kCls] = {};
   // per level, from the tables: distinct coarse cells the halo interpolation
   // reads, coarse cells the coarsening writes, band cells of the per-patch
   // fill, patch cells
@@ -3153,10 +3156,12 @@ static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) 
   const UnRec<S>* run = reinterpret_cast<const UnRec<S>*>(E->d_rec_un.p);
   const int nbk = (int)E->d_bcnt.cap;
   cudaMemsetAsync(E->d_gcache, 0, kL * sizeof(GUni<S>), s);
+  int q = kt_begin(E, 4, 0.0);
   skip_flags_kernel<S><<<nbk, kFlagThreads, 0, s>>>(E->d_nbr.p, E->d_meta + M_NTILES, rin, run, E->d_skip.p,
                                                      E->d_bcnt.p);
   skip_lists_kernel<<<nbk, kFlagThreads, 0, s>>>(E->d_skip.p, E->d_meta + M_NTILES, E->d_bcnt.p, E->d_tiles.p,
                                                  E->d_full_td.p, E->d_full_gti.p, E->d_skip_gti.p, E->d_skipcnt);
+  kt_end(E, q);
   StageArgs A = A0;
   void* args[] = {&A};
   cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
@@ -3177,7 +3182,9 @@ static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) 
   W.left_td = E->d_left_td.p;
   W.left_gti = E->d_left_gti.p;
   W.stats = E->d_stats;
+  q = kt_begin(E, 5, 0.0);
   skip_write_kernel<S><<<E->nsm * 4, 256, 0, s>>>(W);
+  kt_end(E, q);
   StageArgs B = A0;
   B.tiles = E->d_left_td.p;
   B.gti = E->d_left_gti.p;
@@ -3186,7 +3193,9 @@ static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) 
   B.counter64 = E->d_counters64 + 3 + stage;
   B.gcache = nullptr;
   void* bargs[] = {&B};
+  q = kt_begin(E, 6, 0.0);
   cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), bargs, E->smem_bytes, s);
+  kt_end(E, q);
 }
 
 static int step_fused(Engine* E, double dt) {
@@ -4705,7 +4714,7 @@ int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, l
   E->prof_ms = 0.0;
   E->prof_launches = 0;
   E->prof_cells = 0;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < Engine::kCls; ++k) {
     E->kcls_ms[k] = E->kcls_bytes[k] = 0.0;
     E->kcls_n[k] = 0;
   }
@@ -4718,7 +4727,7 @@ int enl_engine_profile(void* e, int on, double* ms_total, long long* launches, l
 int enl_engine_profile_kernels(void* e, double* ms, double* bytes, long long* launches) {
   Engine* E = (Engine*)e;
   if (!E) return ENL_ERR_ARG;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < Engine::kCls; ++k) {
     if (ms) ms[k] = E->kcls_ms[k];
     if (bytes) bytes[k] = E->kcls_bytes[k];
     if (launches) launches[k] = E->kcls_n[k];
