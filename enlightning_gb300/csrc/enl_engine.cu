@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -382,9 +383,9 @@ static_assert(sizeof(OutRec<double>) == 64 && sizeof(UnRec<double>) == 64, "FP64
 static_assert(sizeof(OutRec<float>) == 32 && sizeof(UnRec<float>) == 32, "FP32 records: 32 bytes");
 
 // Per tile: 1 when the stage's input records prove the tile's halo box
-// uniform (nbr[t] = tiles per row of its patch for a tile whose eight
-// neighbours lie in the patch, else 0).  Block b takes tiles [256 b, 256 b +
-// 256) and writes its count of tiles to compute and to skip to bcnt[b].
+// uniform (nbr[8 t .. 8 t + 7]: the tiles whose interiors hold its halo, or
+// -1 first when they do not).  Block b takes tiles [256 b, 256 b + 256) and
+// writes its count of tiles to compute and to skip to bcnt[b].
 constexpr int kFlagThreads = 256;
 template <typename S>
 __global__ void __launch_bounds__(kFlagThreads) skip_flags_kernel(const int* nbr, const int* ntiles,
@@ -395,11 +396,11 @@ __global__ void __launch_bounds__(kFlagThreads) skip_flags_kernel(const int* nbr
   if (blockIdx.x * kFlagThreads >= n) return;  // (the whole block: no barrier below is left half-way)
   bool ok = false;
   if (t < n) {
-    const int nc = nbr[t];
-    ok = nc > 0 && run[t].valid != 0 && rin[t].valid != 0;
+    const int4 n0 = reinterpret_cast<const int4*>(nbr)[2 * t], n1 = reinterpret_cast<const int4*>(nbr)[2 * t + 1];
+    ok = n0.x >= 0 && run[t].valid != 0 && rin[t].valid != 0;
     if (ok) {
       const OutRec<S> c = rin[t];
-      const int q[8] = {t - nc - 1, t - nc, t - nc + 1, t - 1, t + 1, t + nc - 1, t + nc, t + nc + 1};
+      const int q[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
 #pragma unroll
       for (int m = 0; m < 8; ++m) {
         const OutRec<S> r = rin[q[m]];
@@ -1188,51 +1189,65 @@ struct SkipWriteArgs {
   unsigned long long* stats;
 };
 
-// One block per skipped tile: its key (input record, u^n / H0 record)
-// against the level's published uniform result; a match stores the result
-// into every cell (and the tile's output record), as a cache hit of the stage
+// One warp per skipped tile (a block takes eight at a time): lanes 0..12
+// load the tile's key (input record, u^n / H0 record) in one round and
+// compare it with the level's published uniform result (staged in shared
+// memory once per block); a match stores the result into every cell, eight
+// rows of 32 (and the tile's output record), as a cache hit of the stage
 // kernel would; otherwise the tile goes to the list of the second launch.
 template <typename S>
 __global__ void skip_write_kernel(SkipWriteArgs<S> A) {
   __shared__ unsigned long long s_st[4 * kL];
-  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  __shared__ GUni<S> s_g[kL];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, wpb = blockDim.x >> 5;
   if (tid < 4 * kL) s_st[tid] = 0ull;
+  for (int e = tid; e < (int)(kL * sizeof(GUni<S>) / sizeof(int)); e += blockDim.x)
+    reinterpret_cast<int*>(s_g)[e] = reinterpret_cast<const int*>(A.gcache)[e];
   __syncthreads();
   const int n = A.counts[1];
-  for (int q = blockIdx.x; q < n; q += gridDim.x) {
+  unsigned long long st_w[kL], st_c[kL];  // lane 0: this warp's counts
+#pragma unroll
+  for (int l = 0; l < kL; ++l) st_w[l] = st_c[l] = 0ull;
+  for (int q = blockIdx.x * wpb + warp; q < n; q += gridDim.x * wpb) {
     const int gi = A.skip_gti[q];
     const int4 td = A.tiles[gi];
+    S kv = S(0);
+    if (lane < 7) kv = A.rin[gi].v[lane];
+    else if (lane < 13) kv = A.run[gi].v[lane - 7];
     const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
-    const GUni<S>& G = A.gcache[lvl];
-    const OutRec<S>& ri = A.rin[gi];
-    const UnRec<S>& ru = A.run[gi];
-    bool match = G.state == 2;
-#pragma unroll
-    for (int k = 0; k < 7; ++k) match = match && same_bits(ri.v[k], G.key[k]);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) match = match && same_bits(ru.v[k], G.key[7 + k]);
+    const GUni<S>& G = s_g[lvl];
+    const bool ok = lane >= 13 || same_bits(kv, G.key[lane]);
+    const bool match = __all_sync(0xffffffffu, ok) && G.state == 2;
     if (match) {
-      if (tx < w && ty < h) {
-        const long g = (long)(td.y + ty + 3) * A.pitch[lvl] + (td.x + tx + 3);
+      if (lane < w) {
+        S* o = A.out[lvl] + (long)(td.y + 3) * A.pitch[lvl] + (td.x + lane + 3);
+        for (int r = 0; r < h; ++r)
 #pragma unroll
-        for (int k = 0; k < kNF; ++k) A.out[lvl][k * A.fstride[lvl] + g] = G.res[k];
+          for (int k = 0; k < kNF; ++k) o[k * A.fstride[lvl] + (long)r * A.pitch[lvl]] = G.res[k];
       }
-      if (tid == 0) {
-        s_st[4 * lvl + 0] += G.weno ? (unsigned long long)(w * h) : 0ull;
-        s_st[4 * lvl + 1] += (unsigned long long)(w * h);
-        s_st[4 * lvl + 3] += (unsigned long long)(w * h);
-        if (A.rout) {
-#pragma unroll
-          for (int k = 0; k < 7; ++k) A.rout[gi].v[k] = G.res[k];
-          A.rout[gi].valid = 1;
-        }
+      if (lane == 0) {
+        st_w[lvl] += G.weno ? (unsigned long long)(w * h) : 0ull;
+        st_c[lvl] += (unsigned long long)(w * h);
       }
-    } else if (tid == 0) {
+      if (A.rout && lane < 8) {
+        if (lane < 7) A.rout[gi].v[lane] = G.res[lane];
+        else A.rout[gi].valid = 1;
+      }
+    } else if (lane == 0) {
       const int k = atomicAdd(&A.counts[2], 1);
       A.left_td[k] = td;
       A.left_gti[k] = gi;
     }
   }
+  if (lane == 0)
+#pragma unroll
+    for (int l = 0; l < kL; ++l) {
+      if (st_w[l]) atomicAdd(&s_st[4 * l + 0], st_w[l]);
+      if (st_c[l]) {
+        atomicAdd(&s_st[4 * l + 1], st_c[l]);
+        atomicAdd(&s_st[4 * l + 3], st_c[l]);
+      }
+    }
   __syncthreads();
   if (tid < 4 * kL && s_st[tid] && A.stats) atomicAdd(&A.stats[tid], s_st[tid]);
 }
@@ -2494,19 +2509,63 @@ static void halo_segments(const std::vector<int4>& P, int nx, int ny, std::vecto
   }
 }
 
-// Neighbour strides of the tiles tiles_of_box makes for box b, in its order:
-// the patch's tiles per row for a tile whose eight neighbours are tiles of
-// the same patch reaching at least 3 cells (the stencil) into its halo box,
-// else 0.
-static void nbr_of_box(int4 b, std::vector<int>& out) {
-  const int W = b.y - b.x + 1, H = b.w - b.z + 1;
-  const int nc = (W + kTW - 1) / kTW, nr = (H + kTH - 1) / kTH;
-  for (int r = 0; r < nr; ++r)
-    for (int c = 0; c < nc; ++c) {
-      const bool inner = c >= 1 && r >= 1 && c + 1 < nc && r + 1 < nr &&
-                         std::min(kTW, W - kTW * (c + 1)) >= 3 && std::min(kTH, H - kTH * (r + 1)) >= 3;
-      out.push_back(inner ? nc : 0);
+// The eight neighbours of every tile of one level (table entries [t0, t1)),
+// 8 table indices per tile in the order skip_flags_kernel reads them (above
+// left, above, above right, left, right, below left, below, below right; rows
+// counted downwards in j), when its halo box lies in their interiors, else
+// -1 in the first slot: tiles of the same patch row-major around a tile whose
+// neighbours reach at least 3 cells into its box, and, across patches, full
+// 32 x 8 tiles on the level's 32 x 8 grid whose eight grid neighbours are
+// such tiles too (the base level's patches are aligned to it).
+static void level_neighbours(const std::vector<int4>& tiles, const std::vector<int4>& patches, int t0, int t1,
+                             std::vector<int>& out) {
+  out.resize((size_t)8 * t1, -1);
+  for (int t = t0; t < t1; ++t) out[(size_t)8 * t] = -1;
+  // within a patch
+  int t = t0;
+  for (const int4& b : patches) {
+    const int W = b.y - b.x + 1, H = b.w - b.z + 1;
+    const int nc = (W + kTW - 1) / kTW, nr = (H + kTH - 1) / kTH;
+    for (int r = 0; r < nr; ++r)
+      for (int c = 0; c < nc; ++c, ++t) {
+        const bool inner = c >= 1 && r >= 1 && c + 1 < nc && r + 1 < nr &&
+                           std::min(kTW, W - kTW * (c + 1)) >= 3 && std::min(kTH, H - kTH * (r + 1)) >= 3;
+        if (!inner) continue;
+        const int q[8] = {t - nc - 1, t - nc, t - nc + 1, t - 1, t + 1, t + nc - 1, t + nc, t + nc + 1};
+        for (int m = 0; m < 8; ++m) out[(size_t)8 * t + m] = q[m];
+      }
+  }
+  // across patches, on the 32 x 8 grid (over the bounding box of the full,
+  // aligned tiles)
+  auto full = [&](const int4& td) {
+    return (td.x % kTW) == 0 && (td.y % kTH) == 0 && ((td.z >> 8) & 0xff) == kTW && ((td.z >> 16) & 0xff) == kTH;
+  };
+  int gx0 = INT_MAX, gy0 = INT_MAX, gx1 = INT_MIN, gy1 = INT_MIN;
+  for (int u = t0; u < t1; ++u)
+    if (full(tiles[u])) {
+      gx0 = std::min(gx0, tiles[u].x / kTW);
+      gx1 = std::max(gx1, tiles[u].x / kTW);
+      gy0 = std::min(gy0, tiles[u].y / kTH);
+      gy1 = std::max(gy1, tiles[u].y / kTH);
     }
+  if (gx0 > gx1) return;
+  const int gw = gx1 - gx0 + 1, gh = gy1 - gy0 + 1;
+  std::vector<int> grid((size_t)gw * gh, -1);
+  for (int u = t0; u < t1; ++u)
+    if (full(tiles[u])) grid[(size_t)(tiles[u].y / kTH - gy0) * gw + (tiles[u].x / kTW - gx0)] = u;
+  for (int u = t0; u < t1; ++u) {
+    if (!full(tiles[u]) || out[(size_t)8 * u] >= 0) continue;
+    const int gx = tiles[u].x / kTW - gx0, gy = tiles[u].y / kTH - gy0;
+    if (gx < 1 || gy < 1 || gx + 1 >= gw || gy + 1 >= gh) continue;
+    int q[8], m = 0;
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx)
+        if (dx || dy) q[m++] = grid[(size_t)(gy + dy) * gw + (gx + dx)];
+    bool all = true;
+    for (int k = 0; k < 8; ++k) all = all && q[k] >= 0;
+    if (all)
+      for (int k = 0; k < 8; ++k) out[(size_t)8 * u + k] = q[k];
+  }
 }
 
 // Coarse index of the lower of the two coarse cells a fine cell
@@ -2586,7 +2645,7 @@ static int rebuild_tables(Engine* E) {
   const size_t keep_ct = l0 < nl ? (size_t)E->h_meta[M_CT_OFF + l0] : E->h_ctiles.size();
   E->h_tiles.resize(keep_tiles);
   E->h_tileoff.resize(keep_tiles);
-  E->h_nbr.resize(keep_tiles);
+  E->h_nbr.resize((size_t)8 * keep_tiles);
   E->h_patchtab.resize(keep_pt);
   E->h_halo.resize(keep_halo);
   E->h_ctiles.resize(keep_ct);
@@ -2596,9 +2655,9 @@ static int rebuild_tables(Engine* E) {
     for (auto& b : E->lev[l].patches) {
       // tile .w = index of the patch in the all-level patch table
       tiles_of_box(b, l, (int)E->h_patchtab.size(), E->h_tiles);
-      nbr_of_box(b, E->h_nbr);
       E->h_patchtab.push_back(b);
     }
+    level_neighbours(E->h_tiles, E->lev[l].patches, E->tile_off[l], (int)E->h_tiles.size(), E->h_nbr);
     E->tile_cnt[l] = (int)E->h_tiles.size() - E->tile_off[l];
     E->patch_cnt[l] = (int)E->h_patchtab.size() - E->patch_off[l];
     E->h_meta[M_HALO_OFF + l] = (int)E->h_halo.size();
@@ -2676,7 +2735,7 @@ static int rebuild_tables(Engine* E) {
   grew |= E->d_patchtab.ensure(std::max<size_t>(E->h_patchtab.size(), 1));
   {
     const size_t nt = std::max<size_t>(E->h_tiles.size(), 1), rb = E->f32s ? 32 : 64;
-    grew |= E->d_nbr.ensure(nt);
+    grew |= E->d_nbr.ensure(8 * nt);
     grew |= E->d_skip.ensure(nt);
     grew |= E->d_rec_o1.ensure(nt * rb);
     grew |= E->d_rec_o2.ensure(nt * rb);
@@ -2711,7 +2770,7 @@ static int rebuild_tables(Engine* E) {
                k_ct = keep_dev ? keep_ct : 0, k_pt = keep_dev ? keep_pt : 0;
   // one pinned staging buffer for all tables, copied asynchronously; the
   // previous rebuild's copies must have left it before it is rewritten
-  const size_t b_nbr = (E->h_nbr.size() - k_tiles) * sizeof(int);
+  const size_t b_nbr = (E->h_nbr.size() - (size_t)8 * k_tiles) * sizeof(int);
   const size_t b_off = (E->h_tileoff.size() - k_tiles) * sizeof(long long),
                b_tiles = (E->h_tiles.size() - k_tiles) * sizeof(int4),
                b_halo = (E->h_halo.size() - k_halo) * sizeof(int4), b_ct = (E->h_ctiles.size() - k_ct) * sizeof(int4),
@@ -2738,7 +2797,7 @@ static int rebuild_tables(Engine* E) {
     h += n;
   };
   put(E->d_tileoff.p + k_tiles, E->h_tileoff.data() + k_tiles, b_off);
-  put(E->d_nbr.p + k_tiles, E->h_nbr.data() + k_tiles, b_nbr);
+  put(E->d_nbr.p + (size_t)8 * k_tiles, E->h_nbr.data() + (size_t)8 * k_tiles, b_nbr);
   put(E->d_tiles.p + k_tiles, E->h_tiles.data() + k_tiles, b_tiles);
   put(E->d_halo.p + k_halo, E->h_halo.data() + k_halo, b_halo);
   put(E->d_ctiles.p + k_ct, E->h_ctiles.data() + k_ct, b_ct);
