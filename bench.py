@@ -1193,7 +1193,7 @@ def run_linesource(args):
     # same three direct steps
     roof["other_kernels"] = other_kernels(kcls, 3, hbm_peak, peak_kind)
     roof["skip_kernels"] = {k: {"ms_per_step": kcls[k][0] / 3, "launches_per_step": kcls[k][2] / 3}
-                            for k in ("skip_lists", "skip_write", "stage_rest") if kcls.get(k, (0, 0, 0))[2]}
+                            for k in ("skip_lists", "stage_rest") if kcls.get(k, (0, 0, 0))[2]}
     # the FP32-storage engine: its own timed region (graph replay, regrids)
     secondary = None
     if wl32 is not None:

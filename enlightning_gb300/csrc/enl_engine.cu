@@ -291,6 +291,19 @@ struct StageArgs {
   void* rec_un_out;
   const int* gti;
   void* gcache;
+  // the skipped tiles, taken eight at a time (one per warp) by blocks that
+  // have run out of tiles to compute: their table indices (skip_n of them),
+  // the previous stage's records (their keys), and the list of those without
+  // a cached or published result (left_n, for a second launch)
+  const int* skip_gti;
+  const int* skip_n;
+  int* skip_counter;
+  const int4* tiles_all;  // the tile table (descriptors of the skipped tiles)
+  const void* rec_in;
+  const void* rec_un_in;
+  int* left_n;
+  int4* left_td;
+  int* left_gti;
 };
 
 // Shared-memory accessors centred on one cell of the staged halo tile.
@@ -556,6 +569,82 @@ __device__ __forceinline__ void record_out(OutRec<S>* ro, const W* wn, S pv, S t
   ro->v[5] = pv;
   ro->v[6] = tv;
   ro->valid = 1;
+}
+
+// The skipped tiles of a stage launch (stages 2 and 3 with skipping), taken
+// by blocks that have run out of tiles to compute, eight per claim, one per
+// warp: lanes 0..12 load the tile's key from the previous stage's records;
+// the block's cache entry for the level, or else the launch's published
+// result, with that key gives the outputs of every cell (stored eight rows of
+// 32, and recorded for the next stage), as a cache hit of the full path
+// would; a tile with neither goes to the list of the second launch.  Called
+// by the whole block after its last computed tile (all its copies landed).
+template <typename S>
+__device__ __noinline__ void skip_phase(const StageArgs& A, const UniEntry<S>* uc, unsigned* stats, int* s_claim) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ns = *A.skip_n;
+  const OutRec<S>* rin = static_cast<const OutRec<S>*>(A.rec_in);
+  const UnRec<S>* run = static_cast<const UnRec<S>*>(A.rec_un_in);
+  OutRec<S>* rout = static_cast<OutRec<S>*>(A.rec_out);
+  const GUni<S>* gc = static_cast<const GUni<S>*>(A.gcache);
+  for (;;) {
+    __syncthreads();  // (the claim slot is free)
+    if (tid == 0) s_claim[0] = atomicAdd(A.skip_counter, 8);
+    __syncthreads();
+    const int q = s_claim[0] + warp;
+    if (q - warp >= ns) break;
+    if (q >= ns) continue;
+    const int gi = A.skip_gti[q];
+    const int4 td = A.tiles_all[gi];
+    const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
+    S kv = S(0);
+    if (lane < 7) kv = rin[gi].v[lane];
+    else if (lane < 13) kv = run[gi].v[lane - 7];
+    // the block's cache entry first, then the published result (read after
+    // its completed state, past L1)
+    const UniEntry<S>& U = uc[lvl];
+    bool hit = __all_sync(0xffffffffu, U.valid != 0 && (lane >= 13 || same_bits(kv, U.key[lane])));
+    S rv = S(0);
+    int weno = 0;
+    if (hit) {
+      if (lane < 7) rv = U.res[lane];
+      weno = U.weno;
+    } else {
+      const GUni<S>* G = gc + lvl;
+      const int state = *reinterpret_cast<const volatile int*>(&G->state);
+      __threadfence();
+      const volatile S* gk = G->key;
+      hit = __all_sync(0xffffffffu, state == 2 && (lane >= 13 || same_bits(kv, (S)gk[lane])));
+      if (hit) {
+        if (lane < 7) rv = ((const volatile S*)G->res)[lane];
+        weno = *reinterpret_cast<const volatile int*>(&G->weno);
+      }
+    }
+    if (hit) {
+      S res[7];
+#pragma unroll
+      for (int k = 0; k < 7; ++k) res[k] = __shfl_sync(0xffffffffu, rv, k);
+      if (lane < w) {
+        S* o = static_cast<S*>(A.out[lvl]) + (long)(td.y + 3) * A.pitch[lvl] + (td.x + lane + 3);
+        for (int r = 0; r < h; ++r)
+#pragma unroll
+          for (int k = 0; k < kNF; ++k) o[k * A.fstride[lvl] + (long)r * A.pitch[lvl]] = res[k];
+      }
+      if (lane == 0) {
+        if (weno) atomicAdd(&stats[4 * lvl + 0], (unsigned)(w * h));
+        atomicAdd(&stats[4 * lvl + 1], (unsigned)(w * h));
+        atomicAdd(&stats[4 * lvl + 3], (unsigned)(w * h));
+      }
+      if (rout && lane < 8) {
+        if (lane < 7) rout[gi].v[lane] = rv;
+        else rout[gi].valid = 1;
+      }
+    } else if (lane == 0) {
+      const int k = atomicAdd(A.left_n, 1);
+      A.left_td[k] = td;
+      A.left_gti[k] = gi;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1089,19 +1178,20 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
     t = s_t[b ^ 1];
     b ^= 1;
   }
+  if (A.skip_gti) skip_phase<S>(A, s_uc, s_stats, s_t);
   if (tid == 0 && A.stats)
     for (int q = 0; q < 4 * kL; ++q)
       if (s_stats[q]) atomicAdd(&A.stats[q], (unsigned long long)s_stats[q]);
 }
 
 // ---------------------------------------------------------------------------
-// Uniform-tile skipping, stages 2 and 3: after skip_flags_kernel, one block
-// splits the tile table into the tiles to compute (their descriptors and
-// table indices, in table order, so the schedule's tile orders still apply)
-// and the tiles to skip; the stage launch computes the first list and
-// publishes its first uniform result per level; skip_write_kernel stores
-// that result into every skipped tile whose records carry the same key and
-// passes the others on to a second stage launch (usually empty).
+// Uniform-tile skipping, stages 2 and 3: after skip_flags_kernel, the tile
+// table is split into the tiles to compute (their descriptors and table
+// indices, in table order, so the schedule's tile orders still apply) and the
+// tiles to skip; the stage launch computes the first list, publishes its
+// first uniform result per level and stores the cached or published result
+// into the skipped tiles whose records carry the same key (skip_phase); the
+// others go to a second stage launch (usually empty).
 // counts: [0] tiles to compute, [1] tiles to skip, [2] passed on.
 // Block b (of the flag pass's blocks) writes the entries of its 256 tiles at
 // the offsets that the counts of the blocks before it give; block 0 also
@@ -1171,85 +1261,6 @@ __global__ void __launch_bounds__(kFlagThreads) skip_lists_kernel(const unsigned
     full_td[p] = tiles[t];
     full_gti[p] = t;
   }
-}
-
-template <typename S>
-struct SkipWriteArgs {
-  S* out[kL];
-  long pitch[kL], fstride[kL];
-  const int4* tiles;
-  const int* skip_gti;
-  int* counts;
-  const OutRec<S>* rin;
-  const UnRec<S>* run;
-  OutRec<S>* rout;  // stage 2: the output records (null in stage 3)
-  const GUni<S>* gcache;
-  int4* left_td;
-  int* left_gti;
-  unsigned long long* stats;
-};
-
-// One warp per skipped tile (a block takes eight at a time): lanes 0..12
-// load the tile's key (input record, u^n / H0 record) in one round and
-// compare it with the level's published uniform result (staged in shared
-// memory once per block); a match stores the result into every cell, eight
-// rows of 32 (and the tile's output record), as a cache hit of the stage
-// kernel would; otherwise the tile goes to the list of the second launch.
-template <typename S>
-__global__ void skip_write_kernel(SkipWriteArgs<S> A) {
-  __shared__ unsigned long long s_st[4 * kL];
-  __shared__ GUni<S> s_g[kL];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, wpb = blockDim.x >> 5;
-  if (tid < 4 * kL) s_st[tid] = 0ull;
-  for (int e = tid; e < (int)(kL * sizeof(GUni<S>) / sizeof(int)); e += blockDim.x)
-    reinterpret_cast<int*>(s_g)[e] = reinterpret_cast<const int*>(A.gcache)[e];
-  __syncthreads();
-  const int n = A.counts[1];
-  unsigned long long st_w[kL], st_c[kL];  // lane 0: this warp's counts
-#pragma unroll
-  for (int l = 0; l < kL; ++l) st_w[l] = st_c[l] = 0ull;
-  for (int q = blockIdx.x * wpb + warp; q < n; q += gridDim.x * wpb) {
-    const int gi = A.skip_gti[q];
-    const int4 td = A.tiles[gi];
-    S kv = S(0);
-    if (lane < 7) kv = A.rin[gi].v[lane];
-    else if (lane < 13) kv = A.run[gi].v[lane - 7];
-    const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
-    const GUni<S>& G = s_g[lvl];
-    const bool ok = lane >= 13 || same_bits(kv, G.key[lane]);
-    const bool match = __all_sync(0xffffffffu, ok) && G.state == 2;
-    if (match) {
-      if (lane < w) {
-        S* o = A.out[lvl] + (long)(td.y + 3) * A.pitch[lvl] + (td.x + lane + 3);
-        for (int r = 0; r < h; ++r)
-#pragma unroll
-          for (int k = 0; k < kNF; ++k) o[k * A.fstride[lvl] + (long)r * A.pitch[lvl]] = G.res[k];
-      }
-      if (lane == 0) {
-        st_w[lvl] += G.weno ? (unsigned long long)(w * h) : 0ull;
-        st_c[lvl] += (unsigned long long)(w * h);
-      }
-      if (A.rout && lane < 8) {
-        if (lane < 7) A.rout[gi].v[lane] = G.res[lane];
-        else A.rout[gi].valid = 1;
-      }
-    } else if (lane == 0) {
-      const int k = atomicAdd(&A.counts[2], 1);
-      A.left_td[k] = td;
-      A.left_gti[k] = gi;
-    }
-  }
-  if (lane == 0)
-#pragma unroll
-    for (int l = 0; l < kL; ++l) {
-      if (st_w[l]) atomicAdd(&s_st[4 * l + 0], st_w[l]);
-      if (st_c[l]) {
-        atomicAdd(&s_st[4 * l + 1], st_c[l]);
-        atomicAdd(&s_st[4 * l + 3], st_c[l]);
-      }
-    }
-  __syncthreads();
-  if (tid < 4 * kL && s_st[tid] && A.stats) atomicAdd(&A.stats[tid], s_st[tid]);
 }
 
 // ---------------------------------------------------------------------------
@@ -2323,13 +2334,13 @@ struct Engine {
   long long prof_launches = 0, prof_cells = 0;
   // per-class timing of the step's other kernels (profile 2): 0 interp,
   // 1 physical band fill, 2 coarsen, 3 CFL maximum (speed + dt), and with
-  // uniform-tile skipping 4 the flag pass and lists, 5 the writer of the
-  // skipped tiles, 6 the second stage launch
+  // uniform-tile skipping 4 the flag pass and lists, 5 the second stage
+  // launch
   static constexpr int kKev = 128;
   cudaEvent_t kev[2 * kKev] = {};
   int kev_cls[kKev] = {};
   int kev_n = 0;
-  static constexpr int kCls = 7;
+  static constexpr int kCls = 6;
   double kev_bytes[kKev] = {};
   double kcls_ms[kCls] = {};
   double kcls_bytes[kCls] = {};
@@ -3222,28 +3233,17 @@ static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) 
                                                  E->d_full_td.p, E->d_full_gti.p, E->d_skip_gti.p, E->d_skipcnt);
   kt_end(E, q);
   StageArgs A = A0;
+  A.skip_gti = E->d_skip_gti.p;
+  A.skip_n = E->d_skipcnt + 1;
+  A.skip_counter = E->d_counters + 6 + stage;
+  A.tiles_all = E->d_tiles.p;
+  A.rec_in = rin;
+  A.rec_un_in = run;
+  A.left_n = E->d_skipcnt + 2;
+  A.left_td = E->d_left_td.p;
+  A.left_gti = E->d_left_gti.p;
   void* args[] = {&A};
   cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), args, E->smem_bytes, s);
-  SkipWriteArgs<S> W;
-  memset(&W, 0, sizeof(W));
-  for (int l = 0; l < E->cfg.nlevels; ++l) {
-    W.out[l] = static_cast<S*>(A0.out[l]);
-    W.pitch[l] = A0.pitch[l];
-    W.fstride[l] = A0.fstride[l];
-  }
-  W.tiles = E->d_tiles.p;
-  W.skip_gti = E->d_skip_gti.p;
-  W.counts = E->d_skipcnt;
-  W.rin = rin;
-  W.run = run;
-  W.rout = static_cast<OutRec<S>*>(A0.rec_out);
-  W.gcache = static_cast<const GUni<S>*>(E->d_gcache);
-  W.left_td = E->d_left_td.p;
-  W.left_gti = E->d_left_gti.p;
-  W.stats = E->d_stats;
-  q = kt_begin(E, 5, 0.0);
-  skip_write_kernel<S><<<E->nsm * 4, 256, 0, s>>>(W);
-  kt_end(E, q);
   StageArgs B = A0;
   B.tiles = E->d_left_td.p;
   B.gti = E->d_left_gti.p;
@@ -3252,7 +3252,7 @@ static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) 
   B.counter64 = E->d_counters64 + 3 + stage;
   B.gcache = nullptr;
   void* bargs[] = {&B};
-  q = kt_begin(E, 6, 0.0);
+  q = kt_begin(E, 5, 0.0);
   cudaLaunchKernel((const void*)fn, dim3(E->stage_blocks), dim3(256), bargs, E->smem_bytes, s);
   kt_end(E, q);
 }
@@ -3867,7 +3867,7 @@ int enl_engine_launches_per_step(void* e, int plain) {
     // interpolation below level 1)
     const int refresh = E->samrai_order ? (nl - 1) + (nl > 2 ? nl - 2 : 0) : 0;
     return 3 * (bands + (nl - 1) + (E->samrai_order ? nl : 1) + refresh) + (nl - 1) + dt +
-           (skip_on(E) ? 8 : 0);  // stages 2 and 3: flags, lists, writer, second launch
+           (skip_on(E) ? 6 : 0);  // stages 2 and 3: flags, lists, second launch
   }
   const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;

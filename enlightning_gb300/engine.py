@@ -266,13 +266,13 @@ class Engine:
                    "enl_engine_profile")
         return ms.value, n.value, c.value
 
-    KERNEL_CLASSES = ("interp", "physbc", "coarsen", "cfl", "skip_lists", "skip_write", "stage_rest")
+    KERNEL_CLASSES = ("interp", "physbc", "coarsen", "cfl", "skip_lists", "stage_rest")
 
     def profile_kernels(self):
         """{class: (ms, algorithmic bytes, launches)} of the step's other
-        kernels under profile(2), since the last profile() call (the three
+        kernels under profile(2), since the last profile() call (the two
         skip classes are part of the stage figures; bytes 0)."""
-        ms, by, n = (C.c_double * 7)(), (C.c_double * 7)(), (C.c_longlong * 7)()
+        ms, by, n = (C.c_double * 6)(), (C.c_double * 6)(), (C.c_longlong * 6)()
         _lib.check(self.L.enl_engine_profile_kernels(self.h, ms, by, n), "enl_engine_profile_kernels")
         return {k: (ms[i], by[i], n[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 

@@ -330,12 +330,11 @@ int enl_engine_profile(void* engine, int on, double* ms_total,
                        long long* launches, long long* cells);
 
 /* Per-class figures of profile mode 2 since the last enl_engine_profile
- * call, seven entries each: 0 coarse-fine halo interpolation, 1 physical
+ * call, six entries each: 0 coarse-fine halo interpolation, 1 physical
  * band fill, 2 coarsening, 3 CFL maximum (speed + dt kernels), and with
  * uniform-tile skipping (schedule reuse 2, RK stages 2 and 3) 4 the flag
- * pass and tile lists, 5 the writer of the skipped tiles, 6 the second stage
- * launch (bytes 0 for these three; their time is also inside the stage
- * figures of enl_engine_profile).  bytes are
+ * pass and tile lists, 5 the second stage launch (bytes 0 for these two;
+ * their time is also inside the stage figures of enl_engine_profile).  bytes are
  * algorithmic: every cell value the launch must read or write, once
  * (interpolation: the halo cells written and the distinct coarse cells
  * under their 2 x 2 stencils; band fill: one read and one write per band
