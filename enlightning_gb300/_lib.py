@@ -67,7 +67,8 @@ ENGINE_SIGNATURES = {
     "enl_engine_graph_replay": (C.c_int, [C.c_void_p, C.c_int]),
     "enl_engine_tag": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "enl_engine_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
-    "enl_engine_skipped_tiles": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "enl_engine_skipped_tiles": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                           C.POINTER(C.c_longlong)]),
     "enl_engine_health": (C.c_int, [C.c_void_p]),
     "enl_engine_launches_per_step": (C.c_int, [C.c_void_p, C.c_int]),
     "enl_engine_paint_source": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,

@@ -3826,17 +3826,19 @@ int enl_engine_stats(void* e, long long* counts) {
   return check_launch("engine stats");
 }
 
-int enl_engine_skipped_tiles(void* e, long long* flagged, long long* tiles) {
+int enl_engine_skipped_tiles(void* e, long long* flagged, long long* written, long long* tiles) {
   Engine* E = (Engine*)e;
   if (!E || !flagged) return ENL_ERR_ARG;
   const size_t n = E->h_tiles.size();
   *flagged = 0;
+  if (written) *written = 0;
   if (tiles) *tiles = (long long)n;
   if (!skip_on(E) || n == 0) return ENL_OK;
   int h[3] = {0, 0, 0};
   cudaMemcpyAsync(h, E->d_skipcnt, sizeof(h), cudaMemcpyDeviceToHost, stream());
   cudaStreamSynchronize(stream());
-  *flagged = (long long)h[1] - h[2];  // written from a published result
+  *flagged = h[1];
+  if (written) *written = (long long)h[1] - h[2];
   return check_launch("engine skipped tiles");
 }
 

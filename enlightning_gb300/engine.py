@@ -237,10 +237,12 @@ class Engine:
         return a[: self.nlevels]
 
     def skipped_tiles(self):
-        """(tiles the last step's stage 3 took without their halo box, tiles)."""
-        f, n = C.c_longlong(), C.c_longlong()
-        _lib.check(self.L.enl_engine_skipped_tiles(self.h, C.byref(f), C.byref(n)), "enl_engine_skipped_tiles")
-        return f.value, n.value
+        """(tiles the last step's stage 3 flagged as uniform from the records,
+        of those stored without loading their halo box, tiles)."""
+        f, w, n = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        _lib.check(self.L.enl_engine_skipped_tiles(self.h, C.byref(f), C.byref(w), C.byref(n)),
+                   "enl_engine_skipped_tiles")
+        return f.value, w.value, n.value
 
     def health(self):
         return int(self.L.enl_engine_health(self.h))

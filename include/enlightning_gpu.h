@@ -269,11 +269,14 @@ int enl_engine_tag(void* engine, int level, int* tags);
  * uniform tiles whose outputs came from the block's cache (host array of
  * 4*ENL_MAX_LEVELS long long), then reset. */
 int enl_engine_stats(void* engine, long long* counts);
-/* Tiles the last step's RK stage 3 took without loading their halo box
- * (uniform-tile reuse 2: the records of stage 2 proved them uniform), and
- * the tiles of the hierarchy (tiles may be NULL).  Synchronises the library
- * stream.  0 when skipping is off. */
-int enl_engine_skipped_tiles(void* engine, long long* flagged, long long* tiles);
+/* Uniform-tile skipping in the last step's RK stage 3 (schedule reuse 2):
+ * tiles whose halo box the records of stage 2 proved uniform (flagged), of
+ * those the tiles stored from a cached or published result without loading
+ * their box (written; the others took the full path in a second launch,
+ * which happens when blocks reach them before any block has computed a
+ * tile with their key), and the tiles of the hierarchy.  written and tiles
+ * may be NULL.  Synchronises the library stream.  0 when skipping is off. */
+int enl_engine_skipped_tiles(void* engine, long long* flagged, long long* written, long long* tiles);
 /* Health word: 0, or the first code a kernel raised since the last call:
  * ENL_ERR_NONFINITE (rho <= 0 or non-finite state), ENL_ERR_TIMEOUT (a
  * bounded wait gave up), ENL_ERR_STATE (a TMA precondition failed and the

@@ -103,9 +103,9 @@ def test_autotune_leaves_the_state_and_is_no_slower_than_default(tmp_path):
 @pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32_STATE])
 def test_skipping_uniform_tiles_changes_nothing(precision):
     """Reuse 2 takes the tiles that the previous stage's records prove
-    uniform without loading their halo boxes; a line source run (regrids
-    included) and an ambient hierarchy step bit for bit as with reuse 1 and
-    0, and the ambient run skips most of its tiles."""
+    uniform without loading their halo boxes (or, when no block has computed
+    their key yet, in a second launch over the full path); a line source run
+    with a regrid steps bit for bit as with reuse 1 and 0, and flags tiles."""
     results = {}
     for reuse in (2, 1, 0):
         E, H, _ = small_line_source(precision)
@@ -116,8 +116,9 @@ def test_skipping_uniform_tiles_changes_nothing(precision):
             E.step(1.0)
         torch.cuda.synchronize()
         assert E.health() == 0
-        skipped, tiles = E.skipped_tiles()
-        results[reuse] = (states(E), E.time(), E.stats(), skipped, tiles)
+        flagged, written, tiles = E.skipped_tiles()
+        assert 0 <= written <= flagged <= tiles
+        results[reuse] = (states(E), E.time(), E.stats(), flagged, tiles, written)
         E.close()
     for reuse in (1, 0):
         assert results[reuse][1] == results[2][1]
@@ -125,5 +126,6 @@ def test_skipping_uniform_tiles_changes_nothing(precision):
             assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a,
                                   b.view(np.int64) if b.dtype == np.float64 else b), reuse
     assert results[1][3] == 0 and results[0][3] == 0
-    print("line source: stage 3 skipped", results[2][3], "of", results[2][4], "tiles")
+    print("line source: stage 3 flagged", results[2][3], "of", results[2][4], "tiles,", results[2][5],
+          "stored without their box")
     assert results[2][3] > 0
