@@ -114,6 +114,8 @@ ENGINE_SIGNATURES = {
     "enl_engine_sync": (C.c_int, [C.c_void_p]),
     "enl_check_bounded_wait": (C.c_int, [C.c_int, C.c_int]),
     "enl_mlp_erf_error": (C.c_int, [C.POINTER(C.c_double)]),
+    "enl_tile_neighbours": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.POINTER(C.c_int)]),
     "enl_halo_segments": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
                                     C.POINTER(C.c_int)]),
     "enl_measure_fp_peaks": (C.c_int, [C.POINTER(C.c_double), C.c_int]),

@@ -4229,6 +4229,37 @@ int enl_halo_segments(const int* boxes, int nbox, int nx, int ny, int* segs, int
   return ENL_OK;
 }
 
+int enl_tile_neighbours(const int* boxes, int nbox, int* tiles, int* nbr, int max_tiles, int* ntiles) {
+  if (nbox < 0 || (nbox > 0 && !boxes) || max_tiles < 0 || (max_tiles > 0 && (!tiles || !nbr)) || !ntiles) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  std::vector<int4> P(nbox), T;
+  for (int q = 0; q < nbox; ++q) {
+    P[q] = make_int4(boxes[4 * q], boxes[4 * q + 1], boxes[4 * q + 2], boxes[4 * q + 3]);
+    if (P[q].y < P[q].x || P[q].w < P[q].z) {
+      set_error(ENL_ERR_ARG);
+      return ENL_ERR_ARG;
+    }
+    tiles_of_box(P[q], 0, q, T);
+  }
+  std::vector<int> N;
+  level_neighbours(T, P, 0, (int)T.size(), N);
+  *ntiles = (int)T.size();
+  if ((int)T.size() > max_tiles) {
+    set_error(ENL_ERR_ARG);
+    return ENL_ERR_ARG;
+  }
+  for (size_t t = 0; t < T.size(); ++t) {
+    tiles[4 * t] = T[t].x;
+    tiles[4 * t + 1] = T[t].y;
+    tiles[4 * t + 2] = (T[t].z >> 8) & 0xff;
+    tiles[4 * t + 3] = (T[t].z >> 16) & 0xff;
+    for (int m = 0; m < 8; ++m) nbr[8 * t + m] = N[8 * t + m];
+  }
+  return ENL_OK;
+}
+
 int enl_check_bounded_wait(int polls, int arrive) {
   if (polls < 1) {
     set_error(ENL_ERR_ARG);

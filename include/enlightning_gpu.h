@@ -522,6 +522,18 @@ int enl_measure_fp_peaks(double* out, int n);
 int enl_halo_segments(const int* boxes, int nbox, int nx, int ny, int* segs,
                       int max_segs, int* nseg);
 
+/* Host-side: the 32x8 stage tiles of one level's patches (nbox boxes ilo,
+ * ihi, jlo, jhi; per patch row-major from its corner) and, per tile, the
+ * table indices of the eight tiles whose interiors hold its 3-cell halo
+ * ring, as the uniform-tile skipping uses them (above left, above, above
+ * right, left, right, below left, below, below right), or -1 in the first
+ * slot when the engine does not skip that tile.  tiles receives (i0, j0,
+ * width, height) per tile, nbr 8 ints per tile; at most max_tiles tiles, the
+ * count needed in ntiles (ENL_ERR_ARG when that exceeds max_tiles).  No GPU
+ * involved. */
+int enl_tile_neighbours(const int* boxes, int nbox, int* tiles, int* nbr, int max_tiles,
+                        int* ntiles);
+
 /* ---------------------------------------------------------------------------
  * Allocation-free stable time step of one patch.  No counterpart in the
  * reference (its dt, enlightning.C:433-456, needs no reduction); it is for
