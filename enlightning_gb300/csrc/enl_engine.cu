@@ -282,12 +282,13 @@ struct StageArgs {
   float margin;               // |p - 0.5| <= margin -> plain sensor decides
   float feat_eps, feat_eps_p, feat_inv_sqrt_eps;
   // uniform-tile skipping (null when off).  Records of the current step,
-  // per table index: stages 1 and 2 write rec_out for the next stage.  The
-  // launch runs over a list of tiles: tiles holds their descriptors, gti
-  // their table indices (null: the table itself), and the first uniform tile
-  // computed per level is published in gcache (GUni<S>[kL]) for the skipped
-  // tiles.
+  // per table index: stage 1 writes rec_un_out and rec_out, stage 2 writes
+  // rec_out.  In stages 2 and 3 the launch runs over a list of tiles: tiles
+  // holds their descriptors, gti their table indices (null: the table
+  // itself), and the first uniform tile computed per level is published in
+  // gcache (GUni<S>[kL]) for the writer of the skipped tiles.
   void* rec_out;
+  void* rec_un_out;
   const int* gti;
   void* gcache;
   // the skipped tiles, taken eight at a time (one per warp) by blocks that
@@ -371,17 +372,16 @@ __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_
 
 // Records of one step for skipping uniform tiles.  Within a step nothing but
 // the stage kernels writes patch interiors (ghost fills write ghosts, the
-// coarsening follows the last stage), so what a pass over the data records
-// before stage 1, and what stages 1 and 2 record about the tiles they wrote,
-// still holds when the next stage reads it:
-//   OutRec: the tile's interior, when every cell holds the same 7 values
-//           (the step's input, or a uniform tile's outputs);
+// coarsening follows the last stage), so what stage 1 and stage 2 record
+// about the tiles they wrote still holds when the next stage reads it:
+//   OutRec: the tile's stored outputs, when every cell of the tile holds the
+//           same 7 values (a uniform tile, from the cache or computed);
 //   UnRec:  the tile's u^n (5 fields) and H0, when uniform over its cells and
-//           the tile lies in no absorbing band (the pass before stage 1).
-// A tile whose own input record and its eight neighbours' (tiles whose
-// interiors hold its halo ring) carry the same values has a uniform halo box
-// with those values: with a matching cached or published result its outputs
-// are that result, and the box is not loaded.
+//           the tile lies in no absorbing band (from stage 1's uniform test).
+// A tile of stage 2 or 3 whose own input record and its eight neighbours'
+// (all in its patch, each reaching at least 3 cells into the halo) hold the
+// same values has a uniform halo box with those values: with a matching
+// cache entry its outputs are the entry's, and the box is not loaded.
 template <typename S>
 struct alignas(16) OutRec {
   S v[7];
@@ -834,8 +834,15 @@ __global__ void __launch_bounds__(256, std::is_same<S, float>::value ? kStageBlo
                                                                  un_c[3], un_c[4], h0_c);
       const bool all = __syncthreads_and(ok) != 0;  // (also publishes s_tile and s_wl)
       if (all && s_tile.absorb == 0) ucode = uniform_hit<S, kPl>(A, box, s_uc, s_wl, s_stats, lvl, i0, j0, w, h);
-      // this step's record of the tile's outputs (a computed uniform tile,
-      // ucode 2, records them where its first cell records the cache entry)
+      // this step's records of the tile (a computed uniform tile, ucode 2,
+      // records its outputs where its first cell records the cache entry)
+      if (tid == 0 && A.rec_un_out) {
+        UnRec<S>* rn = static_cast<UnRec<S>*>(A.rec_un_out) + gti;
+        if (ucode != 0)
+#pragma unroll
+          for (int k = 0; k < 6; ++k) rn->v[k] = uni_key<S, kPl>(box, s_wl[0], A.un_is_in, 7 + k);
+        rn->valid = ucode != 0 ? 1 : 0;
+      }
       if (tid == 0 && A.rec_out && ucode != 2) {
         OutRec<S>* ro = static_cast<OutRec<S>*>(A.rec_out) + gti;
         if (ucode == 1)
@@ -1253,64 +1260,6 @@ __global__ void __launch_bounds__(kFlagThreads) skip_lists_kernel(const unsigned
     const int p = of + pf + __popc(bf & lt);
     full_td[p] = tiles[t];
     full_gti[p] = t;
-  }
-}
-
-// Stage 1's records, from the data: one warp per tile reads its interior (7
-// fields and H0, eight rows of up to 32 lanes) and records whether every cell
-// holds the first cell's values (OutRec: the 7 values; UnRec: u^n, which in
-// stage 1 is the input itself, and H0, valid when the tile also lies in no
-// absorbing band, as the stage kernel's uniform test requires).
-template <typename S>
-struct RecordArgs {
-  const S* lev[kL];
-  const S* h0[kL];
-  long pitch[kL], fstride[kL];
-  const int4* tiles;
-  const int* ntiles;
-  const int4* patchtab;
-  AbsorbTables absorb;
-  bool any_absorb;
-  OutRec<S>* rout;
-  UnRec<S>* run;
-};
-template <typename S>
-__global__ void uniform_records_kernel(RecordArgs<S> A) {
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  const int n = *A.ntiles;
-  for (int t = blockIdx.x * wpb + (threadIdx.x >> 5); t < n; t += gridDim.x * wpb) {
-    const int4 td = A.tiles[t];
-    const int lvl = td.z & 0xff, w = (td.z >> 8) & 0xff, h = (td.z >> 16) & 0xff;
-    const S* base = A.lev[lvl] + (long)(td.y + 3) * A.pitch[lvl] + (td.x + 3);
-    const S* hb = A.h0[lvl] + (long)(td.y + 3) * A.pitch[lvl] + (td.x + 3);
-    const long fs = A.fstride[lvl], pt = A.pitch[lvl];
-    S first[7];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) first[k] = base[k * fs];
-    const S hfirst = hb[0];
-    bool same = true, hsame = true;
-    if (lane < w) {
-      for (int r = 0; r < h; ++r) {
-#pragma unroll
-        for (int k = 0; k < 7; ++k) same = same && same_bits(base[k * fs + r * pt + lane], first[k]);
-        hsame = hsame && same_bits(hb[r * pt + lane], hfirst);
-      }
-    }
-    same = __all_sync(0xffffffffu, same);
-    hsame = __all_sync(0xffffffffu, hsame);
-    // lane k < 7 writes field k of the output record, lane 8 + k (k < 6) entry
-    // k of the u^n / H0 record; lanes 7 and 14 the valid words
-    S v = hfirst;  // (lane 13: H0)
-#pragma unroll
-    for (int k = 0; k < 7; ++k)
-      if (lane == k || (k < 5 && lane == 8 + k)) v = first[k];
-    if (lane < 7) A.rout[t].v[lane] = v;
-    else if (lane == 7) A.rout[t].valid = same ? 1 : 0;
-    else if (lane < 14) A.run[t].v[lane - 8] = v;
-    else if (lane == 14) {
-      const int absorb = A.any_absorb ? absorb_tile_mask(A.absorb, lvl, td.x, td.y, w, h, A.patchtab[td.w]) : 0;
-      A.run[t].valid = (same && hsame && absorb == 0) ? 1 : 0;
-    }
   }
 }
 
@@ -2447,7 +2396,7 @@ struct Engine {
   int skip = 1;
   DevArray<int> d_nbr;
   std::vector<int> h_nbr;
-  DevArray<unsigned char> d_rec_o0, d_rec_o1, d_rec_o2, d_rec_un, d_skip;
+  DevArray<unsigned char> d_rec_o1, d_rec_o2, d_rec_un, d_skip;
   DevArray<int2> d_bcnt;                       // per flag-pass block: tiles to compute, to skip
   DevArray<int4> d_full_td, d_left_td;         // descriptors of the tiles to compute / passed on
   DevArray<int> d_full_gti, d_skip_gti, d_left_gti;
@@ -2799,7 +2748,6 @@ static int rebuild_tables(Engine* E) {
     const size_t nt = std::max<size_t>(E->h_tiles.size(), 1), rb = E->f32s ? 32 : 64;
     grew |= E->d_nbr.ensure(8 * nt);
     grew |= E->d_skip.ensure(nt);
-    grew |= E->d_rec_o0.ensure(nt * rb);
     grew |= E->d_rec_o1.ensure(nt * rb);
     grew |= E->d_rec_o2.ensure(nt * rb);
     grew |= E->d_rec_un.ensure(nt * rb);
@@ -2813,7 +2761,7 @@ static int rebuild_tables(Engine* E) {
     grew |= E->d_bcnt.ensure((E->d_skip.cap + kFlagThreads - 1) / kFlagThreads);
   }
   if (grew) E->graph_valid = false;
-  if (!E->d_nbr.p || !E->d_skip.p || !E->d_rec_o0.p || !E->d_rec_o1.p || !E->d_rec_o2.p || !E->d_rec_un.p || !E->d_full_td.p ||
+  if (!E->d_nbr.p || !E->d_skip.p || !E->d_rec_o1.p || !E->d_rec_o2.p || !E->d_rec_un.p || !E->d_full_td.p ||
       !E->d_left_td.p || !E->d_full_gti.p || !E->d_skip_gti.p || !E->d_left_gti.p || !E->d_bcnt.p) {
     E->tables_on_device = false;
     E->graph_valid = false;
@@ -2993,15 +2941,19 @@ static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   A.feat_eps_p = (float)(A.P[0].sensor_eps * (c.c * c.c) * (c.c * c.c));
   A.feat_inv_sqrt_eps = (float)(1.0 / sqrt(A.P[0].sensor_eps));
   if (skip_on(E)) {
-    // every stage runs over the list of tiles to compute (skip_stage_t) and
-    // publishes its uniform results for the skipped ones; stages 1 and 2
-    // record their outputs for the next stage (stage 1's input records come
-    // from a pass over the data, uniform_records_kernel)
-    A.rec_out = stage == 0 ? E->d_rec_o1.p : (stage == 1 ? E->d_rec_o2.p : nullptr);
-    A.tiles = E->d_full_td.p;
-    A.gti = E->d_full_gti.p;
-    A.ntiles = E->d_skipcnt;
-    A.gcache = E->d_gcache;
+    // stage 1 records its outputs and u^n / H0, stage 2 its outputs; stages
+    // 2 and 3 run over the list of tiles to compute (skip_stage_t) and
+    // publish their uniform results for the writer of the skipped ones
+    if (stage == 0) {
+      A.rec_out = E->d_rec_o1.p;
+      A.rec_un_out = E->d_rec_un.p;
+    } else {
+      A.rec_out = stage == 1 ? E->d_rec_o2.p : nullptr;
+      A.tiles = E->d_full_td.p;
+      A.gti = E->d_full_gti.p;
+      A.ntiles = E->d_skipcnt;
+      A.gcache = E->d_gcache;
+    }
   }
   return A;
 }
@@ -3263,40 +3215,18 @@ static void record_mics(Engine* E) {
   else mics_t<double>(E);
 }
 
-// RK stage `stage` (0, 1 or 2) with skipping: the input records (for stage
-// 0 a pass over the data, else the previous stage's), flags and lists, the
-// launch over the tiles to compute (its blocks then store the skipped tiles),
-// and a launch over the skipped tiles without a cached or published result
-// (usually none).
+// Stage `stage` (1 or 2) with skipping: flags and lists from the previous
+// stage's records, the launch over the tiles to compute, the writer of the
+// skipped tiles, and a launch over the skipped tiles without a published
+// result (usually none).
 template <typename S>
 static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) {
   cudaStream_t s = stream();
-  const unsigned char* rb = stage == 0 ? E->d_rec_o0.p : (stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p);
-  const OutRec<S>* rin = reinterpret_cast<const OutRec<S>*>(rb);
+  const OutRec<S>* rin = reinterpret_cast<const OutRec<S>*>(stage == 1 ? E->d_rec_o1.p : E->d_rec_o2.p);
   const UnRec<S>* run = reinterpret_cast<const UnRec<S>*>(E->d_rec_un.p);
   const int nbk = (int)E->d_bcnt.cap;
   cudaMemsetAsync(E->d_gcache, 0, kL * sizeof(GUni<S>), s);
   int q = kt_begin(E, 4, 0.0);
-  if (stage == 0) {
-    // stage 1's input records (and the u^n / H0 records of the step) from
-    // the data
-    RecordArgs<S> R;
-    memset(&R, 0, sizeof(R));
-    for (int l = 0; l < E->cfg.nlevels; ++l) {
-      R.lev[l] = static_cast<const S*>(A0.in[l]);
-      R.h0[l] = static_cast<const S*>(A0.h0[l]);
-      R.pitch[l] = A0.pitch[l];
-      R.fstride[l] = A0.fstride[l];
-    }
-    R.tiles = E->d_tiles.p;
-    R.ntiles = E->d_meta + M_NTILES;
-    R.patchtab = E->d_patchtab.p;
-    R.absorb = A0.absorb;
-    R.any_absorb = A0.any_absorb;
-    R.rout = reinterpret_cast<OutRec<S>*>(E->d_rec_o0.p);
-    R.run = reinterpret_cast<UnRec<S>*>(E->d_rec_un.p);
-    uniform_records_kernel<S><<<E->nsm * 8, 256, 0, s>>>(R);
-  }
   skip_flags_kernel<S><<<nbk, kFlagThreads, 0, s>>>(E->d_nbr.p, E->d_meta + M_NTILES, rin, run, E->d_skip.p,
                                                      E->d_bcnt.p);
   skip_lists_kernel<<<nbk, kFlagThreads, 0, s>>>(E->d_skip.p, E->d_meta + M_NTILES, E->d_bcnt.p, E->d_tiles.p,
@@ -3363,7 +3293,7 @@ static int step_fused(Engine* E, double dt) {
     StageArgs A = stage_args(E, st, dt);
     void* args[] = {&A};
     if (E->profile) cudaEventRecord(E->pev[2 * st], s);
-    if (skip_on(E)) {
+    if (st > 0 && skip_on(E)) {
       if (E->f32s) skip_stage_t<float>(E, st, fn, A);
       else skip_stage_t<double>(E, st, fn, A);
     } else {
@@ -3939,7 +3869,7 @@ int enl_engine_launches_per_step(void* e, int plain) {
     // interpolation below level 1)
     const int refresh = E->samrai_order ? (nl - 1) + (nl > 2 ? nl - 2 : 0) : 0;
     return 3 * (bands + (nl - 1) + (E->samrai_order ? nl : 1) + refresh) + (nl - 1) + dt +
-           (skip_on(E) ? 10 : 0);  // per stage flags, lists, second launch; stage 1's records
+           (skip_on(E) ? 6 : 0);  // stages 2 and 3: flags, lists, second launch
   }
   const int absorbs = any_absorb(E) ? 1 : 0;
   int npatch = 0, copies = 0;

@@ -335,8 +335,8 @@ int enl_engine_profile(void* engine, int on, double* ms_total,
 /* Per-class figures of profile mode 2 since the last enl_engine_profile
  * call, six entries each: 0 coarse-fine halo interpolation, 1 physical
  * band fill, 2 coarsening, 3 CFL maximum (speed + dt kernels), and with
- * uniform-tile skipping (schedule reuse 2) 4 the record pass before stage
- * 1, the flag passes and tile lists, 5 the second stage launches (bytes 0 for these two;
+ * uniform-tile skipping (schedule reuse 2, RK stages 2 and 3) 4 the flag
+ * pass and tile lists, 5 the second stage launch (bytes 0 for these two;
  * their time is also inside the stage figures of enl_engine_profile).  bytes are
  * algorithmic: every cell value the launch must read or write, once
  * (interpolation: the halo cells written and the distinct coarse cells
@@ -360,10 +360,9 @@ int enl_engine_set_level_order(void* engine, int samrai);
  * and the schedule decides how its blocks take the tiles.
  *   sched[0] resident blocks per SM (0 = the occupancy limit),
  *   sched[1] tile order (as enl_engine_config.tile_order),
- *   sched[2] uniform-tile reuse: 2 on (the default), with every RK stage
+ *   sched[2] uniform-tile reuse: 2 on (the default), with RK stages 2 and 3
  *            skipping the halo box of a tile whose own and neighbours'
- *            records (for stage 1 from a pass over the step's input, else
- *            from the previous stage) prove it uniform;
+ *            records from the previous stage of the step prove it uniform;
  *            1 on, every tile's box loaded and tested; 0 off (as
  *            enl_engine_config.dense = 1),
  *   sched[3] run length: tiles a block claims at a time (1..16; consecutive
