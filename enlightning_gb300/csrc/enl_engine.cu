@@ -286,7 +286,7 @@ struct StageArgs {
   // rec_out.  In stages 2 and 3 the launch runs over a list of tiles: tiles
   // holds their descriptors, gti their table indices (null: the table
   // itself), and the first uniform tile computed per level is published in
-  // gcache (GUni<S>[kL]) for the writer of the skipped tiles.
+  // gcache (GUni<S>[kL]) for the skipped tiles (skip_phase).
   void* rec_out;
   void* rec_un_out;
   const int* gti;
@@ -539,9 +539,9 @@ __device__ __noinline__ void uniform_record(UniEntry<S>* U, const S* box, const 
 }
 
 // The first uniform tile a stage launch computes on a level publishes its
-// inputs and outputs (the block-cache entry it just filled) for the writer
-// of the skipped tiles, which runs after the launch: state 0 empty, 1 being
-// written, 2 complete.
+// inputs and outputs (the block-cache entry it just filled) for the skipped
+// tiles that blocks without that entry take at the end of the launch: state
+// 0 empty, 1 being written, 2 complete.
 template <typename S>
 struct GUni {
   S key[13];
@@ -2943,7 +2943,7 @@ static StageArgs stage_args(Engine* E, int stage, double dt, int level = -1) {
   if (skip_on(E)) {
     // stage 1 records its outputs and u^n / H0, stage 2 its outputs; stages
     // 2 and 3 run over the list of tiles to compute (skip_stage_t) and
-    // publish their uniform results for the writer of the skipped ones
+    // publish their uniform results for the skipped ones
     if (stage == 0) {
       A.rec_out = E->d_rec_o1.p;
       A.rec_un_out = E->d_rec_un.p;
@@ -3215,10 +3215,10 @@ static void record_mics(Engine* E) {
   else mics_t<double>(E);
 }
 
-// Stage `stage` (1 or 2) with skipping: flags and lists from the previous
-// stage's records, the launch over the tiles to compute, the writer of the
-// skipped tiles, and a launch over the skipped tiles without a published
-// result (usually none).
+// RK stage `stage` (1 or 2) with skipping: flags and lists from the previous
+// stage's records, the launch over the tiles to compute (its blocks then
+// store the skipped tiles, skip_phase), and a launch over the skipped tiles
+// without a cached or published result (usually none).
 template <typename S>
 static void skip_stage_t(Engine* E, int stage, StageFn fn, const StageArgs& A0) {
   cudaStream_t s = stream();
