@@ -2985,12 +2985,14 @@ static StageFn pick_stage(int precision, int variant) {
 // with the launch's algorithmic bytes (each cell value read or written once).
 static int kt_begin(Engine* E, int cls, double bytes) {
   if (E->profile < 2 || E->kev_n >= Engine::kKev) return -1;
-  const int q = E->kev_n++;
-  if (!E->kev[2 * q] && (cudaEventCreate(&E->kev[2 * q]) != cudaSuccess ||
-                         cudaEventCreate(&E->kev[2 * q + 1]) != cudaSuccess)) {
-    E->kev_n = q;
-    return -1;
-  }
+  const int q = E->kev_n;
+  for (int k = 0; k < 2; ++k)
+    if (!E->kev[2 * q + k] && cudaEventCreate(&E->kev[2 * q + k]) != cudaSuccess) {
+      E->kev[2 * q + k] = nullptr;
+      cudaGetLastError();
+      return -1;
+    }
+  E->kev_n = q + 1;
   E->kev_cls[q] = cls;
   E->kev_bytes[q] = bytes;
   cudaEventRecord(E->kev[2 * q], stream());
@@ -3375,6 +3377,7 @@ static int step_plain(Engine* E, double dt) {
                                                                E->d_tiles.p, E->tile_off[l], E->tile_cnt[l]);
   coarsen_all(E);
   record_mics(E);
+  if (E->profile >= 2) kt_collect(E);  // the other kernels' events of this step
   return check_launch("engine plain step");
 }
 
